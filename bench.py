@@ -1,0 +1,396 @@
+#!/usr/bin/env python3
+"""Throughput of the SPH time step on GB300: Mparticle-steps/s.
+
+Workload (N=1): the 4,000,000-point wave tank -- a jittered lattice filling
+the low-x 40% of a ~330-unit box, dam-break parameters (h = 0.01 m, cell 2h,
+gridSrch 2), X- wall forcing at frequency 0.2 and amplitude 0.3. One step
+is one full Run: insert, scan, index scatter, canonical sort + gather,
+density, force + advance (six kernels).
+
+  value   device-timed throughput, state resident in HBM, graph replay of
+          exactly K steps between CUDA events on the system stream
+  e2e     the same metric through the public C ABI with host buffers: per
+          step, pinned host -> device upload of the step's inputs
+          (fl_set_particles), fl_run, device -> host read of the positions
+  roofline  the dominant kernel's algorithmic bytes per launch / its mean
+          launch time (per-phase CUDA events over a second K-step region)
+  cpu_baseline  the reference's CPU path (the reference kernels built for the
+          host where available, else the oracle port) on a bounded sample
+
+--impl reference prints the reference arm instead (CPU, all host threads).
+Multi-GPU (torchrun): every rank steps its own replica (no exchange), the
+slowest rank's time sets the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mparticle-steps/s"
+# Algorithmic bytes per point per kernel: each input read once, each output
+# written once (canonical figures; grid terms per cell are added separately).
+ALGO_BYTES = {
+    "insert": 20,          # R pos 12, W cell + rank 8
+    "scan": 0,             # per cell: R 4, W 4 (+ clear 4) -> 12 B/cell
+    "scatter": 12,         # R cell + rank 8, W src 4
+    "sort": 92,            # R pos, vel, veval, clr, gcell, gndx; W pos, vel, veval, clr, gcell
+    "density": 16,         # R pos 12, W density 4
+    "force_advance": 128,  # force 40 (R pos, veval, density; W F) + advance 88
+}
+KERNELS_PER_STEP = 6
+
+
+def parse():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=4_000_000, help="points in the wave tank")
+    ap.add_argument("--e2e-steps", type=int, default=None, help="steps in the e2e region (default: min(K, 20))")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 100 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "100",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return self
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append((time.perf_counter(), [x.strip() for x in line.split(",")]))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+
+    def summary(self, t0: float, t1: float) -> dict:
+        rows = [r for t, r in self.samples if t0 - 0.15 <= t <= t1 + 0.15 and len(r) >= 9]
+        if not rows:
+            rows = [r for _, r in self.samples if len(r) >= 9][-3:]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": num(rows[0][2]), "reasons": reasons, "samples": len(rows),
+                "power_w_max": max((num(r[3]) or 0.0) for r in rows)}
+
+
+def measured_peak():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            d = json.loads(f.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except (ValueError, KeyError):
+            pass
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    f = ROOT / "profiles" / "traffic.json"
+    if not f.exists():
+        return None
+    try:
+        return json.loads(f.read_text()).get(kernel, {}).get("dram_bytes_per_launch")
+    except ValueError:
+        return None
+
+
+# ---------------------------------------------------------------------------
+def cpu_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_reference_rate(scene, budget_s: float, threads: int):
+    """Particle-steps/s of the reference's CPU path on a sample of `scene`:
+    the first points of the scene in fill order (its bottom layers, same box
+    and grid), sized so the sample runs about `budget_s` seconds."""
+    from oracle import oracle as O
+
+    kind = "reference" if O.ref_available() else "port"
+    p = scene.params
+
+    def run(n, steps):
+        pos, vel, veval, clr = scene.pos[:n], scene.vel[:n], scene.veval[:n], scene.clr[:n]
+        if kind == "reference":
+            R = O.RefKernels(p, pos, vel, veval, clr)
+            t0 = time.perf_counter()
+            R.run(steps, 0.0, threads=threads)
+        else:
+            st = O.State.new(p, pos, vel, veval, clr)
+            t0 = time.perf_counter()
+            O.run(p, st, steps, 0.0, threads=threads)
+        return time.perf_counter() - t0
+
+    n = min(scene.n, 250_000)
+    dt1 = run(n, 1)
+    per_point = max(dt1 / n, 1e-9)
+    steps = 2
+    n = int(min(scene.n, max(10_000, budget_s / (steps * per_point))))
+    el = run(n, steps)
+    return {"value": n * steps / el / 1e6, "unit": METRIC, "cores": threads, "kind": kind,
+            "sample": f"{steps} full steps over the first {n:,} of the {scene.n:,} points (same box, grid "
+                      f"and parameters), {el:.1f} s, {threads} host threads"}, el
+
+
+def reference_arm(args, rank, world):
+    """The reference's CPU implementation of the step on this machine's host cores.
+    A step is one full step over a bounded sample of the workload -- its first
+    points in fill order, same box, grid and parameters -- sized so that the
+    W + K steps take about two minutes."""
+    if rank != 0:
+        return
+    from fluids3_gb300 import scenes
+    from oracle import oracle as O
+
+    scene = scenes.wave_tank(n=args.n)
+    p = scene.params
+    threads = cpu_threads()
+    kind = "reference" if O.ref_available() else "port"
+
+    def make(n):
+        a = (scene.pos[:n], scene.vel[:n], scene.veval[:n], scene.clr[:n])
+        return O.RefKernels(p, *a) if kind == "reference" else O.State.new(p, *a)
+
+    def steps(obj, k, t):
+        return obj.run(k, t, threads=threads) if kind == "reference" else O.run(p, obj, k, t, threads=threads)
+
+    calib_n = min(scene.n, 100_000)
+    obj = make(calib_n)
+    c0 = time.perf_counter()
+    steps(obj, 1, 0.0)
+    per_point = max((time.perf_counter() - c0) / calib_n, 1e-9)
+    total = args.steps + max(args.warmup, 0)
+    n = int(min(scene.n, max(10_000, 120.0 / (max(total, 1) * per_point))))
+    obj = make(n)
+    t = steps(obj, max(args.warmup, 0), 0.0)
+    t0 = time.perf_counter()
+    steps(obj, args.steps, t)
+    el = time.perf_counter() - t0
+    value = n * args.steps / el / 1e6
+    info = {"value": value, "unit": METRIC, "cores": threads, "kind": kind,
+            "sample": f"each step: one full step over the first {n:,} of the {scene.n:,} points (same box, "
+                      f"grid, parameters); {args.steps} timed steps in {el:.1f} s on {threads} host threads"}
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / max(args.steps, 1) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": config_of(scene, args), "cpu_baseline": info,
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_of(scene, args):
+    p = scene.params
+    return {"workload": f"{scene.name}: {scene.n:,}-point SPH wave tank (dam break with X- wall forcing, "
+                        f"freq {p.bound_wall_freq:g}, amplitude {p.bound_wall_force:g}), cell 2h, gridSrch {p.gridSrch}",
+            "n_points": scene.n, "cells": p.gridTotal, "grid": list(p.gridRes),
+            "l2": "inputs larger than L2 (state ~1 GB in HBM), no flush needed",
+            "step": "insert, scan, index scatter, canonical sort+gather, density, force+advance"}
+
+
+# ---------------------------------------------------------------------------
+def our_arm(args, rank, world, local_rank):
+    import ctypes as C
+
+    import fluids3_gb300 as F
+    from fluids3_gb300 import scenes
+
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(local_rank)
+        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist = tdist
+    else:
+        try:
+            import torch
+            if torch.cuda.is_available():
+                torch.cuda.set_device(local_rank)
+        except ImportError:
+            pass
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    def allmax(x: float) -> float:
+        if not dist:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    scene = scenes.wave_tank(n=args.n)
+    p = scene.params
+    s = F.FluidSystem(p, scene.n)
+    s.SetParticles(scene.pos, scene.vel, scene.veval, clr=scene.clr)
+
+    # warm-up (untimed): graph capture + W steps
+    s.RunSteps(max(args.warmup, 3))
+    s.Sync()
+
+    # -- timed region: exactly K steps, graph replay ---------------------------
+    clocks = ClockSampler(local_rank).start()
+    time.sleep(0.3)
+    barrier()
+    s.Sync()
+    t0 = time.perf_counter()
+    ms = s.TimeSteps(args.steps, graph=True)
+    t1 = time.perf_counter()
+    s.Sync()
+    barrier()
+    time.sleep(0.25)
+    clocks.stop()
+    ms = allmax(ms)
+    status = s.DeviceStatus()
+
+    # -- per-kernel times over a second K-step region (eager, event-bracketed)
+    s.SetTiming(True)
+    nphase = min(args.steps, 4096)
+    s.RunSteps(nphase)
+    phases, nsteps_timed = s.PhaseTimes()
+    s.SetTiming(False)
+    n_in = int(s.GetBuffer(F.FGRIDCNT).sum(dtype=np.int64))
+
+    # -- e2e: host buffers through the C ABI ------------------------------------
+    e2e_steps = args.e2e_steps or min(args.steps, 20)
+    n = scene.n
+    pin_pos = F.PinnedArray((n, 3), np.float32)
+    pin_vel = F.PinnedArray((n, 3), np.float32)
+    pin_vev = F.PinnedArray((n, 3), np.float32)
+    pin_clr = F.PinnedArray((n,), np.uint32)
+    pin_out = F.PinnedArray((n, 3), np.float32)
+    pin_pos.array[:] = s.GetBuffer(F.FPOS)
+    pin_vel.array[:] = s.GetBuffer(F.FVEL)
+    pin_vev.array[:] = s.GetBuffer(F.FVEVAL)
+    pin_clr.array[:] = s.GetBuffer(F.FCLR)
+    lib = F.lib()
+    vp = lambda a: a.ctypes.data_as(C.c_void_p)
+    h2d = n * (12 * 3 + 4)
+    d2h = n * 12
+    barrier()
+    s.Sync()
+    te0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        F._lib.check("fl_set_particles", lib.fl_set_particles(
+            s.handle, n, vp(pin_pos.array), vp(pin_vel.array), vp(pin_vev.array), None, None, vp(pin_clr.array)))
+        F._lib.check("fl_run", lib.fl_run(s.handle))
+        F._lib.check("fl_get_buffer", lib.fl_get_buffer(s.handle, F.FPOS, vp(pin_out.array), d2h))
+    te1 = time.perf_counter()
+    barrier()
+    e2e_s = allmax(te1 - te0)
+    for a in (pin_pos, pin_vel, pin_vev, pin_clr, pin_out):
+        a.free()
+    s.close()
+
+    if rank != 0:
+        return
+
+    value = world * scene.n * args.steps / (ms / 1e3) / 1e6
+    dominant = max((k for k in phases if k != "scan"), key=lambda k: phases[k])
+    dur_ms = phases[dominant]
+    algo = ALGO_BYTES[dominant] * n_in
+    achieved = algo / (dur_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = ncu_traffic(dominant)
+    roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": f"of {peak_kind}", "traffic": traffic,
+                "algorithmic_bytes_per_launch": algo, "mean_launch_ms": dur_ms}
+    step_bytes = sum(ALGO_BYTES[k] for k in ALGO_BYTES) * n_in + 12 * (p.gridTotal + 1)
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu, _ = cpu_reference_rate(scene, args.cpu_seconds, cpu_threads())
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded jittered lattice (splitmix64), no dataset",
+        "config": config_of(scene, args),
+        "roofline": roofline,
+        "step_roofline": {"algorithmic_bytes_per_step": step_bytes,
+                          "achieved_gbs": step_bytes / (ms / args.steps / 1e3) / 1e9,
+                          "frac": step_bytes / (ms / args.steps / 1e3) / 1e9 / peak},
+        "phases_ms": {k: round(v, 5) for k, v in phases.items()}, "phase_steps": nsteps_timed,
+        "cpu_baseline": cpu,
+        "e2e": {"value": world * n * e2e_steps / e2e_s / 1e6, "unit": METRIC, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+        "clocks": clocks.summary(t0, t1),
+        "gpu_launches": KERNELS_PER_STEP * args.steps,
+        "device_status": status,
+        "points_in_range": n_in,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local_rank = dist_env()
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+    our_arm(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,740 @@
+// Host runtime behind the C ABI (include/fluids_gb300.h): allocation, data
+// movement, the phase sequence of FluidSystem::Run and graph replay.
+//
+// Reference counterparts (fluids4.0/fluid_system.cpp):
+//   Initialize/Start/AllocateParticles/AllocateGrid   92-168, 218-272
+//   TransferToCUDA / TransferFromCUDA                 2312-2330
+//   InsertParticlesCUDA ... AdvanceCUDA               2334-2531
+//   Run (RUN_GPU_FULL) / AdvanceTime                  475-542
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <map>
+#include <vector>
+
+#include "fl_internal.h"
+
+// ---------------------------------------------------------------------------
+// errors
+
+static thread_local char g_err[512] = "";
+
+int fl_fail(int code, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+extern "C" const char *fl_last_error(void) { return g_err; }
+extern "C" int fl_abi_version(void) { return FL_ABI_VERSION; }
+
+// ---------------------------------------------------------------------------
+// parameters
+
+void fl_make_dev_params(const fl_params &p, DevParams *d) {
+    memset(d, 0, sizeof(*d));
+    d->gridMin = make_float3(p.gridMin[0], p.gridMin[1], p.gridMin[2]);
+    d->gridDelta = make_float3(p.gridDelta[0], p.gridDelta[1], p.gridDelta[2]);
+    d->gridRes = make_int3(p.gridRes[0], p.gridRes[1], p.gridRes[2]);
+    d->gridScanMax = make_int3(p.gridScanMax[0], p.gridScanMax[1], p.gridScanMax[2]);
+    d->gridSrch = p.gridSrch;
+    d->gridAdjCnt = p.gridAdjCnt;
+    d->ncells = p.gridTotal;
+    d->nadj = (1 * p.gridRes[2] + 1) * p.gridRes[0] + 1;   // fluid_kernels.cu:120
+    d->rd2 = p.rd2; d->d2 = p.d2; d->pmass = p.pmass; d->poly6kern = p.poly6kern;
+    d->psmoothradius = p.psmoothradius; d->prest_dens = p.prest_dens;
+    d->pintstiff = p.pintstiff; d->sim_scale = p.sim_scale;
+    d->spikykern = p.spikykern; d->vterm = p.vterm;
+    d->pradius = p.pradius; d->bound_slope = p.bound_slope; d->bound_stiff = p.bound_stiff;
+    d->bound_damp = p.bound_damp; d->bound_friction = p.bound_friction;
+    d->bound_wall_force = p.bound_wall_force; d->bound_wall_freq = p.bound_wall_freq;
+    d->bound_min = make_float3(p.bound_min[0], p.bound_min[1], p.bound_min[2]);
+    d->bound_max = make_float3(p.bound_max[0], p.bound_max[1], p.bound_max[2]);
+    d->gravity = make_float3(p.gravity[0], p.gravity[1], p.gravity[2]);
+    d->AL = p.AL; d->AL2 = p.AL2; d->VL = p.VL; d->VL2 = p.VL2;
+    for (int c = 0; c < p.gridAdjCnt && c < 216; c++) d->adj[c] = p.gridAdj[c];
+}
+
+static int check_derived(const fl_params *p) {
+    if (p->gridTotal <= 0 || p->gridSrch < 2 || p->gridSrch > FL_MAX_GRID_SRCH ||
+        p->gridAdjCnt != p->gridSrch * p->gridSrch * p->gridSrch)
+        return fl_fail(FL_ERR_PARAMS, "parameters are not derived (call fl_params_derive)");
+    if ((long long)p->gridRes[0] * p->gridRes[1] * p->gridRes[2] != p->gridTotal)
+        return fl_fail(FL_ERR_PARAMS, "gridTotal disagrees with gridRes");
+    return FL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// allocation
+
+static int dalloc(void **p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fl_fail(e == cudaErrorMemoryAllocation ? FL_ERR_NOMEM : FL_ERR_CUDA,
+                       "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    }
+    return FL_OK;
+}
+
+static void free_grid(fl_system *s) {
+    cudaFree(s->cnt);
+    cudaFree(s->off);
+    s->cnt = s->off = nullptr;
+    s->scan_ticket = nullptr;
+    s->scan_status = nullptr;
+}
+
+// Grid block: [cnt (grid_pad) | ticket (256 B) | descriptors] in one
+// allocation so one memset clears all of it; off is separate.
+static size_t grid_block_bytes(const fl_system *s) {
+    return s->grid_pad * sizeof(uint32_t) + fl_scan_scratch_bytes(s->scan_tiles);
+}
+
+static int alloc_grid(fl_system *s) {
+    const size_t tile = fl_scan_tile();
+    const size_t entries = (size_t)s->ncells + 1;
+    s->scan_tiles = (int)((entries + tile - 1) / tile);
+    s->grid_pad = (size_t)s->scan_tiles * tile;
+    void *blk = nullptr, *off = nullptr;
+    FL_TRY(dalloc(&blk, grid_block_bytes(s)));
+    int r = dalloc(&off, s->grid_pad * sizeof(uint32_t));
+    if (r != FL_OK) { cudaFree(blk); return r; }
+    s->cnt = (uint32_t *)blk;
+    s->scan_ticket = (uint32_t *)((char *)blk + s->grid_pad * sizeof(uint32_t));
+    s->scan_status = (uint64_t *)((char *)s->scan_ticket + 256);
+    s->off = (uint32_t *)off;
+    s->scan_epoch = 1;
+    FL_CUDA_TRY(cudaMemsetAsync(blk, 0, grid_block_bytes(s), s->stream));
+    FL_CUDA_TRY(cudaMemsetAsync(off, 0, s->grid_pad * sizeof(uint32_t), s->stream));
+    return FL_OK;
+}
+
+static void destroy_graph(fl_system *s) {
+    if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+    s->graph_exec = nullptr;
+    s->graph_steps = 0;
+}
+
+static void free_all(fl_system *s) {
+    destroy_graph(s);
+    for (int k = 0; k < F_COUNT; k++)
+        for (int c = 0; c < 2; c++) cudaFree(s->f[k].p[c]);
+    cudaFree(s->cell_pre); cudaFree(s->rank_tmp); cudaFree(s->src);
+    free_grid(s);
+    cudaFree(s->dev_err);
+    cudaFree(s->time_dev);
+    cudaFree(s->stage);
+    for (int k = 0; k < 8; k++)
+        if (s->ev[k]) cudaEventDestroy(s->ev[k]);
+    if (s->stream) cudaStreamDestroy(s->stream);
+}
+
+struct TimingState {
+    std::vector<cudaEvent_t> events;   // 7 per timed step
+    int steps = 0;
+};
+static TimingState *detach_timing(fl_system *s);
+
+extern "C" int fl_create(const fl_params *p, int max_points, fl_system **out) {
+    if (!p || !out) return fl_fail(FL_ERR_ARG, "fl_create: null argument");
+    *out = nullptr;
+    if (max_points < 0) return fl_fail(FL_ERR_ARG, "fl_create: max_points < 0");
+    FL_TRY(check_derived(p));
+    fl_system *s = (fl_system *)calloc(1, sizeof(fl_system));
+    if (!s) return fl_fail(FL_ERR_NOMEM, "fl_create: host allocation failed");
+    int r = FL_OK;
+    do {
+        if (cudaGetDevice(&s->device) != cudaSuccess) {
+            r = fl_fail(FL_ERR_CUDA, "fl_create: no CUDA device");
+            break;
+        }
+        if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            r = fl_fail(FL_ERR_CUDA, "fl_create: cudaStreamCreate failed");
+            break;
+        }
+        s->P = *p;
+        fl_make_dev_params(*p, &s->D);
+        s->max_points = max_points;
+        s->ncells = p->gridTotal;
+        const size_t np = (size_t)(max_points > 0 ? max_points : 1);
+        const size_t esz[F_COUNT] = {16, 16, 16, 16, 4, 4, 4, 4};
+        for (int k = 0; k < F_COUNT && r == FL_OK; k++) {
+            s->f[k].esz = esz[k];
+            for (int c = 0; c < 2 && r == FL_OK; c++) r = dalloc(&s->f[k].p[c], esz[k] * np);
+        }
+        if (r != FL_OK) break;
+        if ((r = dalloc((void **)&s->cell_pre, 4 * np)) != FL_OK) break;
+        if ((r = dalloc((void **)&s->rank_tmp, 4 * np)) != FL_OK) break;
+        if ((r = dalloc((void **)&s->src, 4 * np)) != FL_OK) break;
+        if ((r = dalloc((void **)&s->dev_err, 256)) != FL_OK) break;
+        if ((r = dalloc((void **)&s->time_dev, 256)) != FL_OK) break;
+        if ((r = alloc_grid(s)) != FL_OK) break;
+        if (cudaMemsetAsync(s->dev_err, 0, 256, s->stream) != cudaSuccess ||
+            cudaMemsetAsync(s->time_dev, 0, 256, s->stream) != cudaSuccess) {
+            r = fl_fail(FL_ERR_CUDA, "fl_create: memset failed");
+            break;
+        }
+        for (int k = 0; k < F_COUNT && r == FL_OK; k++)
+            for (int c = 0; c < 2; c++)
+                if (cudaMemsetAsync(s->f[k].p[c], 0, s->f[k].esz * np, s->stream) != cudaSuccess)
+                    r = fl_fail(FL_ERR_CUDA, "fl_create: memset failed");
+        if (r != FL_OK) break;
+        for (int k = 0; k < 8; k++)
+            if (cudaEventCreate(&s->ev[k]) != cudaSuccess) r = fl_fail(FL_ERR_CUDA, "fl_create: event");
+        if (r != FL_OK) break;
+        s->time = 0.0f;
+        s->time_host_valid = 1;
+        if (cudaStreamSynchronize(s->stream) != cudaSuccess) {
+            r = fl_fail(FL_ERR_CUDA, "fl_create: %s", cudaGetErrorString(cudaGetLastError()));
+            break;
+        }
+    } while (0);
+    if (r != FL_OK) {
+        free_all(s);
+        free(s);
+        return r;
+    }
+    *out = s;
+    return FL_OK;
+}
+
+extern "C" int fl_destroy(fl_system *s) {
+    if (!s) return FL_OK;
+    cudaStreamSynchronize(s->stream);
+    TimingState *t = detach_timing(s);
+    if (t) {
+        for (cudaEvent_t e : t->events) cudaEventDestroy(e);
+        delete t;
+    }
+    free_all(s);
+    free(s);
+    return FL_OK;
+}
+
+// Timing state lives beside the system (kept out of the plain-C struct).
+static std::map<fl_system *, TimingState *> g_timing;
+static TimingState *detach_timing(fl_system *s) {
+    auto it = g_timing.find(s);
+    if (it == g_timing.end()) return nullptr;
+    TimingState *t = it->second;
+    g_timing.erase(it);
+    return t;
+}
+
+static void reset_progress(fl_system *s) {
+    s->have_insert = s->have_offsets = s->have_grid = 0;
+    s->offsets_inclusive = 0;
+}
+
+extern "C" int fl_set_params(fl_system *s, const fl_params *p) {
+    if (!s || !p) return fl_fail(FL_ERR_ARG, "fl_set_params: null argument");
+    FL_TRY(check_derived(p));
+    FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (p->gridTotal != s->ncells) {
+        free_grid(s);
+        s->ncells = p->gridTotal;
+        FL_TRY(alloc_grid(s));
+    }
+    s->P = *p;
+    fl_make_dev_params(*p, &s->D);
+    destroy_graph(s);
+    reset_progress(s);
+    return FL_OK;
+}
+
+extern "C" int fl_get_params(const fl_system *s, fl_params *p) {
+    if (!s || !p) return fl_fail(FL_ERR_ARG, "fl_get_params: null argument");
+    *p = s->P;
+    return FL_OK;
+}
+
+extern "C" int fl_num_points(const fl_system *s) { return s ? s->n : 0; }
+extern "C" int fl_grid_total(const fl_system *s) { return s ? s->ncells : 0; }
+
+static int sync_time_to_host(fl_system *s) {
+    if (s->time_host_valid) return FL_OK;
+    FL_CUDA_TRY(cudaMemcpyAsync(&s->time, s->time_dev + s->time_slot, sizeof(float),
+                                cudaMemcpyDeviceToHost, s->stream));
+    FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->time_host_valid = 1;
+    return FL_OK;
+}
+
+extern "C" int fl_get_time(const fl_system *cs, float *t) {
+    fl_system *s = const_cast<fl_system *>(cs);
+    if (!s || !t) return fl_fail(FL_ERR_ARG, "fl_get_time: null argument");
+    FL_TRY(sync_time_to_host(s));
+    *t = s->time;
+    return FL_OK;
+}
+
+extern "C" int fl_set_time(fl_system *s, float t) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_set_time: null system");
+    s->time = t;
+    s->time_host_valid = 1;
+    FL_CUDA_TRY(cudaMemcpyAsync(s->time_dev + s->time_slot, &s->time, sizeof(float),
+                                cudaMemcpyHostToDevice, s->stream));
+    FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return FL_OK;
+}
+
+extern "C" void *fl_stream(fl_system *s) { return s ? (void *)s->stream : nullptr; }
+
+// ---------------------------------------------------------------------------
+// data movement
+
+static int ensure_stage(fl_system *s, size_t bytes) {
+    if (bytes <= s->stage_bytes) return FL_OK;
+    cudaFree(s->stage);
+    s->stage = nullptr;
+    s->stage_bytes = 0;
+    FL_TRY(dalloc(&s->stage, bytes));
+    s->stage_bytes = bytes;
+    return FL_OK;
+}
+
+extern "C" int fl_host_alloc(size_t bytes, void **out) {
+    if (!out) return fl_fail(FL_ERR_ARG, "fl_host_alloc: null argument");
+    *out = nullptr;
+    cudaError_t e = cudaHostAlloc(out, bytes ? bytes : 16, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        return fl_fail(FL_ERR_NOMEM, "cudaHostAlloc(%zu): %s", bytes, cudaGetErrorString(e));
+    }
+    return FL_OK;
+}
+
+extern "C" int fl_host_free(void *p) {
+    if (p) FL_CUDA_TRY(cudaFreeHost(p));
+    return FL_OK;
+}
+
+extern "C" int fl_set_particles(fl_system *s, int n, const float *pos, const float *vel,
+                                const float *veval, const float *force, const float *press,
+                                const uint32_t *clr) {
+    if (!s || !pos) return fl_fail(FL_ERR_ARG, "fl_set_particles: null system or pos");
+    if (n < 0) return fl_fail(FL_ERR_ARG, "fl_set_particles: n < 0");
+    if (n > s->max_points)
+        return fl_fail(FL_ERR_CAPACITY, "fl_set_particles: %d points exceed capacity %d", n, s->max_points);
+    destroy_graph(s);
+    s->n = n;
+    if (n > 0) {
+        // one staging slice per float3 field, then unpack to float4 on device
+        const size_t v3 = 12 * (size_t)n;
+        FL_TRY(ensure_stage(s, 4 * v3));
+        const float *src3[4] = {pos, vel, veval, force};
+        const int fid[4] = {F_POS, F_VEL, F_VEVAL, F_FORCE};
+        for (int k = 0; k < 4; k++) {
+            float4 *dst = s->f[fid[k]].cur<float4>();
+            if (!src3[k]) {
+                FL_CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(float4) * (size_t)n, s->stream));
+                continue;
+            }
+            float *slice = (float *)((char *)s->stage + k * v3);
+            FL_CUDA_TRY(cudaMemcpyAsync(slice, src3[k], v3, cudaMemcpyHostToDevice, s->stream));
+            FL_TRY(fl_launch_unpack3(s, slice, dst, n));
+        }
+        const void *src1[2] = {press, clr};
+        const int fid1[2] = {F_PRESS, F_CLR};
+        for (int k = 0; k < 2; k++) {
+            void *dst = s->f[fid1[k]].cur<void>();
+            if (!src1[k]) FL_CUDA_TRY(cudaMemsetAsync(dst, 0, 4 * (size_t)n, s->stream));
+            else FL_CUDA_TRY(cudaMemcpyAsync(dst, src1[k], 4 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+        }
+    }
+    // the caller may reuse its host arrays on return
+    FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    reset_progress(s);
+    return FL_OK;
+}
+
+static int buffer_bytes(const fl_system *s, int id, size_t *bytes) {
+    switch (id) {
+    case FL_FPOS: case FL_FVEL: case FL_FVEVAL: case FL_FFORCE: *bytes = 12 * (size_t)s->n; return FL_OK;
+    case FL_FPRESS: case FL_FCLR: case FL_FGCELL: case FL_FGNDX: case FL_FGRID:
+        *bytes = 4 * (size_t)s->n; return FL_OK;
+    case FL_FGRIDCNT: case FL_FGRIDOFF: *bytes = 4 * (size_t)s->ncells; return FL_OK;
+    default: return fl_fail(FL_ERR_ARG, "unknown buffer id %d", id);
+    }
+}
+
+static int field_of(int id) {
+    switch (id) {
+    case FL_FPOS: return F_POS; case FL_FVEL: return F_VEL; case FL_FVEVAL: return F_VEVAL;
+    case FL_FFORCE: return F_FORCE; case FL_FPRESS: return F_PRESS; case FL_FCLR: return F_CLR;
+    case FL_FGCELL: return F_GCELL; case FL_FGNDX: return F_GNDX;
+    default: return -1;
+    }
+}
+
+// Produce buffer `id` in fluid.h layout at device address dev (async).
+static int export_to_device(fl_system *s, int id, void *dev) {
+    const int fi = field_of(id);
+    if (id == FL_FPOS || id == FL_FVEL || id == FL_FVEVAL || id == FL_FFORCE)
+        return fl_launch_pack3(s, s->f[fi].cur<float4>(), (float *)dev, s->n);
+    if (fi >= 0) {
+        FL_CUDA_TRY(cudaMemcpyAsync(dev, s->f[fi].cur<void>(), 4 * (size_t)s->n,
+                                    cudaMemcpyDeviceToDevice, s->stream));
+        return FL_OK;
+    }
+    if (id == FL_FGRIDCNT) {
+        FL_CUDA_TRY(cudaMemcpyAsync(dev, s->cnt, 4 * (size_t)s->ncells, cudaMemcpyDeviceToDevice, s->stream));
+        return FL_OK;
+    }
+    if (id == FL_FGRIDOFF) {
+        FL_CUDA_TRY(cudaMemcpyAsync(dev, s->off, 4 * (size_t)s->ncells, cudaMemcpyDeviceToDevice, s->stream));
+        return FL_OK;
+    }
+    if (id == FL_FGRID) {
+        // identity over the in-range slots (countingSortFull sets FGRID[s] = s, cu:83)
+        uint32_t n_in = 0;
+        FL_CUDA_TRY(cudaMemcpyAsync(&n_in, s->off + s->ncells, 4, cudaMemcpyDeviceToHost, s->stream));
+        FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+        if (!s->have_grid) n_in = 0;
+        return fl_launch_grid_identity(s, (uint32_t *)dev, s->n, (int)n_in);
+    }
+    return fl_fail(FL_ERR_ARG, "unknown buffer id %d", id);
+}
+
+extern "C" int fl_get_buffer(fl_system *s, int id, void *host, size_t bytes) {
+    if (!s || !host) return fl_fail(FL_ERR_ARG, "fl_get_buffer: null argument");
+    size_t need = 0;
+    FL_TRY(buffer_bytes(s, id, &need));
+    if (bytes < need) return fl_fail(FL_ERR_ARG, "fl_get_buffer: %zu bytes < %zu needed", bytes, need);
+    if (need == 0) return FL_OK;
+    FL_TRY(ensure_stage(s, need));
+    FL_TRY(export_to_device(s, id, s->stage));
+    FL_CUDA_TRY(cudaMemcpyAsync(host, s->stage, need, cudaMemcpyDeviceToHost, s->stream));
+    FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (id == FL_FGRIDOFF && s->offsets_inclusive) {
+        // zero_offsets = 0 asks for the inclusive scan: off[c] + cnt[c]
+        std::vector<uint32_t> cnt(s->ncells);
+        FL_CUDA_TRY(cudaMemcpy(cnt.data(), s->cnt, 4 * (size_t)s->ncells, cudaMemcpyDeviceToHost));
+        uint32_t *o = (uint32_t *)host;
+        for (int c = 0; c < s->ncells; c++) o[c] += cnt[c];
+    }
+    return FL_OK;
+}
+
+extern "C" int fl_export_device(fl_system *s, int id, void *dev, size_t bytes) {
+    if (!s || !dev) return fl_fail(FL_ERR_ARG, "fl_export_device: null argument");
+    size_t need = 0;
+    FL_TRY(buffer_bytes(s, id, &need));
+    if (bytes < need) return fl_fail(FL_ERR_ARG, "fl_export_device: %zu bytes < %zu needed", bytes, need);
+    if (need == 0) return FL_OK;
+    if (id == FL_FGRIDOFF && s->offsets_inclusive)
+        return fl_fail(FL_ERR_STATE, "fl_export_device: inclusive offsets are host-readback only");
+    return export_to_device(s, id, dev);
+}
+
+extern "C" int fl_import_device(fl_system *s, int n, const void *dev_pos, const void *dev_vel,
+                                const void *dev_veval) {
+    if (!s || !dev_pos) return fl_fail(FL_ERR_ARG, "fl_import_device: null system or pos");
+    if (n < 0 || n > s->max_points)
+        return fl_fail(FL_ERR_CAPACITY, "fl_import_device: %d points (capacity %d)", n, s->max_points);
+    destroy_graph(s);
+    s->n = n;
+    FL_TRY(fl_launch_unpack3(s, (const float *)dev_pos, s->f[F_POS].cur<float4>(), n));
+    if (dev_vel) FL_TRY(fl_launch_unpack3(s, (const float *)dev_vel, s->f[F_VEL].cur<float4>(), n));
+    else FL_CUDA_TRY(cudaMemsetAsync(s->f[F_VEL].cur<void>(), 0, 16 * (size_t)n, s->stream));
+    if (dev_veval) FL_TRY(fl_launch_unpack3(s, (const float *)dev_veval, s->f[F_VEVAL].cur<float4>(), n));
+    else FL_CUDA_TRY(cudaMemsetAsync(s->f[F_VEVAL].cur<void>(), 0, 16 * (size_t)n, s->stream));
+    reset_progress(s);
+    return FL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// phases
+
+static int clear_grid(fl_system *s) {
+    // InsertParticlesCUDA clears FGRIDCNT/FGRIDOFF (cpp:2336-2337); here one
+    // memset clears the counts, the scan ticket and the scan descriptors.
+    FL_CUDA_TRY(cudaMemsetAsync(s->cnt, 0, grid_block_bytes(s), s->stream));
+    return FL_OK;
+}
+
+static int readback(fl_system *s, void *host, const void *dev, size_t bytes) {
+    if (!host || bytes == 0) return FL_OK;
+    FL_CUDA_TRY(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, s->stream));
+    FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return FL_OK;
+}
+
+extern "C" int fl_insert_particles(fl_system *s, uint32_t *gcell, uint32_t *gndx, uint32_t *gcnt) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_insert_particles: null system");
+    FL_TRY(clear_grid(s));
+    FL_TRY(fl_launch_insert(s, s->f[F_GCELL].cur<uint32_t>()));
+    // canonical gndx: offsets, arrival-order index scatter, per-cell sort
+    FL_TRY(fl_launch_scan(s, s->ncells + 1, 0));
+    FL_TRY(fl_launch_scatter_index(s));
+    FL_TRY(fl_launch_sort_cells(s, 0));
+    s->have_insert = 1;
+    s->have_offsets = 0;
+    s->have_grid = 0;
+    FL_TRY(readback(s, gcell, s->f[F_GCELL].cur<void>(), 4 * (size_t)s->n));
+    FL_TRY(readback(s, gndx, s->f[F_GNDX].cur<void>(), 4 * (size_t)s->n));
+    FL_TRY(readback(s, gcnt, s->cnt, 4 * (size_t)s->ncells));
+    return FL_OK;
+}
+
+extern "C" int fl_prefix_sum_cells(fl_system *s, uint32_t *goff, int zero_offsets) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_prefix_sum_cells: null system");
+    if (!s->have_insert) return fl_fail(FL_ERR_STATE, "fl_prefix_sum_cells before fl_insert_particles");
+    FL_TRY(fl_launch_scan(s, s->ncells + 1, 1));
+    s->have_offsets = 1;
+    s->offsets_inclusive = zero_offsets ? 0 : 1;
+    if (goff) FL_TRY(fl_get_buffer(s, FL_FGRIDOFF, goff, 4 * (size_t)s->ncells));
+    return FL_OK;
+}
+
+static void flip(fl_system *s, int k) { s->f[k].live ^= 1; }
+
+extern "C" int fl_counting_sort_full(fl_system *s, float *ppos) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_counting_sort_full: null system");
+    if (!s->have_insert || !s->have_offsets)
+        return fl_fail(FL_ERR_STATE, "fl_counting_sort_full before insert and prefix sum");
+    FL_TRY(fl_launch_gather_all(s));
+    for (int k = 0; k < F_COUNT; k++) flip(s, k);
+    s->have_grid = 1;
+    s->have_insert = 0;   // the pre-sort cell list no longer matches the order
+    if (ppos) FL_TRY(fl_get_buffer(s, FL_FPOS, ppos, 12 * (size_t)s->n));
+    return FL_OK;
+}
+
+extern "C" int fl_compute_pressure(fl_system *s) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_compute_pressure: null system");
+    if (!s->have_grid) return fl_fail(FL_ERR_STATE, "fl_compute_pressure before fl_counting_sort_full");
+    return fl_launch_density(s);
+}
+
+extern "C" int fl_compute_force(fl_system *s) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_compute_force: null system");
+    if (!s->have_grid) return fl_fail(FL_ERR_STATE, "fl_compute_force before fl_counting_sort_full");
+    return fl_launch_force(s);
+}
+
+extern "C" int fl_advance(fl_system *s, float time, float dt, float ss) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_advance: null system");
+    if (!s->have_grid) return fl_fail(FL_ERR_STATE, "fl_advance before fl_counting_sort_full");
+    return fl_launch_advance(s, time, dt, ss);
+}
+
+// ---------------------------------------------------------------------------
+// Run: the fused step
+
+static int record(fl_system *s, TimingState *t, int k) {
+    if (!t) return FL_OK;
+    FL_CUDA_TRY(cudaEventRecord(t->events[(size_t)t->steps * 7 + k], s->stream));
+    return FL_OK;
+}
+
+static int run_step(fl_system *s, TimingState *t) {
+    // InsertParticles, PrefixSumCells, CountingSortFull, ComputePressure,
+    // ComputeForce + Advance (cpp:507-515) as six launches.
+    FL_TRY(record(s, t, 0));
+    FL_TRY(clear_grid(s));
+    FL_TRY(fl_launch_insert(s, nullptr));
+    FL_TRY(record(s, t, 1));
+    FL_TRY(fl_launch_scan(s, s->ncells + 1, 0));
+    FL_TRY(record(s, t, 2));
+    FL_TRY(fl_launch_scatter_index(s));
+    FL_TRY(record(s, t, 3));
+    FL_TRY(fl_launch_sort_cells(s, 1));
+    flip(s, F_POS); flip(s, F_VEL); flip(s, F_VEVAL); flip(s, F_CLR); flip(s, F_GCELL); flip(s, F_GNDX);
+    FL_TRY(record(s, t, 4));
+    FL_TRY(fl_launch_density(s));
+    FL_TRY(record(s, t, 5));
+    FL_TRY(fl_launch_force_advance(s, s->P.dt));
+    flip(s, F_POS); flip(s, F_VEVAL);
+    FL_TRY(record(s, t, 6));
+    s->time_slot ^= 1;
+    if (t) t->steps++;
+    return FL_OK;
+}
+
+static TimingState *active_timing(fl_system *s) {
+    if (!s->timing) return nullptr;
+    auto it = g_timing.find(s);
+    if (it == g_timing.end()) return nullptr;
+    TimingState *t = it->second;
+    if (t->steps >= 4096) return nullptr;
+    const size_t need = (size_t)(t->steps + 1) * 7;
+    while (t->events.size() < need) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        t->events.push_back(e);
+    }
+    return t;
+}
+
+static int begin_run(fl_system *s) {
+    if (!s->time_host_valid) return FL_OK;
+    // host time is authoritative: publish it to the slot the next step reads
+    FL_CUDA_TRY(cudaMemcpyAsync(s->time_dev + s->time_slot, &s->time, sizeof(float),
+                                cudaMemcpyHostToDevice, s->stream));
+    return FL_OK;
+}
+
+extern "C" int fl_run(fl_system *s) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_run: null system");
+    FL_TRY(begin_run(s));
+    FL_TRY(run_step(s, active_timing(s)));
+    if (s->time_host_valid) s->time += s->P.dt;   // AdvanceTime (cpp:529), same float add
+    s->have_insert = 0;
+    s->have_offsets = 1;
+    s->have_grid = 1;
+    return FL_OK;
+}
+
+// A captured pair of steps returns every field's live copy and the time
+// slot to where they started, so the same graph replays any number of times.
+static int capture_pair(fl_system *s) {
+    destroy_graph(s);
+    int live[F_COUNT];
+    for (int k = 0; k < F_COUNT; k++) live[k] = s->f[k].live;
+    const int slot = s->time_slot;
+    cudaGraph_t g = nullptr;
+    FL_CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    int r = run_step(s, nullptr);
+    if (r == FL_OK) r = run_step(s, nullptr);
+    cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+    for (int k = 0; k < F_COUNT; k++) s->f[k].live = live[k];
+    s->time_slot = slot;
+    if (r != FL_OK) { if (g) cudaGraphDestroy(g); return r; }
+    if (e != cudaSuccess) return fl_fail(FL_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&s->graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        s->graph_exec = nullptr;
+        return fl_fail(FL_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    }
+    s->graph_steps = 2;
+    for (int k = 0; k < F_COUNT; k++) s->graph_live[k] = live[k];
+    return FL_OK;
+}
+
+extern "C" int fl_run_steps(fl_system *s, int nsteps) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_run_steps: null system");
+    if (nsteps < 0) return fl_fail(FL_ERR_ARG, "fl_run_steps: nsteps < 0");
+    if (s->timing) {   // timed steps stay eager so each launch is bracketed
+        for (int k = 0; k < nsteps; k++) FL_TRY(fl_run(s));
+        return FL_OK;
+    }
+    const int pairs = nsteps / 2;
+    if (pairs > 0) {
+        bool match = s->graph_exec != nullptr;
+        for (int k = 0; k < F_COUNT && match; k++) match = s->graph_live[k] == s->f[k].live;
+        if (!match) FL_TRY(capture_pair(s));
+        FL_TRY(begin_run(s));
+        for (int p = 0; p < pairs; p++) FL_CUDA_TRY(cudaGraphLaunch(s->graph_exec, s->stream));
+        s->time_host_valid = 0;   // the device slot now holds the time
+        s->have_insert = 0;
+        s->have_offsets = 1;
+        s->have_grid = 1;
+    }
+    if (nsteps & 1) {
+        if (!s->time_host_valid) {
+            // the eager step must read the device time, not a stale host copy
+            FL_TRY(run_step(s, nullptr));
+            s->have_insert = 0; s->have_offsets = 1; s->have_grid = 1;
+        } else {
+            FL_TRY(fl_run(s));
+        }
+    }
+    return FL_OK;
+}
+
+extern "C" int fl_device_status(fl_system *s, uint32_t *flags) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_device_status: null system");
+    uint32_t v = 0;
+    FL_CUDA_TRY(cudaMemcpyAsync(&v, s->dev_err, 4, cudaMemcpyDeviceToHost, s->stream));
+    FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (flags) *flags = v;
+    return FL_OK;
+}
+
+extern "C" int fl_sync(fl_system *s) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_sync: null system");
+    FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    uint32_t v = 0;
+    FL_TRY(fl_device_status(s, &v));
+    if (v) {
+        FL_CUDA_TRY(cudaMemsetAsync(s->dev_err, 0, 4, s->stream));
+        FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+        return fl_fail(FL_ERR_DEVICE, "device error word 0x%x%s%s%s", v,
+                       (v & FL_DEV_SPIN_TIMEOUT) ? " (scan look-back timed out)" : "",
+                       (v & FL_DEV_BAD_CELL) ? " (cell index out of range)" : "",
+                       (v & FL_DEV_NONFINITE) ? " (non-finite position)" : "");
+    }
+    return FL_OK;
+}
+
+extern "C" int fl_integrity_check(fl_system *s, int64_t *bad) {
+    if (!s || !bad) return fl_fail(FL_ERR_ARG, "fl_integrity_check: null argument");
+    if (!s->have_grid) return fl_fail(FL_ERR_STATE, "fl_integrity_check needs a sorted grid");
+    FL_TRY(ensure_stage(s, 16));
+    FL_CUDA_TRY(cudaMemsetAsync(s->stage, 0, 8, s->stream));
+    FL_TRY(fl_launch_integrity(s, (unsigned long long *)s->stage));
+    unsigned long long v = 0;
+    FL_TRY(readback(s, &v, s->stage, 8));
+    *bad = (int64_t)v;
+    return FL_OK;
+}
+
+extern "C" int fl_set_timing(fl_system *s, int enable) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_set_timing: null system");
+    FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    TimingState *t = detach_timing(s);
+    if (t) {
+        for (cudaEvent_t e : t->events) cudaEventDestroy(e);
+        delete t;
+    }
+    s->timing = enable ? 1 : 0;
+    if (enable) g_timing[s] = new TimingState();
+    return FL_OK;
+}
+
+extern "C" int fl_time_steps(fl_system *s, int nsteps, int use_graph, double *ms) {
+    if (!s || !ms) return fl_fail(FL_ERR_ARG, "fl_time_steps: null argument");
+    if (nsteps < 0) return fl_fail(FL_ERR_ARG, "fl_time_steps: nsteps < 0");
+    FL_CUDA_TRY(cudaEventRecord(s->ev[0], s->stream));
+    if (use_graph) {
+        FL_TRY(fl_run_steps(s, nsteps));
+    } else {
+        for (int k = 0; k < nsteps; k++) FL_TRY(fl_run(s));
+    }
+    FL_CUDA_TRY(cudaEventRecord(s->ev[1], s->stream));
+    FL_CUDA_TRY(cudaEventSynchronize(s->ev[1]));
+    float v = 0.0f;
+    FL_CUDA_TRY(cudaEventElapsedTime(&v, s->ev[0], s->ev[1]));
+    *ms = v;
+    return FL_OK;
+}
+
+extern "C" int fl_get_phase_times(fl_system *s, double ms[8], int *steps) {
+    if (!s || !ms) return fl_fail(FL_ERR_ARG, "fl_get_phase_times: null argument");
+    for (int k = 0; k < 8; k++) ms[k] = 0.0;
+    if (steps) *steps = 0;
+    auto it = g_timing.find(s);
+    if (it == g_timing.end()) return FL_OK;
+    TimingState *t = it->second;
+    FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    for (int st = 0; st < t->steps; st++)
+        for (int k = 0; k < 6; k++) {
+            float v = 0.0f;
+            FL_CUDA_TRY(cudaEventElapsedTime(&v, t->events[(size_t)st * 7 + k],
+                                             t->events[(size_t)st * 7 + k + 1]));
+            ms[k] += v;
+        }
+    if (t->steps > 0)
+        for (int k = 0; k < 6; k++) ms[k] /= t->steps;
+    if (steps) *steps = t->steps;
+    return FL_OK;
+}

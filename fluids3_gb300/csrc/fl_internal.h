@@ -1,0 +1,134 @@
+// Internal declarations shared by the host runtime and the kernels.
+#pragma once
+
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+#include "../../include/fluids_gb300.h"
+
+// Record a failure message for fl_last_error() and return `code`.
+int fl_fail(int code, const char *fmt, ...);
+
+#define FL_CUDA_TRY(expr)                                                       \
+    do {                                                                        \
+        cudaError_t _e = (expr);                                                \
+        if (_e != cudaSuccess)                                                  \
+            return fl_fail(FL_ERR_CUDA, "%s: %s (%s:%d)", #expr,                \
+                           cudaGetErrorString(_e), __FILE__, __LINE__);         \
+    } while (0)
+
+#define FL_TRY(expr)                                                            \
+    do {                                                                        \
+        int _r = (expr);                                                        \
+        if (_r != FL_OK) return _r;                                             \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// Kernel-side parameter block, passed by value (__grid_constant__) to every
+// launch: the FParams fields the step reads (fluids4.0/fluid.h:155-192).
+struct DevParams {
+    float3 gridMin, gridDelta;
+    int3 gridRes, gridScanMax;
+    int gridSrch, gridAdjCnt;
+    int ncells;          // C; cell index C is the bin for out-of-range points
+    int nadj;            // (resZ + 1) * resX + 1: corner offset of the search block
+    float rd2, d2, pmass, poly6kern;
+    float psmoothradius, prest_dens, pintstiff, sim_scale, spikykern, vterm;
+    float pradius, bound_slope, bound_stiff, bound_damp, bound_friction;
+    float bound_wall_force, bound_wall_freq;
+    float3 bound_min, bound_max, gravity;
+    float AL, AL2, VL, VL2;
+    int adj[216];
+};
+
+void fl_make_dev_params(const fl_params &p, DevParams *d);
+
+// One particle field held twice in HBM. Gathers (the counting sort) and the
+// fused force+advance pass write the copy that is not live and then flip,
+// so no kernel overwrites a value that another thread may still read.
+struct Field {
+    void *p[2];
+    int live;
+    size_t esz;          // bytes per element in HBM
+    template <class T> T *cur() const { return (T *)p[live]; }
+    template <class T> T *nxt() const { return (T *)p[live ^ 1]; }
+};
+
+enum { F_POS, F_VEL, F_VEVAL, F_FORCE, F_PRESS, F_CLR, F_GCELL, F_GNDX, F_COUNT };
+
+struct fl_system {
+    int device;
+    cudaStream_t stream;
+    fl_params P;
+    DevParams D;
+    int max_points;
+    int n;                 // live point count
+    int ncells;            // C
+    float time;
+
+    Field f[F_COUNT];      // pos/vel/veval/force: float4; press: float; clr/gcell/gndx: uint
+
+    // insert / sort scratch, indexed by pre-sort point index unless noted
+    uint32_t *cell_pre;    // cell of point i (C when out of range)
+    uint32_t *rank_tmp;    // arrival rank from the counting atomics; reused by the dense-cell path
+    uint32_t *src;         // sorted slot -> pre-sort index
+
+    // grid: C + 1 entries (entry C is the out-of-range bin), padded to whole
+    // scan tiles. One allocation holds [cnt | scan ticket | scan descriptors]
+    // so a single memset clears all three at the start of a step.
+    uint32_t *cnt;
+    uint32_t *off;
+    size_t grid_pad;
+    uint32_t *scan_ticket; // dynamic tile counter (256 B slot)
+    uint64_t *scan_status; // decoupled look-back tile descriptors
+    int scan_tiles;
+    uint32_t scan_epoch;
+
+    uint32_t *dev_err;     // device error word (FL_DEV_*)
+
+    // m_Time on the device, double-buffered by step parity so a captured
+    // graph replays with the time advancing: step k reads time_dev[k & 1]
+    // and writes time_dev[(k + 1) & 1] = time + dt (AdvanceTime, cpp:527-531).
+    float *time_dev;
+    int time_slot;
+    int time_host_valid;   // host `time` mirrors the device value
+
+    void *stage;           // device staging for fluid.h-layout import/export
+    size_t stage_bytes;
+
+    // phase-API progress, in the order Run issues the phases. have_grid: the
+    // sorted copies, counts and offsets come from one completed sort.
+    int have_insert, have_offsets, have_grid;
+    int offsets_inclusive;
+
+    // graph replay for fl_run_steps
+    cudaGraphExec_t graph_exec;
+    int graph_steps;
+    int graph_live[F_COUNT];
+
+    // per-phase event timing (PERF_PUSH/PERF_POP of Run, cpp:507-515)
+    int timing;
+    cudaEvent_t ev[8];
+    double phase_ms[8];
+    int phase_runs;
+};
+
+// ---- launch wrappers (fl_kernels.cu, fl_scan.cu) ---------------------------
+int fl_launch_insert(fl_system *s, uint32_t *gcell_pre_or_null);
+int fl_launch_scan(fl_system *s, int count, int clear_status);
+int fl_launch_scatter_index(fl_system *s);
+// mode 0: rank only (sorted src + canonical gndx into f[F_GNDX].cur, pre-sort order)
+// mode 1: fused rank + gather of pos/vel/veval/clr/gcell/gndx into the nxt copies
+int fl_launch_sort_cells(fl_system *s, int mode);
+// gather every field cur -> nxt through src (phase-API counting sort)
+int fl_launch_gather_all(fl_system *s);
+int fl_launch_density(fl_system *s);
+int fl_launch_force(fl_system *s);
+int fl_launch_force_advance(fl_system *s, float dt);
+int fl_launch_advance(fl_system *s, float time, float dt, float ss);
+int fl_launch_pack3(fl_system *s, const float4 *src, float *dst, int n);
+int fl_launch_unpack3(fl_system *s, const float *src, float4 *dst, int n);
+int fl_launch_grid_identity(fl_system *s, uint32_t *dst, int n, int n_in);
+int fl_launch_integrity(fl_system *s, unsigned long long *bad_dev);
+size_t fl_scan_tile();
+size_t fl_scan_scratch_bytes(int ntiles);

@@ -1,0 +1,249 @@
+"""Host-side mirror of the reference's FluidSystem (fluids4.0/fluid_system.h:145-353)
+over the C ABI. Method names and argument meaning follow the reference's
+GPU pathway; every call runs the CUDA kernels of libfluids_gb300.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import call, lib
+from .params import FlParams
+
+# Buffer ids (fluids4.0/fluid.h:45-70)
+FPOS, FVEL, FVEVAL, FFORCE, FPRESS, FCLR, FGCELL, FGNDX = 0, 1, 2, 3, 4, 5, 6, 7
+FGRID, FGRIDCNT, FGRIDOFF = 12, 13, 14
+GRID_UNDEF = 0xFFFFFFFF
+
+_VEC3 = {FPOS, FVEL, FVEVAL, FFORCE}
+_PER_CELL = {FGRIDCNT, FGRIDOFF}
+
+PHASES = ("insert", "prefix", "sort", "pressure", "force_advance")
+
+
+def default_params() -> FlParams:
+    """SetupDefaultParams (fluids4.0/fluid_system.cpp:1953-2041), example-3 box."""
+    p = FlParams()
+    call("fl_params_default", C.byref(p))
+    return p
+
+
+def derive_params(p: FlParams) -> FlParams:
+    """SetupSpacing/SetupGrid/FluidSetupCUDA/UpdateParamsCUDA restated in FP32."""
+    out = p.copy()
+    call("fl_params_derive", C.byref(out))
+    return out
+
+
+class PinnedArray:
+    """A numpy array in page-locked host memory (fl_host_alloc)."""
+
+    def __init__(self, shape, dtype):
+        dtype = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dtype.itemsize
+        ptr = C.c_void_p()
+        call("fl_host_alloc", max(nbytes, 16), C.byref(ptr))
+        self._ptr = ptr.value
+        raw = (C.c_uint8 * max(nbytes, 16)).from_address(self._ptr)
+        self.array = np.frombuffer(raw, dtype=np.uint8, count=nbytes).view(dtype).reshape(shape)
+
+    def free(self) -> None:
+        if self._ptr:
+            self.array = None
+            lib().fl_host_free(C.c_void_p(self._ptr))
+            self._ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def _ptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class FluidSystem:
+    """One SPH system on the current CUDA device.
+
+    ``FluidSystem(params, max_points)`` corresponds to Initialize + Start's
+    allocation (fluids4.0/fluid_system.cpp:92-168); particles are loaded with
+    :meth:`SetParticles` (TransferToCUDA). ``params`` must be derived.
+    """
+
+    def __init__(self, params: FlParams, max_points: int):
+        self._h = C.c_void_p()
+        call("fl_create", C.byref(params), int(max_points), C.byref(self._h))
+        self.max_points = int(max_points)
+
+    # -- lifetime -------------------------------------------------------------
+    def close(self) -> None:
+        if self._h:
+            lib().fl_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    # -- parameters -----------------------------------------------------------
+    @property
+    def params(self) -> FlParams:
+        p = FlParams()
+        call("fl_get_params", self._h, C.byref(p))
+        return p
+
+    def UpdateParams(self, params: FlParams) -> None:
+        call("fl_set_params", self._h, C.byref(params))
+
+    def NumPoints(self) -> int:
+        return lib().fl_num_points(self._h)
+
+    def getGridTotal(self) -> int:
+        return lib().fl_grid_total(self._h)
+
+    @property
+    def time(self) -> float:
+        t = C.c_float()
+        call("fl_get_time", self._h, C.byref(t))
+        return float(t.value)
+
+    @time.setter
+    def time(self, t: float) -> None:
+        call("fl_set_time", self._h, C.c_float(t))
+
+    # -- data -----------------------------------------------------------------
+    def SetParticles(self, pos, vel=None, veval=None, force=None, press=None, clr=None) -> None:
+        """TransferToCUDA (cpp:2312-2321) from (N,3) float32 / (N,) arrays."""
+        pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+        n = pos.shape[0]
+
+        def f3(a):
+            return None if a is None else np.ascontiguousarray(a, dtype=np.float32).reshape(n, 3)
+
+        def s1(a, dt):
+            return None if a is None else np.ascontiguousarray(a, dtype=dt).reshape(n)
+
+        arrs = (pos, f3(vel), f3(veval), f3(force), s1(press, np.float32), s1(clr, np.uint32))
+        call("fl_set_particles", self._h, n, *[_ptr(a) for a in arrs])
+
+    def GetBuffer(self, buf_id: int) -> np.ndarray:
+        """Read buffer ``buf_id`` back in fluid.h layout."""
+        n = self.getGridTotal() if buf_id in _PER_CELL else self.NumPoints()
+        if buf_id in _VEC3:
+            out = np.empty((n, 3), dtype=np.float32)
+        elif buf_id == FPRESS:
+            out = np.empty(n, dtype=np.float32)
+        else:
+            out = np.empty(n, dtype=np.uint32)
+        if n:
+            call("fl_get_buffer", self._h, int(buf_id), _ptr(out), out.nbytes)
+        return out
+
+    def state(self) -> dict:
+        """All per-point buffers and the grid, as numpy arrays."""
+        names = {FPOS: "pos", FVEL: "vel", FVEVAL: "veval", FFORCE: "force", FPRESS: "press",
+                 FCLR: "clr", FGCELL: "gcell", FGNDX: "gndx", FGRIDCNT: "gridcnt",
+                 FGRIDOFF: "gridoff"}
+        return {v: self.GetBuffer(k) for k, v in names.items()}
+
+    # -- phases (fluid_system.h:249-256) --------------------------------------
+    def InsertParticlesCUDA(self, readback: bool = False):
+        n, c = self.NumPoints(), self.getGridTotal()
+        if not readback:
+            call("fl_insert_particles", self._h, None, None, None)
+            return None
+        gcell = np.empty(n, np.uint32)
+        gndx = np.empty(n, np.uint32)
+        gcnt = np.empty(c, np.uint32)
+        call("fl_insert_particles", self._h, _ptr(gcell), _ptr(gndx), _ptr(gcnt))
+        return gcell, gndx, gcnt
+
+    def PrefixSumCellsCUDA(self, zero_offsets: int = 1, readback: bool = False):
+        if not readback:
+            call("fl_prefix_sum_cells", self._h, None, int(zero_offsets))
+            return None
+        goff = np.empty(self.getGridTotal(), np.uint32)
+        call("fl_prefix_sum_cells", self._h, _ptr(goff), int(zero_offsets))
+        return goff
+
+    def CountingSortFullCUDA(self, readback: bool = False):
+        if not readback:
+            call("fl_counting_sort_full", self._h, None)
+            return None
+        ppos = np.empty((self.NumPoints(), 3), np.float32)
+        call("fl_counting_sort_full", self._h, _ptr(ppos))
+        return ppos
+
+    def ComputePressureCUDA(self) -> None:
+        call("fl_compute_pressure", self._h)
+
+    def ComputeForceCUDA(self) -> None:
+        call("fl_compute_force", self._h)
+
+    def AdvanceCUDA(self, time: float, dt: float, ss: float) -> None:
+        call("fl_advance", self._h, C.c_float(time), C.c_float(dt), C.c_float(ss))
+
+    def Run(self) -> None:
+        """One RUN_GPU_FULL step (cpp:506-524) on the fused kernels, then time += dt."""
+        call("fl_run", self._h)
+
+    def RunSteps(self, nsteps: int) -> None:
+        """``nsteps`` Run steps replayed from a captured CUDA graph."""
+        call("fl_run_steps", self._h, int(nsteps))
+
+    def Sync(self) -> None:
+        call("fl_sync", self._h)
+
+    def DeviceStatus(self) -> int:
+        v = C.c_uint32()
+        call("fl_device_status", self._h, C.byref(v))
+        return int(v.value)
+
+    def IntegrityCheck(self) -> int:
+        """IntegrityCheck (cpp:2426-2453): number of inconsistent sorted slots."""
+        bad = C.c_int64()
+        call("fl_integrity_check", self._h, C.byref(bad))
+        return int(bad.value)
+
+    # -- timing ---------------------------------------------------------------
+    def SetTiming(self, enable: bool) -> None:
+        call("fl_set_timing", self._h, 1 if enable else 0)
+
+    def TimeSteps(self, nsteps: int, graph: bool = True) -> float:
+        """Device milliseconds for ``nsteps`` Run steps, CUDA events on the system stream."""
+        ms = C.c_double()
+        call("fl_time_steps", self._h, int(nsteps), 1 if graph else 0, C.byref(ms))
+        return float(ms.value)
+
+    def PhaseTimes(self) -> tuple[dict, int]:
+        ms = (C.c_double * 8)()
+        steps = C.c_int()
+        call("fl_get_phase_times", self._h, ms, C.byref(steps))
+        names = ("insert", "scan", "scatter", "sort", "density", "force_advance")
+        return {k: float(ms[i]) for i, k in enumerate(names)}, int(steps.value)
+
+    def stream(self) -> int:
+        return int(lib().fl_stream(self._h) or 0)
+
+
+__all__ = ["FluidSystem", "PinnedArray", "default_params", "derive_params", "FPOS", "FVEL", "FVEVAL",
+           "FFORCE", "FPRESS", "FCLR", "FGCELL", "FGNDX", "FGRID", "FGRIDCNT", "FGRIDOFF",
+           "GRID_UNDEF", "_lib"]

@@ -1,0 +1,244 @@
+/*
+ * fluids_gb300.h -- C ABI of the GB300 (sm_103a) SPH time step.
+ *
+ * Drop-in for the GPU pathway of the reference's FluidSystem
+ * (fluids4.0/fluid_system.h:145-353): the same phases, the same buffer ids
+ * and host layouts (fluids4.0/fluid.h:45-70), the same derived parameters
+ * (fluids4.0/fluid.h:155-192), behind plain pointers and status codes.
+ *
+ *   reference (fluids4.0)                          this ABI
+ *   -------------------------------------------    ---------------------------
+ *   FluidSystem::Initialize + Start (cpp:92-168)   fl_params_default/derive, fl_create
+ *   SetupSpacing/SetupGrid/FluidSetupCUDA/
+ *     UpdateParamsCUDA (cpp:2099,793,2249,2289)    fl_params_derive, fl_set_params
+ *   TransferToCUDA (cpp:2312-2321)                 fl_set_particles
+ *   TransferFromCUDA (cpp:2323-2330)               fl_get_buffer
+ *   InsertParticlesCUDA (cpp:2334-2350)            fl_insert_particles
+ *   PrefixSumCellsCUDA (cpp:2354-2424)             fl_prefix_sum_cells
+ *   CountingSortFullCUDA (cpp:2455-2479)           fl_counting_sort_full
+ *   ComputePressureCUDA (cpp:2515-2519)            fl_compute_pressure
+ *   ComputeForceCUDA (cpp:2521-2525)               fl_compute_force
+ *   AdvanceCUDA (cpp:2527-2531)                    fl_advance
+ *   Run, case RUN_GPU_FULL (cpp:506-524)           fl_run / fl_run_steps
+ *   IntegrityCheck (cpp:2426-2453)                 fl_integrity_check
+ *
+ * Errors: every call returns FL_OK (0) or a negative FL_ERR_* code and never
+ * exits the process (the reference prints and calls exit(-1), cpp:26-55).
+ * fl_last_error() gives a message for the calling thread's last failure.
+ *
+ * Threading: one fl_system is driven by one host thread at a time. All
+ * device work of a system is issued on its own CUDA stream; calls that hand
+ * results to host memory synchronise that stream before returning.
+ */
+#ifndef FLUIDS_GB300_H
+#define FLUIDS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FL_ABI_VERSION 1
+
+/* Buffer ids, numbered as in fluids4.0/fluid.h:45-70. */
+#define FL_FPOS      0   /* float3 [N] position, world units          */
+#define FL_FVEL      1   /* float3 [N] velocity v(t+1/2)               */
+#define FL_FVEVAL    2   /* float3 [N] evaluated velocity v(t)         */
+#define FL_FFORCE    3   /* float3 [N] SPH force (before mass scaling) */
+#define FL_FPRESS    4   /* float  [N] density (named press upstream)  */
+#define FL_FCLR      5   /* uint   [N] RGBA8 colour                    */
+#define FL_FGCELL    6   /* uint   [N] grid cell or FL_GRID_UNDEF      */
+#define FL_FGNDX     7   /* uint   [N] index within the cell           */
+#define FL_FGRID     12  /* uint   [N] sorted-slot lookup (identity)   */
+#define FL_FGRIDCNT  13  /* uint   [C] particles per cell              */
+#define FL_FGRIDOFF  14  /* uint   [C] first sorted slot of each cell  */
+
+#define FL_GRID_UNDEF 0xFFFFFFFFu   /* GRID_UNDEF, fluids4.0/fluid_kernels.cuh:19 */
+#define FL_MAX_GRID_SRCH 6          /* fatal above this, fluids4.0/fluid_system.cpp:830-833 */
+
+/* Status codes. */
+#define FL_OK             0
+#define FL_ERR_ARG       -1   /* null pointer, bad id, size out of range        */
+#define FL_ERR_CUDA      -2   /* a CUDA runtime call failed                      */
+#define FL_ERR_PARAMS    -3   /* parameters give an unusable grid (gridSrch > 6) */
+#define FL_ERR_CAPACITY  -4   /* more points than the system was created for    */
+#define FL_ERR_DEVICE    -5   /* a kernel raised its device error word           */
+#define FL_ERR_STATE     -6   /* phase called before the phase it depends on     */
+#define FL_ERR_NOMEM     -7   /* device allocation failed                        */
+
+/* Device error word bits (fl_device_status). */
+#define FL_DEV_SPIN_TIMEOUT  0x1u  /* a look-back wait hit its iteration limit */
+#define FL_DEV_BAD_CELL      0x2u  /* a cell index outside [0, C] was seen     */
+#define FL_DEV_NONFINITE     0x4u  /* a non-finite position was advanced       */
+
+/*
+ * Simulation parameters: inputs (first block) and the fields that
+ * fl_params_derive computes from them (second block). Names follow FParams
+ * (fluids4.0/fluid.h:155-192). All float arithmetic of the derivation is
+ * FP32 in the reference's own operation order, so grids and kernels match
+ * the reference bit for bit on the same inputs.
+ */
+typedef struct fl_params {
+    /* inputs: SetupDefaultParams / SetupExampleParams (fluid_system.cpp:1953-2097) */
+    float sim_scale;          /* world units -> metres                       */
+    float pvisc;              /* viscosity                                   */
+    float prest_dens;         /* rest density                                */
+    float pmass;              /* particle mass                               */
+    float pradius;            /* collision radius used by the walls          */
+    float psmoothradius;      /* SPH support radius h (metres)               */
+    float pintstiff;          /* pressure stiffness                          */
+    float bound_stiff;        /* wall stiffness                              */
+    float bound_damp;         /* wall damping                                */
+    float bound_slope;        /* Y- wall slope along x                       */
+    float bound_friction;     /* friction on the Y walls                     */
+    float bound_wall_force;   /* amplitude of the moving X- wall             */
+    float bound_wall_freq;    /* frequency of the moving X- wall             */
+    float AL;                 /* acceleration limit                          */
+    float VL;                 /* velocity limit                              */
+    float grav_dir[3];        /* gravity direction * magnitude               */
+    float grav_amt;           /* gravity multiplier                          */
+    float bound_min[3];       /* domain walls, world units                   */
+    float bound_max[3];
+    float grid_density;       /* cell = 1.5 * h / grid_density (cpp:2101)    */
+    float dt;                 /* time step m_DT                              */
+
+    /* derived: SetupSpacing (grid part), SetupGrid, FluidSetupCUDA, UpdateParamsCUDA */
+    float grid_size;          /* cell edge in metres                         */
+    float r2, d2, rd2;        /* h^2, sim_scale^2, h^2/sim_scale^2           */
+    float poly6kern, spikykern, lapkern, vterm;
+    float AL2, VL2;
+    float gravity[3];
+    float pdist;
+    float gridMin[3], gridMax[3], gridSize[3], gridDelta[3];
+    int   gridRes[3];
+    int   gridScanMax[3];
+    int   gridSrch;           /* cells searched per axis, 2..6               */
+    int   gridTotal;          /* C = resX*resY*resZ                          */
+    int   gridAdjCnt;         /* gridSrch^3                                  */
+    int   gridAdj[216];       /* cell offsets of the search block            */
+} fl_params;
+
+typedef struct fl_system fl_system;
+
+/* ---- parameters ---------------------------------------------------------- */
+
+/* SetupDefaultParams (fluid_system.cpp:1953-2041) with grid_density 2.0
+ * (cpp:125) and the example-3 "small dam break" box (cpp:2081-2088). */
+int fl_params_default(fl_params *p);
+
+/* Fill the derived block from the inputs: SetupSpacing's grid bounds
+ * (cpp:2101,2114-2116), SetupGrid (cpp:793-846), FluidSetupCUDA's scan
+ * limits and adjacency (cpp:2249-2287), UpdateParamsCUDA (cpp:2289-2310).
+ * Returns FL_ERR_PARAMS when gridSrch > 6 or the grid is empty. */
+int fl_params_derive(fl_params *p);
+
+/* ---- lifetime ------------------------------------------------------------ */
+
+/* Initialize + AllocateParticles + AllocateGrid (cpp:92-130, 218-272) on the
+ * current CUDA device. `p` must already be derived. */
+int fl_create(const fl_params *p, int max_points, fl_system **out);
+int fl_destroy(fl_system *s);
+
+/* UpdateParamsCUDA (cpp:2289-2310): replace the parameter block. A block
+ * with a different grid reallocates the grid buffers. */
+int fl_set_params(fl_system *s, const fl_params *p);
+int fl_get_params(const fl_system *s, fl_params *p);
+
+int fl_num_points(const fl_system *s);
+int fl_grid_total(const fl_system *s);
+/* Simulation time m_Time, advanced by dt on every fl_run (AdvanceTime, cpp:527-531). */
+int fl_get_time(const fl_system *s, float *t);
+int fl_set_time(fl_system *s, float t);
+
+/* ---- data movement (fluid.h host layout: float3 packed 12 B, uint 4 B) --- */
+
+/* TransferToCUDA (cpp:2312-2321): n points from host SoA arrays. pos is
+ * required; any other pointer may be NULL (zero-filled). */
+int fl_set_particles(fl_system *s, int n, const float *pos, const float *vel,
+                     const float *veval, const float *force, const float *press,
+                     const uint32_t *clr);
+
+/* Copy buffer `buf_id` (FL_F* id) into host memory in fluid.h layout.
+ * `bytes` must be at least the buffer size (N or C elements). */
+int fl_get_buffer(fl_system *s, int buf_id, void *host_dst, size_t bytes);
+
+/* Page-locked host memory for the transfer calls above (transfers from it
+ * run at full link speed and overlap with other streams). */
+int fl_host_alloc(size_t bytes, void **out);
+int fl_host_free(void *p);
+
+/* Device-side export/import in fluid.h layout (headless stand-in for the
+ * reference's CUDA-GL interop buffers, cpp:196-204). `dev` is a device
+ * pointer on the system's device; the copy is ordered on the system stream. */
+int fl_export_device(fl_system *s, int buf_id, void *dev, size_t bytes);
+int fl_import_device(fl_system *s, int n, const void *dev_pos, const void *dev_vel,
+                     const void *dev_veval);
+
+/* ---- phases (fluid_system.h:249-256) ------------------------------------- */
+
+/* InsertParticlesCUDA (cpp:2334-2350; kernel fluid_kernels.cu:22-53).
+ * gcell/gndx (N) and gcnt (C) are optional host readbacks. gndx is the
+ * canonical within-cell index: the number of lower-indexed points in the
+ * same cell (the serial reference's cnt++ order, fluids3.9 cpp:489). */
+int fl_insert_particles(fl_system *s, uint32_t *gcell, uint32_t *gndx, uint32_t *gcnt);
+
+/* PrefixSumCellsCUDA (cpp:2354-2424; kernels fluid_kernels.cu:423-467):
+ * zero_offsets=1 gives the exclusive scan of FGRIDCNT into FGRIDOFF,
+ * zero_offsets=0 the inclusive scan. goff (C) is an optional readback. */
+int fl_prefix_sum_cells(fl_system *s, uint32_t *goff, int zero_offsets);
+
+/* CountingSortFullCUDA (cpp:2455-2479; kernel fluid_kernels.cu:56-87):
+ * permutes all particle buffers to slot FGRIDOFF[cell]+gndx. Points outside
+ * the scan range go to the tail in index order (upstream leaves stale
+ * copies there). ppos (N float3) is an optional readback. */
+int fl_counting_sort_full(fl_system *s, float *ppos);
+
+/* ComputePressureCUDA (cpp:2515-2519; kernel fluid_kernels.cu:112-149). */
+int fl_compute_pressure(fl_system *s);
+/* ComputeForceCUDA (cpp:2521-2525; kernel fluid_kernels.cu:180-217). */
+int fl_compute_force(fl_system *s);
+/* AdvanceCUDA (cpp:2527-2531; kernel fluid_kernels.cu:332-420). */
+int fl_advance(fl_system *s, float time, float dt, float ss);
+
+/* Run (cpp:475-525, RUN_GPU_FULL): one full step on the fused kernel
+ * sequence, then time += dt. Asynchronous: no host sync. */
+int fl_run(fl_system *s);
+/* nsteps consecutive Run steps replayed from a captured CUDA graph. */
+int fl_run_steps(fl_system *s, int nsteps);
+
+/* Wait for the system stream; returns FL_ERR_DEVICE if a kernel raised the
+ * device error word since the last fl_sync (bits in *dev_flags if non-NULL). */
+int fl_sync(fl_system *s);
+int fl_device_status(fl_system *s, uint32_t *dev_flags);
+
+/* IntegrityCheck (cpp:2426-2453): number of sorted slots whose cell/index
+ * disagree with FGRIDOFF/FGRIDCNT (0 when the grid is consistent). */
+int fl_integrity_check(fl_system *s, int64_t *bad);
+
+/* Per-phase device timing, the counterpart of the PERF_PUSH/PERF_POP pairs
+ * around each phase of Run (cpp:507-515). While enabled, fl_run brackets
+ * every launch with CUDA events on the system stream (up to 4096 steps).
+ * fl_get_phase_times synchronises and returns the mean milliseconds per
+ * step of each phase: [0] clear+insert, [1] scan, [2] index scatter,
+ * [3] canonical sort+gather, [4] density, [5] force+advance; *steps gets
+ * the number of timed steps. Enabling again resets the accumulators. */
+int fl_set_timing(fl_system *s, int enable);
+/* Run nsteps steps (graph replay when use_graph != 0, else eager fl_run)
+ * between two CUDA events on the system stream; synchronises and stores the
+ * elapsed device time in *ms. */
+int fl_time_steps(fl_system *s, int nsteps, int use_graph, double *ms);
+int fl_get_phase_times(fl_system *s, double ms[8], int *steps);
+
+/* The CUDA stream (cudaStream_t) the system issues its work on. */
+void *fl_stream(fl_system *s);
+
+/* Message for the calling thread's most recent failed call. */
+const char *fl_last_error(void);
+int fl_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLUIDS_GB300_H */

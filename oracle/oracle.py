@@ -1,0 +1,257 @@
+"""TEST INFRASTRUCTURE ONLY: Python access to the CPU oracle.
+
+Two host libraries, both built from C/C++ in this directory:
+  _build/libfluids_oracle.so  -- fluids_oracle.c, the C restatement (FP32 in
+                                  the reference's operation order + FP64)
+  _ref/libfluids_ref.so       -- the reference's own fluids4.0/fluid_kernels.cu
+                                  compiled for the host (only where the
+                                  reference tree was present at build time)
+
+Only tests/, bench.py's CPU arm and __graft_entry__.smoke() import this
+module, and only to check or time the CUDA path -- never as the product.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ORACLE_LIB = HERE / "_build" / "libfluids_oracle.so"
+REF_LIB = HERE / "_ref" / "libfluids_ref.so"
+
+_orc = None
+_ref = None
+
+
+def build(ref: bool = True) -> None:
+    subprocess.run(["bash", str(HERE / "build_oracle.sh")], check=True)
+    if ref:
+        subprocess.run(["bash", str(HERE / "build_ref.sh")], check=True)
+
+
+def params_from_bytes(raw) -> "FlParams":
+    """FlParams from its exact bytes (as stored in the golden fixtures)."""
+    from fluids3_gb300.params import FlParams
+    raw = bytes(bytearray(raw))
+    p = FlParams()
+    if len(raw) != C.sizeof(FlParams):
+        raise ValueError(f"params blob is {len(raw)} bytes, FlParams is {C.sizeof(FlParams)}")
+    C.memmove(C.byref(p), raw, len(raw))
+    return p
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def orc():
+    global _orc
+    if _orc is None:
+        if not ORACLE_LIB.exists():
+            build(ref=False)
+        _orc = C.CDLL(str(ORACLE_LIB))
+        vp, i, f = C.c_void_p, C.c_int, C.c_float
+        _orc.orc_insert.argtypes = [vp, i, vp, vp, vp, vp]
+        _orc.orc_prefix_sum.argtypes = [i, vp, vp]
+        _orc.orc_counting_sort.argtypes = [vp, i, vp] + [vp] * 16
+        _orc.orc_density.argtypes = [vp, i, vp, vp, vp, vp, vp, i]
+        _orc.orc_force.argtypes = [vp, i, vp, vp, vp, vp, vp, vp, vp, i]
+        _orc.orc_advance.argtypes = [vp, i, f, f, f, vp, vp, vp, vp, vp, i]
+        _orc.orc_density_f64.argtypes = [vp, i, vp, vp, vp, vp, vp, i]
+        _orc.orc_force_f64.argtypes = [vp, i, vp, vp, vp, vp, vp, vp, vp, vp, i]
+        _orc.orc_run.argtypes = [vp, i, i, C.POINTER(f), i] + [vp] * 18
+    return _orc
+
+
+def ref_available() -> bool:
+    return REF_LIB.exists()
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        if not REF_LIB.exists():
+            raise FileNotFoundError("oracle/_ref/libfluids_ref.so is not built (reference tree absent)")
+        _ref = C.CDLL(str(REF_LIB))
+        vp, i, f = C.c_void_p, C.c_int, C.c_float
+        _ref.ref_set_params.argtypes = [vp]
+        _ref.ref_set_params.restype = i
+        _ref.ref_bind.argtypes = [i, vp]
+        _ref.ref_insert.argtypes = [i]
+        _ref.ref_prefix_sum.argtypes = [i]
+        _ref.ref_counting_sort.argtypes = [i]
+        _ref.ref_compute_pressure.argtypes = [i, i]
+        _ref.ref_compute_force.argtypes = [i, i]
+        _ref.ref_advance.argtypes = [f, f, f, i, i]
+        _ref.ref_run.argtypes = [i, i, C.POINTER(f), f, i]
+    return _ref
+
+
+# ---------------------------------------------------------------------------
+@dataclass
+class State:
+    """Host SPH state in fluid.h layout."""
+    pos: np.ndarray
+    vel: np.ndarray
+    veval: np.ndarray
+    force: np.ndarray
+    press: np.ndarray
+    clr: np.ndarray
+    gcell: np.ndarray
+    gndx: np.ndarray
+    cnt: np.ndarray      # C + 1 (entry C: out-of-range bin)
+    off: np.ndarray      # C + 1
+
+    @staticmethod
+    def new(params, pos, vel=None, veval=None, clr=None) -> "State":
+        n = pos.shape[0]
+        c = params.gridTotal + 1
+        z3 = lambda a: np.zeros((n, 3), np.float32) if a is None else np.array(a, np.float32).reshape(n, 3)
+        return State(pos=np.array(pos, np.float32).reshape(n, 3), vel=z3(vel), veval=z3(veval),
+                     force=np.zeros((n, 3), np.float32), press=np.zeros(n, np.float32),
+                     clr=np.zeros(n, np.uint32) if clr is None else np.array(clr, np.uint32),
+                     gcell=np.zeros(n, np.uint32), gndx=np.zeros(n, np.uint32),
+                     cnt=np.zeros(c, np.uint32), off=np.zeros(c, np.uint32))
+
+    def copy(self) -> "State":
+        return State(**{k: v.copy() for k, v in self.__dict__.items()})
+
+    @property
+    def n(self) -> int:
+        return self.pos.shape[0]
+
+
+def insert(params, st: State) -> None:
+    orc().orc_insert(C.byref(params), st.n, _p(st.pos), _p(st.gcell), _p(st.gndx), _p(st.cnt))
+
+
+def prefix_sum(params, st: State) -> None:
+    orc().orc_prefix_sum(params.gridTotal + 1, _p(st.cnt), _p(st.off))
+
+
+def counting_sort(params, st: State) -> None:
+    out = State.new(params, st.pos)
+    orc().orc_counting_sort(C.byref(params), st.n, _p(st.off),
+                            *[_p(a) for a in (st.pos, st.vel, st.veval, st.force, st.press, st.clr, st.gcell, st.gndx)],
+                            *[_p(a) for a in (out.pos, out.vel, out.veval, out.force, out.press, out.clr, out.gcell, out.gndx)])
+    for k in ("pos", "vel", "veval", "force", "press", "clr", "gcell", "gndx"):
+        setattr(st, k, getattr(out, k))
+
+
+def density(params, st: State, threads: int = 1) -> None:
+    orc().orc_density(C.byref(params), st.n, _p(st.pos), _p(st.gcell), _p(st.off), _p(st.cnt),
+                      _p(st.press), threads)
+
+
+def force(params, st: State, threads: int = 1) -> None:
+    orc().orc_force(C.byref(params), st.n, _p(st.pos), _p(st.veval), _p(st.press), _p(st.gcell),
+                    _p(st.off), _p(st.cnt), _p(st.force), threads)
+
+
+def advance(params, st: State, time: float, dt: float, ss: float, threads: int = 1) -> None:
+    orc().orc_advance(C.byref(params), st.n, C.c_float(time), C.c_float(dt), C.c_float(ss),
+                      _p(st.gcell), _p(st.force), _p(st.pos), _p(st.vel), _p(st.veval), threads)
+
+
+def density_f64(params, pos, gcell, off, cnt, threads: int = 1) -> np.ndarray:
+    out = np.zeros(pos.shape[0], np.float64)
+    orc().orc_density_f64(C.byref(params), pos.shape[0], _p(pos), _p(gcell), _p(off), _p(cnt),
+                          _p(out), threads)
+    return out
+
+
+def force_f64(params, pos, veval, press, gcell, off, cnt, threads: int = 1):
+    """(force, scale): FP64 force and, per point, the sum of its pair-term magnitudes."""
+    out = np.zeros((pos.shape[0], 3), np.float64)
+    scale = np.zeros(pos.shape[0], np.float64)
+    orc().orc_force_f64(C.byref(params), pos.shape[0], _p(pos), _p(veval), _p(press), _p(gcell),
+                        _p(off), _p(cnt), _p(out), _p(scale), threads)
+    return out, scale
+
+
+def step(params, st: State, time: float, threads: int = 1) -> float:
+    """One Run step (RUN_GPU_FULL order); returns the new time."""
+    insert(params, st)
+    prefix_sum(params, st)
+    counting_sort(params, st)
+    density(params, st, threads)
+    force(params, st, threads)
+    advance(params, st, time, params.dt, params.sim_scale, threads)
+    return float(np.float32(np.float32(time) + np.float32(params.dt)))
+
+
+def run(params, st: State, steps: int, time: float, threads: int = 1) -> float:
+    """`steps` steps in C (no Python per phase); returns the new time."""
+    t = C.c_float(time)
+    s2 = State.new(params, st.pos)
+    orc().orc_run(C.byref(params), st.n, steps, C.byref(t), threads,
+                  *[_p(a) for a in (st.pos, st.vel, st.veval, st.force, st.press, st.clr, st.gcell, st.gndx)],
+                  *[_p(a) for a in (s2.pos, s2.vel, s2.veval, s2.force, s2.press, s2.clr, s2.gcell, s2.gndx)],
+                  _p(st.cnt), _p(st.off))
+    return float(t.value)
+
+
+# ---------------------------------------------------------------------------
+class RefKernels:
+    """The reference kernels run on the host (tier 1). Buffers are numpy
+    arrays in fluid.h layout bound into the kernels' fbuf table."""
+
+    IDS = dict(pos=0, vel=1, veval=2, force=3, press=4, clr=5, gcell=6, gndx=7,
+               grid=12, gridcnt=13, gridoff=14)
+
+    def __init__(self, params, pos, vel=None, veval=None, clr=None):
+        self.lib = ref()
+        self.params = params
+        if self.lib.ref_set_params(C.byref(params)) != 0:
+            raise ValueError("reference FParams holds at most 64 adjacency entries")
+        n = pos.shape[0]
+        self.n = n
+        z3 = lambda a: np.zeros((n, 3), np.float32) if a is None else np.array(a, np.float32).reshape(n, 3)
+        self.buf = dict(pos=np.array(pos, np.float32).reshape(n, 3), vel=z3(vel), veval=z3(veval),
+                        force=np.zeros((n, 3), np.float32), press=np.zeros(n, np.float32),
+                        clr=np.zeros(n, np.uint32) if clr is None else np.array(clr, np.uint32),
+                        gcell=np.zeros(n, np.uint32), gndx=np.zeros(n, np.uint32),
+                        grid=np.zeros(n, np.uint32),
+                        gridcnt=np.zeros(params.gridTotal, np.uint32),
+                        gridoff=np.zeros(params.gridTotal, np.uint32))
+        for k, a in self.buf.items():
+            self.lib.ref_bind(self.IDS[k], _p(a))
+
+    def rebind(self):
+        self.lib.ref_set_params(C.byref(self.params))
+        for k, a in self.buf.items():
+            self.lib.ref_bind(self.IDS[k], _p(a))
+
+    def insert(self):
+        self.rebind()
+        self.lib.ref_insert(self.n)
+
+    def prefix_sum(self, zero_offsets=1):
+        self.rebind()
+        self.lib.ref_prefix_sum(zero_offsets)
+
+    def counting_sort(self):
+        self.rebind()
+        self.lib.ref_counting_sort(self.n)
+
+    def pressure(self, threads=1):
+        self.rebind()
+        self.lib.ref_compute_pressure(self.n, threads)
+
+    def force(self, threads=1):
+        self.rebind()
+        self.lib.ref_compute_force(self.n, threads)
+
+    def advance(self, time, dt, ss, threads=1):
+        self.rebind()
+        self.lib.ref_advance(C.c_float(time), C.c_float(dt), C.c_float(ss), self.n, threads)
+
+    def run(self, steps, time, threads=1) -> float:
+        self.rebind()
+        t = C.c_float(time)
+        self.lib.ref_run(self.n, steps, C.byref(t), C.c_float(self.params.dt), threads)
+        return float(t.value)

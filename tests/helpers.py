@@ -1,0 +1,53 @@
+"""Shared checks for the parity tests."""
+from __future__ import annotations
+
+import hashlib
+
+import numpy as np
+
+FIELDS = ("pos", "vel", "veval", "force", "press", "clr", "gcell", "gndx")
+
+
+def bits(a: np.ndarray) -> np.ndarray:
+    """The raw 32-bit patterns (bit-exact comparison, NaN-safe)."""
+    a = np.ascontiguousarray(a)
+    return a.view(np.uint32)
+
+
+def assert_bit_equal(got: np.ndarray, want: np.ndarray, what: str) -> None:
+    got, want = np.asarray(got), np.asarray(want)
+    assert got.shape == want.shape, f"{what}: shape {got.shape} != {want.shape}"
+    g, w = bits(got).reshape(-1), bits(want).reshape(-1)
+    bad = np.nonzero(g != w)[0]
+    if bad.size:
+        k = bad[0]
+        raise AssertionError(f"{what}: {bad.size} of {g.size} words differ; first at flat index {k}: "
+                             f"{got.reshape(-1)[k]!r} != {want.reshape(-1)[k]!r}")
+
+
+def digest(buf: dict) -> str:
+    h = hashlib.sha256()
+    for k in FIELDS:
+        h.update(np.ascontiguousarray(buf[k]).tobytes())
+    return h.hexdigest()
+
+
+def density_rel_err(got, ref64, mask) -> float:
+    """Max relative error of densities against the FP64 oracle (density is a
+    sum of positive terms, so its own magnitude is its error scale)."""
+    g = np.asarray(got, np.float64)[mask]
+    r = np.asarray(ref64, np.float64)[mask]
+    return float(np.max(np.abs(g - r) / np.abs(r))) if r.size else 0.0
+
+
+def force_rel_err(got, ref64, scale64, mask) -> float:
+    """Max per-point force error against the FP64 oracle, relative to the
+    point's force scale: the sum of the magnitudes of its pair terms (an
+    FP32 sum's error is bounded by a multiple of that, even when the terms
+    cancel)."""
+    g = np.asarray(got, np.float64)[mask]
+    r = np.asarray(ref64, np.float64)[mask]
+    s = np.asarray(scale64, np.float64)[mask]
+    err = np.linalg.norm(g - r, axis=1)
+    s = np.where(s > 0, s, 1.0)
+    return float(np.max(err / s)) if r.size else 0.0

@@ -1,0 +1,323 @@
+"""GPU parity tests: the CUDA path, called through the C ABI, against the
+golden fixtures (made by the reference's own kernel source) and against the
+CPU oracle on the same inputs.
+
+Bar: integer outputs (cells, counts, offsets, permutation) bit-exact; the
+kernels evaluate every float expression in the reference's order without
+FMA contraction, so density, force and advance are bit-exact as well
+except for the moving X- wall (CUDA sinf vs the host's sinf, plus the
+reference's double-precision wall product), which is held to the stated
+tolerances instead: density <= 1e-5 relative, force <= 1e-4 of its scale.
+"""
+from __future__ import annotations
+
+import json
+
+import numpy as np
+import pytest
+
+import fluids3_gb300 as F
+from fluids3_gb300 import scenes
+from oracle import oracle as O
+
+from helpers import FIELDS, assert_bit_equal, density_rel_err, digest, force_rel_err
+
+pytestmark = pytest.mark.gpu
+UNDEF = 0xFFFFFFFF
+
+
+def gpu_state(s: F.FluidSystem) -> dict:
+    return s.state()
+
+
+def make_system(params, pos, vel=None, veval=None, clr=None, capacity=None) -> F.FluidSystem:
+    s = F.FluidSystem(params, capacity if capacity is not None else max(1, pos.shape[0]))
+    s.SetParticles(pos, vel, veval, clr=clr)
+    return s
+
+
+def load_2000(golden_dir):
+    g = np.load(golden_dir / "dam_break_2000.npz")
+    return g, O.params_from_bytes(g["params"])
+
+
+def test_phases_match_reference_fixture(golden_dir):
+    g, p = load_2000(golden_dir)
+    with make_system(p, g["in_pos"], g["in_vel"], g["in_veval"], g["in_clr"]) as s:
+        gcell, gndx, gcnt = s.InsertParticlesCUDA(readback=True)
+        assert_bit_equal(gcell, g["ins_gcell"], "insert gcell")
+        assert_bit_equal(gndx, g["ins_gndx"], "insert gndx (canonical)")
+        assert_bit_equal(gcnt, g["ins_gridcnt"], "insert gridcnt")
+        goff = s.PrefixSumCellsCUDA(1, readback=True)
+        assert_bit_equal(goff, g["gridoff"], "gridoff")
+        ppos = s.CountingSortFullCUDA(readback=True)
+        assert_bit_equal(ppos, g["sort_pos"], "sorted pos readback")
+        st = gpu_state(s)
+        for k in ("pos", "vel", "veval", "clr", "gcell", "gndx"):
+            assert_bit_equal(st[k], g[f"sort_{k}"], f"sorted {k}")
+        assert s.IntegrityCheck() == 0
+        grid = s.GetBuffer(F.FGRID)
+        assert (grid == np.arange(grid.size)).all()
+        s.ComputePressureCUDA()
+        assert_bit_equal(s.GetBuffer(F.FPRESS), g["press"], "density")
+        s.ComputeForceCUDA()
+        assert_bit_equal(s.GetBuffer(F.FFORCE), g["force"], "force")
+        s.AdvanceCUDA(0.0, p.dt, p.sim_scale)
+        st = gpu_state(s)
+        for k in ("pos", "vel", "veval"):
+            assert_bit_equal(st[k], g[f"adv_{k}"], f"advanced {k}")
+        s.Sync()
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_run_rollout_matches_reference_fixture(golden_dir, graph):
+    g, p = load_2000(golden_dir)
+    with make_system(p, g["in_pos"], g["in_vel"], g["in_veval"], g["in_clr"]) as s:
+        if graph:
+            s.RunSteps(20)
+        else:
+            for _ in range(20):
+                s.Run()
+        s.Sync()
+        st = gpu_state(s)
+        for k in FIELDS:
+            assert_bit_equal(st[k], g[f"s20_{k}"], f"step-20 {k} ({'graph' if graph else 'eager'})")
+        assert np.float32(s.time) == g["s20_time"]
+        assert s.IntegrityCheck() == 0
+
+
+def test_dam_break_32k_digests(golden_dir):
+    rec = json.loads((golden_dir / "digests.json").read_text())["dam_break_32k"]
+    p = O.params_from_bytes(bytes.fromhex(rec["params"]))
+    sc = scenes.dam_break()
+    with make_system(p, sc.pos, sc.vel, sc.veval, sc.clr) as s:
+        done = 0
+        for key in ("step_1", "step_10", "step_30", "step_60"):
+            m = int(key[5:])
+            s.RunSteps(m - done)
+            done = m
+            s.Sync()
+            assert digest(gpu_state(s)) == rec[key], f"32k dam break diverged from the reference by step {m}"
+
+
+def test_graph_and_eager_agree_with_odd_counts():
+    sc = scenes.dam_break(n=5000, seed=9)
+    with make_system(sc.params, sc.pos, sc.vel, sc.veval, sc.clr) as a, \
+            make_system(sc.params, sc.pos, sc.vel, sc.veval, sc.clr) as b:
+        for k in (3, 1, 4, 5):
+            a.RunSteps(k)
+            for _ in range(k):
+                b.Run()
+        a.Sync(); b.Sync()
+        sa, sb = gpu_state(a), gpu_state(b)
+        for k in FIELDS:
+            assert_bit_equal(sa[k], sb[k], f"graph vs eager {k}")
+        assert a.time == b.time
+
+
+def oracle_step_check(s: F.FluidSystem, p, time: float, exact_fp: bool):
+    """Feed the GPU's current state to the oracle, take one step on both, and
+    compare: integers always bit-exact; floats bit-exact or within tolerance."""
+    st0 = gpu_state(s)
+    ref = O.State.new(p, st0["pos"], st0["vel"], st0["veval"], st0["clr"])
+    O.insert(p, ref)
+    O.prefix_sum(p, ref)
+    O.counting_sort(p, ref)
+    O.density(p, ref, threads=8)
+    O.force(p, ref, threads=8)
+    pre_adv = ref.copy()
+    O.advance(p, ref, time, p.dt, p.sim_scale, threads=8)
+    s.Run()
+    s.Sync()
+    st = gpu_state(s)
+    for k in ("gcell", "gndx", "clr"):
+        assert_bit_equal(st[k], getattr(ref, k), f"{k}")
+    assert_bit_equal(st["gridcnt"], ref.cnt[:-1], "gridcnt")
+    assert_bit_equal(st["gridoff"], ref.off[:-1], "gridoff")
+    if exact_fp:
+        for k in ("press", "force", "pos", "vel", "veval"):
+            assert_bit_equal(st[k], getattr(ref, k), k)
+    else:
+        m = ref.gcell != UNDEF
+        assert_bit_equal(st["press"], ref.press, "density (walls do not enter it)")
+        d64 = O.density_f64(p, pre_adv.pos, pre_adv.gcell, pre_adv.off, pre_adv.cnt, threads=8)
+        assert density_rel_err(st["press"], d64, m) <= 1e-5
+        f64, scale = O.force_f64(p, pre_adv.pos, pre_adv.veval, pre_adv.press, pre_adv.gcell,
+                                 pre_adv.off, pre_adv.cnt, threads=8)
+        assert force_rel_err(st["force"], f64, scale, m) <= 1e-4
+        # positions: the wall term may differ by an ulp of sin; one step moves
+        # a point by at most VL*dt/ss, so compare to that scale
+        step_len = p.VL * p.dt / p.sim_scale
+        assert np.max(np.abs(st["pos"][m] - ref.pos[m])) <= 1e-4 * step_len + 1e-5
+    return st
+
+
+def test_wave_tank_per_step_against_oracle():
+    sc = scenes.wave_tank(n=200_000)
+    p = sc.params
+    with make_system(p, sc.pos, sc.vel, sc.veval, sc.clr) as s:
+        s.RunSteps(30)
+        s.Sync()
+        for _ in range(3):
+            oracle_step_check(s, p, s.time, exact_fp=False)
+
+
+def test_dam_break_per_step_exact_against_oracle():
+    sc = scenes.dam_break(n=20_000, seed=4)
+    p = sc.params
+    with make_system(p, sc.pos, sc.vel, sc.veval, sc.clr) as s:
+        s.RunSteps(40)
+        s.Sync()
+        for _ in range(3):
+            oracle_step_check(s, p, s.time, exact_fp=True)
+
+
+# ---- edge cases -------------------------------------------------------------
+
+@pytest.mark.parametrize("n", [0, 1, 31, 33, 255, 257, 1001])
+def test_small_and_ragged_sizes(n):
+    sc = scenes.dam_break(n=max(n, 1), seed=21)
+    p = sc.params
+    pos = sc.pos[:n]
+    with F.FluidSystem(p, max(n, 1)) as s:
+        s.SetParticles(pos, clr=sc.clr[:n])
+        s.Run(); s.Run()
+        s.Sync()
+        st = gpu_state(s)
+        ref = O.State.new(p, pos, clr=sc.clr[:n])
+        t = O.run(p, ref, 2, 0.0)
+        for k in FIELDS:
+            assert_bit_equal(st[k], getattr(ref, k), f"n={n} {k}")
+        assert np.float32(s.time) == np.float32(t)
+
+
+@pytest.mark.parametrize("m", [40, 100, 300, 700, 1024, 1025, 3000])
+def test_crowded_cell_canonical_order(m):
+    """m points inside one cell (every warp-sort width, then the counting
+    path beyond 1024), in shuffled index order among other points."""
+    sc = scenes.dam_break(n=4000, seed=8)
+    p = sc.params
+    rng = np.random.default_rng(m)
+    pos = sc.pos.copy()
+    pick = rng.choice(pos.shape[0], size=m, replace=False)
+    c = np.array([p.gridMin[0] + 7.5 * 5.0, p.gridMin[1] + 5.5 * 5.0, p.gridMin[2] + 6.5 * 5.0], np.float32)
+    pos[pick] = c + rng.uniform(-2.0, 2.0, size=(m, 3)).astype(np.float32)
+    with make_system(p, pos, clr=sc.clr) as s:
+        gcell, gndx, gcnt = s.InsertParticlesCUDA(readback=True)
+        ref = O.State.new(p, pos, clr=sc.clr)
+        O.insert(p, ref)
+        assert_bit_equal(gcell, ref.gcell, "gcell")
+        assert_bit_equal(gndx, ref.gndx, "gndx")
+        assert gcnt.max() >= m
+        s.PrefixSumCellsCUDA(1)
+        s.CountingSortFullCUDA()
+        O.prefix_sum(p, ref)
+        O.counting_sort(p, ref)
+        st = gpu_state(s)
+        for k in ("pos", "gcell", "gndx", "clr"):
+            assert_bit_equal(st[k], getattr(ref, k), f"m={m} {k}")
+        assert s.IntegrityCheck() == 0
+
+
+def test_out_of_range_points_follow_the_oracle():
+    sc = scenes.dam_break(n=3000, seed=12)
+    p = sc.params
+    pos = sc.pos.copy()
+    pos[[0, 10, 2999]] = [(-900.0, 1.0, 1.0), (0.0, 500.0, 0.0), (np.nan, 0.0, 0.0)]
+    with make_system(p, pos, clr=sc.clr) as s:
+        s.Run(); s.Run()
+        s.Sync()
+        st = gpu_state(s)
+        ref = O.State.new(p, pos, clr=sc.clr)
+        O.run(p, ref, 2, 0.0)
+        for k in FIELDS:
+            assert_bit_equal(st[k], getattr(ref, k), f"escaped {k}")
+        assert (st["gcell"][-3:] == UNDEF).all()
+        assert (st["pos"][-3:] == -1000.0).all()
+
+
+def test_all_points_out_of_range():
+    sc = scenes.dam_break(n=500, seed=13)
+    p = sc.params
+    pos = np.full((500, 3), 1.0e6, np.float32)
+    with make_system(p, pos) as s:
+        s.Run()
+        s.Sync()
+        st = gpu_state(s)
+        assert (st["gcell"] == UNDEF).all() and (st["gridcnt"] == 0).all()
+        assert (st["pos"] == -1000.0).all()
+
+
+def test_phase_order_and_capacity_errors():
+    sc = scenes.dam_break(n=100, seed=1)
+    with F.FluidSystem(sc.params, 100) as s:
+        s.SetParticles(sc.pos)
+        with pytest.raises(F.FluidsError) as e:
+            s.ComputePressureCUDA()
+        assert e.value.code == -6
+        with pytest.raises(F.FluidsError) as e:
+            s.PrefixSumCellsCUDA(1)
+        assert e.value.code == -6
+        with pytest.raises(F.FluidsError) as e:
+            s.SetParticles(np.zeros((101, 3), np.float32))
+        assert e.value.code == -4
+        assert s.NumPoints() == 100
+        s.Run()
+        s.Sync()
+
+
+def test_inclusive_offsets_readback():
+    sc = scenes.dam_break(n=2000, seed=2)
+    with make_system(sc.params, sc.pos) as s:
+        _, _, cnt = s.InsertParticlesCUDA(readback=True)
+        inc = s.PrefixSumCellsCUDA(0, readback=True)
+        assert_bit_equal(inc, np.cumsum(cnt, dtype=np.uint64).astype(np.uint32), "inclusive scan")
+        exc = s.PrefixSumCellsCUDA(1, readback=True)
+        assert_bit_equal(exc, (np.cumsum(cnt, dtype=np.uint64) - cnt).astype(np.uint32), "exclusive scan")
+
+
+def test_time_and_phase_timing():
+    sc = scenes.dam_break(n=4000, seed=2)
+    with make_system(sc.params, sc.pos) as s:
+        s.time = 1.5
+        s.SetTiming(True)
+        for _ in range(4):
+            s.Run()
+        ms, steps = s.PhaseTimes()
+        assert steps == 4 and all(v >= 0 for v in ms.values()) and ms["force_advance"] > 0
+        t = np.float32(1.5)
+        for _ in range(4):
+            t = np.float32(t + np.float32(sc.params.dt))
+        assert np.float32(s.time) == t
+        s.SetTiming(False)
+        s.RunSteps(4)
+        for _ in range(4):
+            t = np.float32(t + np.float32(sc.params.dt))
+        assert np.float32(s.time) == t
+
+
+def test_device_export_import_round_trip():
+    torch = pytest.importorskip("torch")
+    sc = scenes.dam_break(n=3000, seed=6)
+    with make_system(sc.params, sc.pos, sc.vel, sc.veval, sc.clr) as s:
+        s.Run()
+        s.Sync()
+        want = s.GetBuffer(F.FPOS)
+        dev = torch.empty((3000, 3), dtype=torch.float32, device="cuda")
+        F._lib.call("fl_export_device", s.handle, F.FPOS, dev.data_ptr(), dev.numel() * 4)
+        s.Sync()
+        torch.cuda.synchronize()
+        assert_bit_equal(dev.cpu().numpy(), want, "exported positions")
+        dev2 = dev + 1.0
+        torch.cuda.synchronize()
+        F._lib.call("fl_import_device", s.handle, 3000, dev2.data_ptr(), None, None)
+        s.Sync()
+        assert_bit_equal(s.GetBuffer(F.FPOS), want + np.float32(1.0), "imported positions")
+
+
+def test_device_error_word_starts_clear():
+    sc = scenes.dam_break(n=1000, seed=2)
+    with make_system(sc.params, sc.pos) as s:
+        s.RunSteps(6)
+        s.Sync()
+        assert s.DeviceStatus() == 0
