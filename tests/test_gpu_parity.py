@@ -7,7 +7,9 @@ kernels evaluate every float expression in the reference's order without
 FMA contraction, so density, force and advance are bit-exact as well
 except for the moving X- wall (CUDA sinf vs the host's sinf, plus the
 reference's double-precision wall product), which is held to the stated
-tolerances instead: density <= 1e-5 relative, force <= 1e-4 of its scale.
+tolerances instead. Against the FP64 oracle: density <= 1e-5 relative on
+every point with density >= 0.1 rest density (norm-wise <= 1e-6 over all),
+force <= 1e-4 of its scale (the sum of its pair-term magnitudes).
 """
 from __future__ import annotations
 
@@ -20,7 +22,8 @@ import fluids3_gb300 as F
 from fluids3_gb300 import scenes
 from oracle import oracle as O
 
-from helpers import FIELDS, assert_bit_equal, density_rel_err, digest, force_rel_err
+from helpers import (FIELDS, assert_bit_equal, density_normwise_err, density_rel_err, digest,
+                     force_rel_err)
 
 pytestmark = pytest.mark.gpu
 UNDEF = 0xFFFFFFFF
@@ -141,7 +144,8 @@ def oracle_step_check(s: F.FluidSystem, p, time: float, exact_fp: bool):
         m = ref.gcell != UNDEF
         assert_bit_equal(st["press"], ref.press, "density (walls do not enter it)")
         d64 = O.density_f64(p, pre_adv.pos, pre_adv.gcell, pre_adv.off, pre_adv.cnt, threads=8)
-        assert density_rel_err(st["press"], d64, m) <= 1e-5
+        assert density_rel_err(st["press"], d64, m, p.prest_dens) <= 1e-5
+        assert density_normwise_err(st["press"], d64, m) <= 1e-6
         f64, scale = O.force_f64(p, pre_adv.pos, pre_adv.veval, pre_adv.press, pre_adv.gcell,
                                  pre_adv.off, pre_adv.cnt, threads=8)
         assert force_rel_err(st["force"], f64, scale, m) <= 1e-4

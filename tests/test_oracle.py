@@ -11,7 +11,8 @@ import pytest
 from fluids3_gb300 import scenes
 from oracle import oracle as O
 
-from helpers import FIELDS, assert_bit_equal, density_rel_err, digest, force_rel_err
+from helpers import (FIELDS, assert_bit_equal, density_normwise_err, density_rel_err, digest,
+                     force_rel_err)
 
 UNDEF = 0xFFFFFFFF
 
@@ -168,7 +169,8 @@ def test_fp32_oracle_within_stated_tolerance_of_fp64():
     O.density(p, st)
     m = st.gcell != UNDEF
     d64 = O.density_f64(p, st.pos, st.gcell, st.off, st.cnt)
-    assert density_rel_err(st.press, d64, m) <= 1e-5
+    assert density_rel_err(st.press, d64, m, p.prest_dens) <= 1e-5
+    assert density_normwise_err(st.press, d64, m) <= 1e-6
     O.force(p, st)
     f64, scale = O.force_f64(p, st.pos, st.veval, st.press, st.gcell, st.off, st.cnt)
     assert force_rel_err(st.force, f64, scale, m) <= 1e-4
