@@ -231,6 +231,28 @@ int fl_set_timing(fl_system *s, int enable);
 int fl_time_steps(fl_system *s, int nsteps, int use_graph, double *ms);
 int fl_get_phase_times(fl_system *s, double ms[8], int *steps);
 
+/* ---- allocation-free scan ------------------------------------------------
+ * No counterpart in the reference. For host applications that cannot let a
+ * library allocate device memory -- an engine or plugin host that owns the
+ * whole device budget, or a real-time loop where cudaMalloc/cudaFree would
+ * synchronise the device and stall its other streams: the cell prefix sum
+ * of fl_prefix_sum_cells over caller-owned device buffers, without a
+ * fl_system. d_counts[n] in, d_offsets[n] out (exclusive scan when
+ * zero_offsets != 0, inclusive otherwise); d_status (nullable) gets
+ * FL_DEV_SPIN_TIMEOUT OR-ed in if a look-back wait gave up. Work is queued
+ * on `stream` (a cudaStream_t; NULL = default stream) and not waited for.
+ * The scan's scratch is a fixed ~8.5 KB device array inside the library,
+ * held by every GPU that loads it until the process exits, so n is limited
+ * to FL_NOALLOC_MAX_COUNTS (larger n is rejected with FL_ERR_ARG). The first
+ * call on each device looks up that array's device address with the device
+ * current; make that first call before any stream capture. All calls share
+ * the one array: calls whose GPU work overlaps (other streams, other host
+ * threads) race on it and must be ordered by the caller. Nothing is
+ * allocated: no cudaMalloc, cudaFree or allocating library routine. */
+#define FL_NOALLOC_MAX_COUNTS 4194304
+int fl_prefix_sum_noalloc(const uint32_t *d_counts, uint32_t *d_offsets, int n, int zero_offsets,
+                          uint32_t *d_status, void *stream);
+
 /* The CUDA stream (cudaStream_t) the system issues its work on. */
 void *fl_stream(fl_system *s);
 
