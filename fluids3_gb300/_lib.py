@@ -47,11 +47,13 @@ SIGNATURES = [
     ("fl_advance", C.c_int, [vp, C.c_float, C.c_float, C.c_float]),
     ("fl_run", C.c_int, [vp]),
     ("fl_run_steps", C.c_int, [vp, C.c_int]),
+    ("fl_checkpoint_save", C.c_int, [vp, C.c_int]),
+    ("fl_checkpoint_restore", C.c_int, [vp, C.c_int]),
     ("fl_sync", C.c_int, [vp]),
     ("fl_device_status", C.c_int, [vp, u32p]),
     ("fl_integrity_check", C.c_int, [vp, C.POINTER(C.c_int64)]),
     ("fl_set_timing", C.c_int, [vp, C.c_int]),
-    ("fl_time_steps", C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
+    ("fl_time_steps", C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]),
     ("fl_get_phase_times", C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     ("fl_prefix_sum_noalloc", C.c_int, [vp, vp, C.c_int, C.c_int, vp, vp]),
     ("fl_stream", vp, [vp]),

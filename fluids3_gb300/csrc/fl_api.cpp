@@ -6,6 +6,7 @@
 //   TransferToCUDA / TransferFromCUDA                 2312-2330
 //   InsertParticlesCUDA ... AdvanceCUDA               2334-2531
 //   Run (RUN_GPU_FULL) / AdvanceTime                  475-542
+#include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -57,6 +58,15 @@ void fl_make_dev_params(const fl_params &p, DevParams *d) {
     d->gravity = make_float3(p.gravity[0], p.gravity[1], p.gravity[2]);
     d->AL = p.AL; d->AL2 = p.AL2; d->VL = p.VL; d->VL2 = p.VL2;
     for (int c = 0; c < p.gridAdjCnt && c < 216; c++) d->adj[c] = p.gridAdj[c];
+    // search-block pruning: cell edge 1/gridDelta per axis; band = h (1 + 1e-4)
+    // plus 1e-3 of the smallest edge, orders of magnitude above the rounding
+    // of the cell computation (see band_code in fl_kernels.cu)
+    d->cellw = make_float3(1.0f / p.gridDelta[0], 1.0f / p.gridDelta[1], 1.0f / p.gridDelta[2]);
+    float wmin = d->cellw.x;
+    if (d->cellw.y < wmin) wmin = d->cellw.y;
+    if (d->cellw.z < wmin) wmin = d->cellw.z;
+    d->band = sqrtf(p.rd2) * 1.0001f + 1.0e-3f * wmin;
+    d->prune = (p.gridSrch == 2) ? 1 : 0;
 }
 
 static int check_derived(const fl_params *p) {
@@ -86,6 +96,7 @@ static int dalloc(void **p, size_t bytes) {
 static void free_grid(fl_system *s) {
     cudaFree(s->cnt);
     cudaFree(s->off);
+    s->codes_valid = 0;
     s->cnt = s->off = nullptr;
     s->scan_ticket = nullptr;
     s->scan_status = nullptr;
@@ -111,6 +122,7 @@ static int alloc_grid(fl_system *s) {
     s->scan_status = (uint64_t *)((char *)s->scan_ticket + 256);
     s->off = (uint32_t *)off;
     s->scan_epoch = 1;
+    s->codes_valid = 0;
     FL_CUDA_TRY(cudaMemsetAsync(blk, 0, grid_block_bytes(s), s->stream));
     FL_CUDA_TRY(cudaMemsetAsync(off, 0, s->grid_pad * sizeof(uint32_t), s->stream));
     return FL_OK;
@@ -126,11 +138,15 @@ static void free_all(fl_system *s) {
     destroy_graph(s);
     for (int k = 0; k < F_COUNT; k++)
         for (int c = 0; c < 2; c++) cudaFree(s->f[k].p[c]);
-    cudaFree(s->cell_pre); cudaFree(s->rank_tmp); cudaFree(s->src);
+    cudaFree(s->cell_pre); cudaFree(s->rank_tmp); cudaFree(s->src); cudaFree(s->upbits);
     free_grid(s);
     cudaFree(s->dev_err);
     cudaFree(s->time_dev);
     cudaFree(s->stage);
+    for (int c = 0; c < FL_MAX_CHECKPOINTS; c++) {
+        for (int k = 0; k < F_COUNT; k++) cudaFree(s->ckpt[c][k]);
+        cudaFree(s->ckpt_time[c]);
+    }
     for (int k = 0; k < 8; k++)
         if (s->ev[k]) cudaEventDestroy(s->ev[k]);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -173,6 +189,8 @@ extern "C" int fl_create(const fl_params *p, int max_points, fl_system **out) {
         if ((r = dalloc((void **)&s->cell_pre, 4 * np)) != FL_OK) break;
         if ((r = dalloc((void **)&s->rank_tmp, 4 * np)) != FL_OK) break;
         if ((r = dalloc((void **)&s->src, 4 * np)) != FL_OK) break;
+        s->D.upwords = (int)((np + 31) / 32 + 1);
+        if ((r = dalloc((void **)&s->upbits, fl_upbits_bytes(s))) != FL_OK) break;
         if ((r = dalloc((void **)&s->dev_err, 256)) != FL_OK) break;
         if ((r = dalloc((void **)&s->time_dev, 256)) != FL_OK) break;
         if ((r = alloc_grid(s)) != FL_OK) break;
@@ -230,6 +248,7 @@ static TimingState *detach_timing(fl_system *s) {
 
 static void reset_progress(fl_system *s) {
     s->have_insert = s->have_offsets = s->have_grid = 0;
+    s->codes_valid = 0;
     s->offsets_inclusive = 0;
 }
 
@@ -242,8 +261,10 @@ extern "C" int fl_set_params(fl_system *s, const fl_params *p) {
         s->ncells = p->gridTotal;
         FL_TRY(alloc_grid(s));
     }
+    const int upwords = s->D.upwords;
     s->P = *p;
     fl_make_dev_params(*p, &s->D);
+    s->D.upwords = upwords;
     destroy_graph(s);
     reset_progress(s);
     return FL_OK;
@@ -475,6 +496,7 @@ extern "C" int fl_insert_particles(fl_system *s, uint32_t *gcell, uint32_t *gndx
     FL_TRY(fl_launch_scan(s, s->ncells + 1, 0));
     FL_TRY(fl_launch_scatter_index(s));
     FL_TRY(fl_launch_sort_cells(s, 0));
+    s->codes_valid = 0;
     s->have_insert = 1;
     s->have_offsets = 0;
     s->have_grid = 0;
@@ -502,6 +524,7 @@ extern "C" int fl_counting_sort_full(fl_system *s, float *ppos) {
         return fl_fail(FL_ERR_STATE, "fl_counting_sort_full before insert and prefix sum");
     FL_TRY(fl_launch_gather_all(s));
     for (int k = 0; k < F_COUNT; k++) flip(s, k);
+    FL_TRY(fl_launch_band_codes(s));
     s->have_grid = 1;
     s->have_insert = 0;   // the pre-sort cell list no longer matches the order
     if (ppos) FL_TRY(fl_get_buffer(s, FL_FPOS, ppos, 12 * (size_t)s->n));
@@ -523,6 +546,7 @@ extern "C" int fl_compute_force(fl_system *s) {
 extern "C" int fl_advance(fl_system *s, float time, float dt, float ss) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_advance: null system");
     if (!s->have_grid) return fl_fail(FL_ERR_STATE, "fl_advance before fl_counting_sort_full");
+    s->codes_valid = 0;   // positions move; their band codes no longer hold
     return fl_launch_advance(s, time, dt, ss);
 }
 
@@ -553,6 +577,7 @@ static int run_step(fl_system *s, TimingState *t) {
     FL_TRY(record(s, t, 5));
     FL_TRY(fl_launch_force_advance(s, s->P.dt));
     flip(s, F_POS); flip(s, F_VEVAL);
+    s->codes_valid = 0;
     FL_TRY(record(s, t, 6));
     s->time_slot ^= 1;
     if (t) t->steps++;
@@ -651,6 +676,44 @@ extern "C" int fl_run_steps(fl_system *s, int nsteps) {
     return FL_OK;
 }
 
+extern "C" int fl_checkpoint_save(fl_system *s, int slot) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_checkpoint_save: null system");
+    if (slot < 0 || slot >= FL_MAX_CHECKPOINTS)
+        return fl_fail(FL_ERR_ARG, "fl_checkpoint_save: slot %d outside [0, %d)", slot, FL_MAX_CHECKPOINTS);
+    const size_t np = (size_t)(s->max_points > 0 ? s->max_points : 1);
+    if (!s->ckpt_time[slot]) {
+        for (int k = 0; k < F_COUNT; k++) FL_TRY(dalloc(&s->ckpt[slot][k], s->f[k].esz * np));
+        FL_TRY(dalloc((void **)&s->ckpt_time[slot], 256));
+    }
+    for (int k = 0; k < F_COUNT; k++)
+        if (s->n > 0)
+            FL_CUDA_TRY(cudaMemcpyAsync(s->ckpt[slot][k], s->f[k].cur<void>(), s->f[k].esz * (size_t)s->n,
+                                        cudaMemcpyDeviceToDevice, s->stream));
+    FL_CUDA_TRY(cudaMemcpyAsync(s->ckpt_time[slot], s->time_dev + s->time_slot, sizeof(float),
+                                cudaMemcpyDeviceToDevice, s->stream));
+    s->ckpt_n[slot] = s->n;
+    s->ckpt_host_time[slot] = s->time;
+    s->ckpt_host_valid[slot] = s->time_host_valid;
+    return FL_OK;
+}
+
+extern "C" int fl_checkpoint_restore(fl_system *s, int slot) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_checkpoint_restore: null system");
+    if (slot < 0 || slot >= FL_MAX_CHECKPOINTS || !s->ckpt_time[slot])
+        return fl_fail(FL_ERR_ARG, "fl_checkpoint_restore: slot %d holds no checkpoint", slot);
+    s->n = s->ckpt_n[slot];
+    for (int k = 0; k < F_COUNT; k++)
+        if (s->n > 0)
+            FL_CUDA_TRY(cudaMemcpyAsync(s->f[k].cur<void>(), s->ckpt[slot][k], s->f[k].esz * (size_t)s->n,
+                                        cudaMemcpyDeviceToDevice, s->stream));
+    FL_CUDA_TRY(cudaMemcpyAsync(s->time_dev + s->time_slot, s->ckpt_time[slot], sizeof(float),
+                                cudaMemcpyDeviceToDevice, s->stream));
+    s->time = s->ckpt_host_time[slot];
+    s->time_host_valid = s->ckpt_host_valid[slot];
+    reset_progress(s);
+    return FL_OK;
+}
+
 extern "C" int fl_device_status(fl_system *s, uint32_t *flags) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_device_status: null system");
     uint32_t v = 0;
@@ -701,14 +764,24 @@ extern "C" int fl_set_timing(fl_system *s, int enable) {
     return FL_OK;
 }
 
-extern "C" int fl_time_steps(fl_system *s, int nsteps, int use_graph, double *ms) {
+extern "C" int fl_time_steps(fl_system *s, int nsteps, int use_graph, int restart_every,
+                             int restart_slot, double *ms) {
     if (!s || !ms) return fl_fail(FL_ERR_ARG, "fl_time_steps: null argument");
     if (nsteps < 0) return fl_fail(FL_ERR_ARG, "fl_time_steps: nsteps < 0");
+    if (restart_every > 0 && (restart_slot < 0 || restart_slot >= FL_MAX_CHECKPOINTS ||
+                              !s->ckpt_time[restart_slot]))
+        return fl_fail(FL_ERR_ARG, "fl_time_steps: restart slot %d holds no checkpoint", restart_slot);
     FL_CUDA_TRY(cudaEventRecord(s->ev[0], s->stream));
-    if (use_graph) {
-        FL_TRY(fl_run_steps(s, nsteps));
-    } else {
-        for (int k = 0; k < nsteps; k++) FL_TRY(fl_run(s));
+    for (int done = 0; done < nsteps;) {
+        const int chunk = restart_every > 0 ? (nsteps - done < restart_every ? nsteps - done : restart_every)
+                                            : nsteps - done;
+        if (restart_every > 0) FL_TRY(fl_checkpoint_restore(s, restart_slot));
+        if (use_graph) {
+            FL_TRY(fl_run_steps(s, chunk));
+        } else {
+            for (int k = 0; k < chunk; k++) FL_TRY(fl_run(s));
+        }
+        done += chunk;
     }
     FL_CUDA_TRY(cudaEventRecord(s->ev[1], s->stream));
     FL_CUDA_TRY(cudaEventSynchronize(s->ev[1]));

@@ -38,6 +38,13 @@ struct DevParams {
     float bound_wall_force, bound_wall_freq;
     float3 bound_min, bound_max, gravity;
     float AL, AL2, VL, VL2;
+    // search-block pruning (gridSrch == 2 only): world-unit cell edge per
+    // axis and the band width (h plus a safety margin) within which a point
+    // can reach into the lower neighbour cell
+    float3 cellw;
+    float band;
+    int prune;           // 1 when gridSrch == 2
+    int upwords;         // words per axis row of the upper-band slot flags
     int adj[216];
 };
 
@@ -86,6 +93,12 @@ struct fl_system {
 
     uint32_t *dev_err;     // device error word (FL_DEV_*)
 
+    // per sorted slot and axis: is the point within `band` of its cell's
+    // upper face (3 rows of upwords 32-bit words); valid together with the
+    // band codes in pos.w while codes_valid is set
+    uint32_t *upbits;
+    int codes_valid;
+
     // m_Time on the device, double-buffered by step parity so a captured
     // graph replays with the time advancing: step k reads time_dev[k & 1]
     // and writes time_dev[(k + 1) & 1] = time + dt (AdvanceTime, cpp:527-531).
@@ -106,6 +119,13 @@ struct fl_system {
     int graph_steps;
     int graph_live[F_COUNT];
 
+    // checkpoints: per slot, one copy of every field's live buffer + time
+    void *ckpt[FL_MAX_CHECKPOINTS][F_COUNT];
+    float *ckpt_time[FL_MAX_CHECKPOINTS];
+    int ckpt_n[FL_MAX_CHECKPOINTS];
+    float ckpt_host_time[FL_MAX_CHECKPOINTS];
+    int ckpt_host_valid[FL_MAX_CHECKPOINTS];
+
     // per-phase event timing (PERF_PUSH/PERF_POP of Run, cpp:507-515)
     int timing;
     cudaEvent_t ev[8];
@@ -122,6 +142,7 @@ int fl_launch_scatter_index(fl_system *s);
 int fl_launch_sort_cells(fl_system *s, int mode);
 // gather every field cur -> nxt through src (phase-API counting sort)
 int fl_launch_gather_all(fl_system *s);
+int fl_launch_band_codes(fl_system *s);
 int fl_launch_density(fl_system *s);
 int fl_launch_force(fl_system *s);
 int fl_launch_force_advance(fl_system *s, float dt);
@@ -131,4 +152,5 @@ int fl_launch_unpack3(fl_system *s, const float *src, float4 *dst, int n);
 int fl_launch_grid_identity(fl_system *s, uint32_t *dst, int n, int n_in);
 int fl_launch_integrity(fl_system *s, unsigned long long *bad_dev);
 size_t fl_scan_tile();
+size_t fl_upbits_bytes(const fl_system *s);
 size_t fl_scan_scratch_bytes(int ntiles);

@@ -36,6 +36,62 @@ __device__ __forceinline__ uint32_t cell_of(const DevParams &P, float4 p) {
     return (uint32_t)P.ncells;
 }
 
+// ---------------------------------------------------------------------------
+// Search-block pruning (gridSrch == 2). The search block of a point in cell
+// c is the 2x2x2 cells c-1..c per axis (fluid_kernels.cu:120,129-131). Along
+// an axis where the block takes the lower neighbour, a pair can only pass
+// the 0 < d^2 < rd2 test if the point lies within h of its cell's lower
+// face and the neighbour lies within h of that same face. Each sorted point
+// carries a band code in pos.w:
+//   bits 0-2  within `band` of its own cell's upper face (x, y, z)
+//   bits 3-5  within `band` of its own cell's lower face (x, y, z)
+// with band = h (1 + 1e-4) + 1e-3 * cell edge, far above the rounding of
+// the cell computation. Skipping only pairs whose every FP32 distance is
+// >= band > h leaves each sum's terms and order unchanged, so the pruned
+// passes are bit-identical to the reference loop.
+__device__ __forceinline__ uint32_t band_code(const DevParams &P, int c, float4 p) {
+    if (c >= P.ncells) return 0u;
+    const int cx = c % P.gridRes.x;
+    const int t = c / P.gridRes.x;
+    const int cz = t % P.gridRes.z;
+    const int cy = t / P.gridRes.z;
+    const float lx = P.gridMin.x + (float)cx * P.cellw.x;
+    const float ly = P.gridMin.y + (float)cy * P.cellw.y;
+    const float lz = P.gridMin.z + (float)cz * P.cellw.z;
+    uint32_t code = 0;
+    code |= ((lx + P.cellw.x) - p.x < P.band) ? 1u : 0u;
+    code |= ((ly + P.cellw.y) - p.y < P.band) ? 2u : 0u;
+    code |= ((lz + P.cellw.z) - p.z < P.band) ? 4u : 0u;
+    code |= (p.x - lx < P.band) ? 8u : 0u;
+    code |= (p.y - ly < P.band) ? 16u : 0u;
+    code |= (p.z - lz < P.band) ? 32u : 0u;
+    return code;
+}
+
+// Upper-band flags of the sorted slots, one bit per slot and axis:
+// upbits[axis * upwords + (slot >> 5)] bit (slot & 31). Published by the
+// 32 lanes of a warp for 32 consecutive slots base + lane (all lanes call).
+__device__ __forceinline__ void publish_upbits(const DevParams &P, uint32_t *upbits, uint32_t base,
+                                               uint32_t code, bool valid) {
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t w0 = base >> 5, sh = base & 31u;
+#pragma unroll
+    for (int ax = 0; ax < 3; ax++) {
+        const unsigned b = __ballot_sync(0xffffffffu, valid && ((code >> ax) & 1u));
+        if (b) {
+            uint32_t *row = upbits + (size_t)ax * P.upwords;
+            if (lane == 0) atomicOr(&row[w0], b << sh);
+            if (lane == 1 && sh) atomicOr(&row[w0 + 1], b >> (32u - sh));
+        }
+    }
+}
+
+// Axes (bit 0 x, 1 y, 2 z) along which adjacency entry k (y,z,x order,
+// fluid_system.cpp:2266-2270) reaches into the lower neighbour cell.
+__device__ __forceinline__ uint32_t lower_axes(int k) {
+    return ((k & 1) ? 0u : 1u) | ((k & 4) ? 0u : 2u) | ((k & 2) ? 0u : 4u);
+}
+
 // insertParticles (fluids4.0/fluid_kernels.cu:22-53) with warp-aggregated
 // counting: lanes of a warp that land in the same cell elect one leader,
 // which adds the group size with a single atomic; each lane's arrival rank is
@@ -78,9 +134,9 @@ k_scatter_index(int n, const uint32_t *__restrict__ cell_pre, const uint32_t *__
 // Canonical within-cell order. Each warp owns one cell segment of src and
 // sorts its point indices ascending, so slot off[c]+k holds the k-th lowest
 // index in cell c -- the order a serial insert (gndx = cnt[cell]++) yields.
-// Segments up to 1024 points are sorted in registers by a warp bitonic
+// Segments up to 128 points are sorted in registers by a warp bitonic
 // network (K keys per lane, element e = lane*K + r); larger ones take a
-// counting-rank path.
+// chunked rank path (sort_segment_dense).
 template <int K>
 __device__ __forceinline__ void warp_bitonic(uint32_t (&v)[K]) {
     const unsigned lane = lane_id();
@@ -123,21 +179,44 @@ struct SortArgs {
     const uint32_t *clr_in;
     float4 *pos_out, *vel_out, *veval_out;
     uint32_t *clr_out, *gcell_out, *gndx_out;
+    uint32_t *upbits;                  // mode 1 with pruning: per-slot upper-band flags
     int ncells;
+    int prune;
+    DevParams P;
 };
 
+// Writes slot o+k of cell c from pre-sort point i; returns the band code
+// (mode 1 with pruning) so the caller can build the cell's masks.
 template <int MODE>
-__device__ __forceinline__ void emit_slot(const SortArgs &a, int c, uint32_t o, uint32_t k, uint32_t i) {
+__device__ __forceinline__ uint32_t emit_slot(const SortArgs &a, int c, uint32_t o, uint32_t k, uint32_t i) {
     if (MODE == 0) {
         a.gndx_pre[i] = k;
+        return 0u;
     } else {
         const uint32_t s = o + k;
-        a.pos_out[s] = a.pos_in[i];
+        float4 p = a.pos_in[i];
+        const uint32_t code = a.prune ? band_code(a.P, c, p) : 0u;
+        p.w = __uint_as_float(code);
+        a.pos_out[s] = p;
         a.vel_out[s] = a.vel_in[i];
         a.veval_out[s] = a.veval_in[i];
         a.clr_out[s] = a.clr_in[i];
         a.gcell_out[s] = (c == a.ncells) ? kUndef : (uint32_t)c;
         a.gndx_out[s] = k;
+        return code;
+    }
+}
+
+// Emit slots o .. o+m-1 of cell c from the sorted src (all lanes call).
+template <int MODE>
+__device__ __forceinline__ void emit_range(const SortArgs &a, int c, uint32_t o, uint32_t m) {
+    const unsigned lane = lane_id();
+    for (uint32_t kb = 0; kb < m; kb += 32) {
+        const uint32_t k = kb + lane;
+        const bool valid = k < m;
+        uint32_t code = 0;
+        if (valid) code = emit_slot<MODE>(a, c, o, k, a.src[o + k]);
+        if (MODE == 1 && a.prune) publish_upbits(a.P, a.upbits, o + kb, code, valid);
     }
 }
 
@@ -152,10 +231,12 @@ __device__ __forceinline__ void sort_segment(const SortArgs &a, int c, uint32_t 
     }
     warp_bitonic<K>(v);
     if constexpr (K == 1) {
+        uint32_t code = 0;
         if (lane < m) {
             if (MODE == 0) a.src[o + lane] = v[0];
-            emit_slot<MODE>(a, c, o, lane, v[0]);
+            code = emit_slot<MODE>(a, c, o, lane, v[0]);
         }
+        if (MODE == 1 && a.prune) publish_upbits(a.P, a.upbits, o, code, lane < m);
     } else {
 #pragma unroll
         for (int r = 0; r < K; r++) {
@@ -163,24 +244,58 @@ __device__ __forceinline__ void sort_segment(const SortArgs &a, int c, uint32_t 
             if (e < m) a.src[o + e] = v[r];
         }
         __syncwarp();
-        for (uint32_t k = lane; k < m; k += 32) emit_slot<MODE>(a, c, o, k, a.src[o + k]);
+        emit_range<MODE>(a, c, o, m);
     }
+}
+
+// Segments above 128 points: sort each 128-key chunk in registers, then
+// place every key at its rank -- its index within its own chunk plus, for
+// each other chunk, the number of smaller keys there (a binary search) --
+// through the scratch array. Keys are distinct point indices.
+__device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t *a, uint32_t len, uint32_t key) {
+    uint32_t lo = 0, hi = len;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
 }
 
 template <int MODE>
 __device__ void sort_segment_dense(const SortArgs &a, int c, uint32_t o, uint32_t m) {
-    // rank of each key = number of smaller keys in the segment (keys are distinct)
     const unsigned lane = lane_id();
+    constexpr uint32_t kChunk = 128;
+    for (uint32_t cb = 0; cb < m; cb += kChunk) {
+        uint32_t v[4];
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const uint32_t e = cb + lane * 4 + r;
+            v[r] = (e < m) ? a.src[o + e] : 0xffffffffu;
+        }
+        warp_bitonic<4>(v);
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const uint32_t e = cb + lane * 4 + r;
+            if (e < m) a.src[o + e] = v[r];
+        }
+    }
+    __syncwarp();
+    const uint32_t nch = (m + kChunk - 1) / kChunk;
     for (uint32_t k = lane; k < m; k += 32) {
         const uint32_t key = a.src[o + k];
-        uint32_t rank = 0;
-        for (uint32_t u = 0; u < m; u++) rank += (a.src[o + u] < key);
+        const uint32_t mine = k / kChunk;
+        uint32_t rank = k - mine * kChunk;
+        for (uint32_t ch = 0; ch < nch; ch++) {
+            if (ch == mine) continue;
+            const uint32_t lo = ch * kChunk;
+            rank += lower_bound_u32(a.src + o + lo, min(kChunk, m - lo), key);
+        }
         a.scratch[o + rank] = key;
     }
     __syncwarp();
     for (uint32_t k = lane; k < m; k += 32) a.src[o + k] = a.scratch[o + k];
     __syncwarp();
-    for (uint32_t k = lane; k < m; k += 32) emit_slot<MODE>(a, c, o, k, a.src[o + k]);
+    emit_range<MODE>(a, c, o, m);
 }
 
 template <int MODE>
@@ -194,10 +309,33 @@ k_sort_cells(const __grid_constant__ SortArgs a) {
     if (m <= 32) sort_segment<MODE, 1>(a, c, o, m);
     else if (m <= 64) sort_segment<MODE, 2>(a, c, o, m);
     else if (m <= 128) sort_segment<MODE, 4>(a, c, o, m);
-    else if (m <= 256) sort_segment<MODE, 8>(a, c, o, m);
-    else if (m <= 512) sort_segment<MODE, 16>(a, c, o, m);
-    else if (m <= 1024) sort_segment<MODE, 32>(a, c, o, m);
     else sort_segment_dense<MODE>(a, c, o, m);
+}
+
+// Band codes and upper-band slot flags for an already sorted grid
+// (phase-API path, after k_gather_all): warp per cell, codes into pos.w.
+__global__ void __launch_bounds__(kThreads)
+k_band_codes(const __grid_constant__ DevParams P, const uint32_t *__restrict__ off,
+             const uint32_t *__restrict__ cnt, float4 *__restrict__ pos,
+             uint32_t *__restrict__ upbits) {
+    const int c = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
+    if (c >= P.ncells) return;
+    const uint32_t m = cnt[c];
+    if (m == 0) return;
+    const uint32_t o = off[c];
+    const unsigned lane = lane_id();
+    for (uint32_t kb = 0; kb < m; kb += 32) {
+        const uint32_t k = kb + lane;
+        const bool valid = k < m;
+        uint32_t code = 0;
+        if (valid) {
+            float4 p = pos[o + k];
+            code = band_code(P, c, p);
+            p.w = __uint_as_float(code);
+            pos[o + k] = p;
+        }
+        publish_upbits(P, upbits, o + kb, code, valid);
+    }
 }
 
 // Phase-API counting sort (countingSortFull, fluids4.0/fluid_kernels.cu:56-87)
@@ -226,23 +364,92 @@ k_gather_all(int n, const uint32_t *__restrict__ src,
 }
 
 // ---------------------------------------------------------------------------
+// Candidate enumeration for one adjacency entry of the search block.
+//
+// Unpruned: every member of the neighbour cell, in sorted order (the
+// reference loop, fluid_kernels.cu:131-133). Pruned (gridSrch == 2 with
+// valid band codes): the cell is skipped unless the point is within the band
+// of its lower face on every axis where the entry reaches down, and only
+// members within the band of their upper face on those axes are visited,
+// read 32 slots at a time from the per-slot flag words. Visiting order is
+// always ascending slot, so a point's sum sees the same terms in the same
+// order as the reference loop.
+struct CandIter {
+    uint32_t w, w_last;   // current and last 32-slot word of the cell's range
+    uint32_t lo, hi;      // slot range [lo, hi)
+    uint32_t bits;        // candidates left in word w
+    uint32_t U;           // axes whose upper-band flag a candidate must carry
+};
+
+template <bool PRUNE>
+__device__ __forceinline__ uint32_t cand_word(const CandIter &it, const DevParams &P,
+                                              const uint32_t *__restrict__ upbits, uint32_t w) {
+    uint32_t v = 0xffffffffu;
+    if (PRUNE) {
+        if (it.U & 1u) v &= upbits[w];
+        if (it.U & 2u) v &= upbits[(size_t)P.upwords + w];
+        if (it.U & 4u) v &= upbits[2 * (size_t)P.upwords + w];
+    }
+    if (w == (it.lo >> 5)) v &= 0xffffffffu << (it.lo & 31u);
+    if (w == it.w_last && (it.hi & 31u)) v &= 0xffffffffu >> (32u - (it.hi & 31u));
+    return v;
+}
+
+template <bool PRUNE>
+__device__ __forceinline__ void cand_begin(CandIter &it, const DevParams &P, int k, int cell,
+                                           uint32_t my_code, bool active,
+                                           const uint32_t *__restrict__ off,
+                                           const uint32_t *__restrict__ cnt,
+                                           const uint32_t *__restrict__ upbits) {
+    it.bits = 0; it.w = 0; it.w_last = 0; it.lo = it.hi = 0; it.U = 0;
+    if (!active) return;
+    if (PRUNE) {
+        it.U = lower_axes(k);
+        if (((my_code >> 3) & it.U) != it.U) return;     // too far from those lower faces
+    }
+    const uint32_t m = cnt[cell];
+    if (m == 0) return;
+    it.lo = off[cell];
+    it.hi = it.lo + m;
+    it.w = it.lo >> 5;
+    it.w_last = (it.hi - 1) >> 5;
+    it.bits = cand_word<PRUNE>(it, P, upbits, it.w);
+}
+
+template <bool PRUNE>
+__device__ __forceinline__ bool cand_next(CandIter &it, const DevParams &P,
+                                          const uint32_t *__restrict__ upbits, uint32_t &j) {
+    while (it.bits == 0) {
+        if (it.w >= it.w_last) return false;
+        it.w++;
+        it.bits = cand_word<PRUNE>(it, P, upbits, it.w);
+    }
+    j = (it.w << 5) + (uint32_t)(__ffs(it.bits) - 1);
+    it.bits &= it.bits - 1u;
+    return true;
+}
+
 // computePressure (fluids4.0/fluid_kernels.cu:112-149). FGRID is the
 // identity after a full sort (cu:83), so neighbour slots are read directly.
+template <bool PRUNE>
 __global__ void __launch_bounds__(kThreads)
 k_density(const __grid_constant__ DevParams P, int n, const float4 *__restrict__ pos,
           const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ off,
-          const uint32_t *__restrict__ cnt, float *__restrict__ press) {
+          const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
+          float *__restrict__ press) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t gc = gcell[i];
     if (gc == kUndef) { press[i] = 0.0f; return; }
     const int base = (int)gc - P.nadj;
     const float4 p = pos[i];
+    const uint32_t my_code = __float_as_uint(p.w);
     float sum = 0.0f;
     for (int c = 0; c < P.gridAdjCnt; c++) {
-        const int cell = base + P.adj[c];
-        const uint32_t j0 = off[cell], j1 = j0 + cnt[cell];
-        for (uint32_t j = j0; j < j1; j++) {
+        CandIter it;
+        cand_begin<PRUNE>(it, P, c, base + P.adj[c], my_code, true, off, cnt, upbits);
+        uint32_t j;
+        while (cand_next<PRUNE>(it, P, upbits, j)) {
             const float4 q = pos[j];
             const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
             float dsq = dx * dx + dy * dy + dz * dz;
@@ -257,58 +464,109 @@ k_density(const __grid_constant__ DevParams P, int n, const float4 *__restrict__
     press[i] = sum;
 }
 
-// computeForce's pair loop (fluids4.0/fluid_kernels.cu:180-217), same
-// operation order; returns the SPH force on point i.
-__device__ __forceinline__ float3 force_sum(const DevParams &P, int i, uint32_t gc,
-                                            const float4 *__restrict__ pos,
-                                            const float4 *__restrict__ veval,
-                                            const float *__restrict__ press,
-                                            const uint32_t *__restrict__ off,
-                                            const uint32_t *__restrict__ cnt) {
-    const int base = (int)gc - P.nadj;
-    const float4 p = pos[i];
-    const float4 vi = veval[i];
-    const float di = press[i];
-    const float pi = (di - P.prest_dens) * P.pintstiff;
-    float3 f = make_float3(0.0f, 0.0f, 0.0f);
-    for (int c = 0; c < P.gridAdjCnt; c++) {
-        const int cell = base + P.adj[c];
-        const uint32_t j0 = off[cell], j1 = j0 + cnt[cell];
-        for (uint32_t j = j0; j < j1; j++) {
+// computeForce (fluids4.0/fluid_kernels.cu:180-217) in two stages per warp:
+// lanes first walk their candidates with the cheap distance test and push
+// each hit's slot onto a per-thread list in shared memory; whenever some
+// lane's list is full (and at the end) the warp drains every list, each
+// lane evaluating its own hits in the order found. The long pair-force
+// arithmetic (sqrt, two IEEE divisions) then runs with every lane busy
+// instead of inside a branch few lanes take, and each point still adds its
+// pair terms in the reference's order.
+constexpr int kForceThreads = 128;
+constexpr int kHitCap = 32;
+
+struct ForcePoint {
+    float4 p, vi;
+    float di, pi;
+    float3 f;
+};
+
+__device__ __forceinline__ void drain_hits(const DevParams &P, ForcePoint &fp, uint32_t &nhits,
+                                           const uint32_t *hits, const float4 *__restrict__ pos,
+                                           const float4 *__restrict__ veval,
+                                           const float *__restrict__ press) {
+    const uint32_t most = __reduce_max_sync(0xffffffffu, nhits);
+    for (uint32_t t = 0; t < most; t++) {
+        if (t < nhits) {
+            const uint32_t j = hits[t * kForceThreads];
             const float4 q = pos[j];
-            const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+            const float dx = fp.p.x - q.x, dy = fp.p.y - q.y, dz = fp.p.z - q.z;
             const float dsq = dx * dx + dy * dy + dz * dz;
-            if (dsq < P.rd2 && dsq > 0.0f) {
-                const float r = sqrtf(dsq * P.d2);
-                const float dj = press[j];
-                const float pj = (dj - P.prest_dens) * P.pintstiff;
-                const float cr = P.psmoothradius - r;
-                const float pterm = P.sim_scale * -0.5f * cr * P.spikykern * (pi + pj) / r;
-                const float4 vj = veval[j];
-                const float sx = dx * pterm + (vj.x - vi.x) * P.vterm;
-                const float sy = dy * pterm + (vj.y - vi.y) * P.vterm;
-                const float sz = dz * pterm + (vj.z - vi.z) * P.vterm;
-                const float inv = 1.0f / (di * dj);
-                f.x += (sx * cr) * inv;
-                f.y += (sy * cr) * inv;
-                f.z += (sz * cr) * inv;
-            }
+            const float r = sqrtf(dsq * P.d2);
+            const float dj = press[j];
+            const float pj = (dj - P.prest_dens) * P.pintstiff;
+            const float cr = P.psmoothradius - r;
+            const float pterm = P.sim_scale * -0.5f * cr * P.spikykern * (fp.pi + pj) / r;
+            const float4 vj = veval[j];
+            const float sx = dx * pterm + (vj.x - fp.vi.x) * P.vterm;
+            const float sy = dy * pterm + (vj.y - fp.vi.y) * P.vterm;
+            const float sz = dz * pterm + (vj.z - fp.vi.z) * P.vterm;
+            const float inv = 1.0f / (fp.di * dj);
+            fp.f.x += (sx * cr) * inv;
+            fp.f.y += (sy * cr) * inv;
+            fp.f.z += (sz * cr) * inv;
         }
     }
-    return f;
+    nhits = 0;
 }
 
-__global__ void __launch_bounds__(kThreads)
+// The force on point i (all 32 lanes of the warp must call this).
+template <bool PRUNE>
+__device__ __forceinline__ float3 force_of(const DevParams &P, int i, bool active, uint32_t gc,
+                                           const float4 *__restrict__ pos,
+                                           const float4 *__restrict__ veval,
+                                           const float *__restrict__ press,
+                                           const uint32_t *__restrict__ off,
+                                           const uint32_t *__restrict__ cnt,
+                                           const uint32_t *__restrict__ upbits) {
+    __shared__ uint32_t s_hits[kHitCap * kForceThreads];
+    uint32_t *hits = s_hits + threadIdx.x;
+    ForcePoint fp;
+    fp.f = make_float3(0.0f, 0.0f, 0.0f);
+    uint32_t my_code = 0;
+    int base = 0;
+    if (active) {
+        fp.p = pos[i];
+        fp.vi = veval[i];
+        fp.di = press[i];
+        fp.pi = (fp.di - P.prest_dens) * P.pintstiff;
+        my_code = __float_as_uint(fp.p.w);
+        base = (int)gc - P.nadj;
+    }
+    uint32_t nhits = 0;
+    for (int c = 0; c < P.gridAdjCnt; c++) {
+        CandIter it;
+        cand_begin<PRUNE>(it, P, c, base + P.adj[c], my_code, active, off, cnt, upbits);
+        for (;;) {
+            uint32_t j = 0;
+            const bool have = cand_next<PRUNE>(it, P, upbits, j);
+            if (!__any_sync(0xffffffffu, have)) break;
+            if (have) {
+                const float4 q = pos[j];
+                const float dx = fp.p.x - q.x, dy = fp.p.y - q.y, dz = fp.p.z - q.z;
+                const float dsq = dx * dx + dy * dy + dz * dz;
+                if (dsq < P.rd2 && dsq > 0.0f) hits[(nhits++) * kForceThreads] = j;
+            }
+            if (__any_sync(0xffffffffu, nhits == kHitCap))
+                drain_hits(P, fp, nhits, hits, pos, veval, press);
+        }
+    }
+    drain_hits(P, fp, nhits, hits, pos, veval, press);
+    return fp.f;
+}
+
+template <bool PRUNE>
+__global__ void __launch_bounds__(kForceThreads)
 k_force(const __grid_constant__ DevParams P, int n, const float4 *__restrict__ pos,
         const float4 *__restrict__ veval, const float *__restrict__ press,
         const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ off,
-        const uint32_t *__restrict__ cnt, float4 *__restrict__ force) {
+        const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
+        float4 *__restrict__ force) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t gc = gcell[i];
-    if (gc == kUndef) { force[i] = make_float4(0.f, 0.f, 0.f, 0.f); return; }
-    const float3 f = force_sum(P, i, gc, pos, veval, press, off, cnt);
-    force[i] = make_float4(f.x, f.y, f.z, 0.0f);
+    const uint32_t gc = (i < n) ? gcell[i] : kUndef;
+    const bool active = gc != kUndef;
+    const float3 f = force_of<PRUNE>(P, i, active, gc, pos, veval, press, off, cnt, upbits);
+    if (i < n) force[i] = active ? make_float4(f.x, f.y, f.z, 0.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 // advanceParticles body (fluids4.0/fluid_kernels.cu:343-419) for an
@@ -414,27 +672,30 @@ k_advance(const __grid_constant__ DevParams P, int n, float time, float dt, floa
 // Force then advance for one point: the last two phases of Run fused.
 // Neighbour reads come from pos_in/veval_in; the new position and evaluated
 // velocity go to the other copies, velocity and force are updated in place.
-__global__ void __launch_bounds__(kThreads)
+template <bool PRUNE>
+__global__ void __launch_bounds__(kForceThreads)
 k_force_advance(const __grid_constant__ DevParams P, int n, float *time_dev, int slot, float dt,
                 const float4 *__restrict__ pos_in, const float4 *__restrict__ veval_in,
                 const float *__restrict__ press, const uint32_t *__restrict__ gcell,
                 const uint32_t *__restrict__ off, const uint32_t *__restrict__ cnt,
+                const uint32_t *__restrict__ upbits,
                 float4 *__restrict__ vel, float4 *__restrict__ force,
                 float4 *__restrict__ pos_out, float4 *__restrict__ veval_out,
                 uint32_t *__restrict__ err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const float time = time_dev[slot];
     if (i == 0) time_dev[slot ^ 1] = time + dt;
+    const uint32_t gc = (i < n) ? gcell[i] : kUndef;
+    const bool active = gc != kUndef;
+    const float3 f = force_of<PRUNE>(P, i, active, gc, pos_in, veval_in, press, off, cnt, upbits);
     if (i >= n) return;
-    const uint32_t gc = gcell[i];
-    if (gc == kUndef) {
+    if (!active) {
         force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         pos_out[i] = make_float4(-1000.f, -1000.f, -1000.f, 0.f);
         vel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         veval_out[i] = veval_in[i];
         return;
     }
-    const float3 f = force_sum(P, i, gc, pos_in, veval_in, press, off, cnt);
     force[i] = f4(f);
     float3 po, vo, eo;
     advance_point(P, time, dt, P.sim_scale, f, xyz(pos_in[i]), xyz(vel[i]), xyz(veval_in[i]), po, vo, eo);
@@ -516,6 +777,9 @@ int fl_launch_sort_cells(fl_system *s, int mode) {
     SortArgs a = {};
     a.off = s->off; a.cnt = s->cnt; a.src = s->src; a.scratch = s->rank_tmp;
     a.ncells = s->ncells;
+    a.P = s->D;
+    a.prune = (mode == 1) ? s->D.prune : 0;
+    a.upbits = s->upbits;
     const int warps_per_block = kThreads / 32;
     const int grid = blocks_for((long long)s->ncells + 1, warps_per_block);
     if (mode == 0) {
@@ -528,7 +792,9 @@ int fl_launch_sort_cells(fl_system *s, int mode) {
         a.clr_in = s->f[F_CLR].cur<uint32_t>(); a.clr_out = s->f[F_CLR].nxt<uint32_t>();
         a.gcell_out = s->f[F_GCELL].nxt<uint32_t>();
         a.gndx_out = s->f[F_GNDX].nxt<uint32_t>();
+        if (a.prune) FL_CUDA_TRY(cudaMemsetAsync(s->upbits, 0, fl_upbits_bytes(s), s->stream));
         k_sort_cells<1><<<grid, kThreads, 0, s->stream>>>(a);
+        s->codes_valid = s->D.prune;
     }
     FL_LAUNCH_CHECK("sort_cells");
     return FL_OK;
@@ -548,29 +814,49 @@ int fl_launch_gather_all(fl_system *s) {
     return FL_OK;
 }
 
+size_t fl_upbits_bytes(const fl_system *s) { return 3 * sizeof(uint32_t) * (size_t)s->D.upwords; }
+
+// Pruned neighbour passes need gridSrch == 2 and band codes that match the
+// live positions (set by the fused sort or fl_launch_band_codes).
+static bool use_prune(const fl_system *s) { return s->D.prune && s->codes_valid; }
+
+int fl_launch_band_codes(fl_system *s) {
+    if (!s->D.prune) { s->codes_valid = 0; return FL_OK; }
+    const int grid = blocks_for((long long)s->ncells, kThreads / 32);
+    FL_CUDA_TRY(cudaMemsetAsync(s->upbits, 0, fl_upbits_bytes(s), s->stream));
+    k_band_codes<<<grid, kThreads, 0, s->stream>>>(s->D, s->off, s->cnt, s->f[F_POS].cur<float4>(),
+                                                     s->upbits);
+    FL_LAUNCH_CHECK("band_codes");
+    s->codes_valid = 1;
+    return FL_OK;
+}
+
 int fl_launch_density(fl_system *s) {
     if (s->n == 0) return FL_OK;
-    k_density<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(
+    auto kern = use_prune(s) ? k_density<true> : k_density<false>;
+    kern<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(
         s->D, s->n, s->f[F_POS].cur<float4>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt,
-        s->f[F_PRESS].cur<float>());
+        s->upbits, s->f[F_PRESS].cur<float>());
     FL_LAUNCH_CHECK("density");
     return FL_OK;
 }
 
 int fl_launch_force(fl_system *s) {
     if (s->n == 0) return FL_OK;
-    k_force<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(
+    auto kern = use_prune(s) ? k_force<true> : k_force<false>;
+    kern<<<blocks_for(s->n, kForceThreads), kForceThreads, 0, s->stream>>>(
         s->D, s->n, s->f[F_POS].cur<float4>(), s->f[F_VEVAL].cur<float4>(),
-        s->f[F_PRESS].cur<float>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt,
+        s->f[F_PRESS].cur<float>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt, s->upbits,
         s->f[F_FORCE].cur<float4>());
     FL_LAUNCH_CHECK("force");
     return FL_OK;
 }
 
 int fl_launch_force_advance(fl_system *s, float dt) {
-    k_force_advance<<<blocks_for(s->n > 0 ? s->n : 1, kThreads), kThreads, 0, s->stream>>>(
+    auto kern = use_prune(s) ? k_force_advance<true> : k_force_advance<false>;
+    kern<<<blocks_for(s->n > 0 ? s->n : 1, kForceThreads), kForceThreads, 0, s->stream>>>(
         s->D, s->n, s->time_dev, s->time_slot, dt, s->f[F_POS].cur<float4>(), s->f[F_VEVAL].cur<float4>(),
-        s->f[F_PRESS].cur<float>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt,
+        s->f[F_PRESS].cur<float>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt, s->upbits,
         s->f[F_VEL].cur<float4>(), s->f[F_FORCE].cur<float4>(),
         s->f[F_POS].nxt<float4>(), s->f[F_VEVAL].nxt<float4>(), s->dev_err);
     FL_LAUNCH_CHECK("force_advance");

@@ -209,6 +209,12 @@ class FluidSystem:
         """``nsteps`` Run steps replayed from a captured CUDA graph."""
         call("fl_run_steps", self._h, int(nsteps))
 
+    def SaveCheckpoint(self, slot: int = 0) -> None:
+        call("fl_checkpoint_save", self._h, int(slot))
+
+    def RestoreCheckpoint(self, slot: int = 0) -> None:
+        call("fl_checkpoint_restore", self._h, int(slot))
+
     def Sync(self) -> None:
         call("fl_sync", self._h)
 
@@ -227,10 +233,14 @@ class FluidSystem:
     def SetTiming(self, enable: bool) -> None:
         call("fl_set_timing", self._h, 1 if enable else 0)
 
-    def TimeSteps(self, nsteps: int, graph: bool = True) -> float:
-        """Device milliseconds for ``nsteps`` Run steps, CUDA events on the system stream."""
+    def TimeSteps(self, nsteps: int, graph: bool = True, restart_every: int = 0,
+                  restart_slot: int = 0) -> float:
+        """Device milliseconds for ``nsteps`` Run steps between CUDA events on the
+        system stream; with ``restart_every`` the steps run as segments that each
+        restart from checkpoint ``restart_slot`` (restores inside the interval)."""
         ms = C.c_double()
-        call("fl_time_steps", self._h, int(nsteps), 1 if graph else 0, C.byref(ms))
+        call("fl_time_steps", self._h, int(nsteps), 1 if graph else 0, int(restart_every),
+             int(restart_slot), C.byref(ms))
         return float(ms.value)
 
     def PhaseTimes(self) -> tuple[dict, int]:

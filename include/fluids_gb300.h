@@ -208,6 +208,15 @@ int fl_run(fl_system *s);
 /* nsteps consecutive Run steps replayed from a captured CUDA graph. */
 int fl_run_steps(fl_system *s, int nsteps);
 
+/* Device-side checkpoints of the particle state (every per-point buffer
+ * and the simulation time) in one of FL_MAX_CHECKPOINTS slots, e.g. to
+ * replay a segment of steps. A slot's storage (80 B per point) is
+ * allocated on its first save and kept until fl_destroy. Restoring leaves
+ * the grid to be rebuilt by the next fl_run / fl_insert_particles. */
+#define FL_MAX_CHECKPOINTS 4
+int fl_checkpoint_save(fl_system *s, int slot);
+int fl_checkpoint_restore(fl_system *s, int slot);
+
 /* Wait for the system stream; returns FL_ERR_DEVICE if a kernel raised the
  * device error word since the last fl_sync (bits in *dev_flags if non-NULL). */
 int fl_sync(fl_system *s);
@@ -227,8 +236,11 @@ int fl_integrity_check(fl_system *s, int64_t *bad);
 int fl_set_timing(fl_system *s, int enable);
 /* Run nsteps steps (graph replay when use_graph != 0, else eager fl_run)
  * between two CUDA events on the system stream; synchronises and stores the
- * elapsed device time in *ms. */
-int fl_time_steps(fl_system *s, int nsteps, int use_graph, double *ms);
+ * elapsed device time in *ms. With restart_every > 0 the steps run as
+ * segments of at most restart_every steps, each starting from checkpoint
+ * `restart_slot` (the restore is inside the timed interval). */
+int fl_time_steps(fl_system *s, int nsteps, int use_graph, int restart_every, int restart_slot,
+                  double *ms);
 int fl_get_phase_times(fl_system *s, double ms[8], int *steps);
 
 /* ---- allocation-free scan ------------------------------------------------

@@ -221,6 +221,32 @@ def test_crowded_cell_canonical_order(m):
         for k in ("pos", "gcell", "gndx", "clr"):
             assert_bit_equal(st[k], getattr(ref, k), f"m={m} {k}")
         assert s.IntegrityCheck() == 0
+        # neighbour passes over the crowded cell (pruned loops, any size)
+        s.ComputePressureCUDA()
+        s.ComputeForceCUDA()
+        O.density(p, ref)
+        O.force(p, ref)
+        assert_bit_equal(s.GetBuffer(F.FPRESS), ref.press, f"m={m} density")
+        assert_bit_equal(s.GetBuffer(F.FFORCE), ref.force, f"m={m} force")
+
+
+@pytest.mark.parametrize("m", [90, 700, 2500])
+def test_crowded_cell_fused_steps(m):
+    sc = scenes.dam_break(n=5000, seed=18)
+    p = sc.params
+    rng = np.random.default_rng(100 + m)
+    pos = sc.pos.copy()
+    pick = rng.choice(pos.shape[0], size=m, replace=False)
+    c = np.array([p.gridMin[0] + 8.5 * 5.0, p.gridMin[1] + 4.5 * 5.0, p.gridMin[2] + 7.5 * 5.0], np.float32)
+    pos[pick] = c + rng.uniform(-2.4, 2.4, size=(m, 3)).astype(np.float32)
+    with make_system(p, pos, sc.vel, sc.veval, sc.clr) as s:
+        s.RunSteps(3)
+        s.Sync()
+        st = gpu_state(s)
+    ref = O.State.new(p, pos, sc.vel, sc.veval, sc.clr)
+    O.run(p, ref, 3, 0.0)
+    for k in FIELDS:
+        assert_bit_equal(st[k], getattr(ref, k), f"crowded m={m} {k}")
 
 
 def test_out_of_range_points_follow_the_oracle():
@@ -325,3 +351,65 @@ def test_device_error_word_starts_clear():
         s.RunSteps(6)
         s.Sync()
         assert s.DeviceStatus() == 0
+
+
+def test_checkpoint_replays_identical_steps():
+    sc = scenes.dam_break(n=6000, seed=14)
+    with make_system(sc.params, sc.pos, sc.vel, sc.veval, sc.clr) as s:
+        s.RunSteps(5)
+        s.SaveCheckpoint(1)
+        t_saved = s.time
+        s.RunSteps(7)
+        s.Sync()
+        first = gpu_state(s)
+        s.RestoreCheckpoint(1)
+        assert s.time == t_saved
+        for _ in range(7):
+            s.Run()
+        s.Sync()
+        again = gpu_state(s)
+        for k in FIELDS:
+            assert_bit_equal(again[k], first[k], f"replayed {k}")
+        with pytest.raises(F.FluidsError):
+            s.RestoreCheckpoint(3)
+
+
+def test_search_block_of_three_unpruned_path():
+    """The reference default grid (cell 0.75 h, gridSrch 3, 27 cells) takes the
+    unpruned neighbour loops; rollout bit-equal to the oracle."""
+    sc = scenes.dam_break(n=3000, seed=15)
+    p = scenes.make_params((-30.0, 0.0, -30.0), (30.0, 60.0, 30.0), grid_density=2.0)
+    assert p.gridSrch == 3
+    with make_system(p, sc.pos, sc.vel, sc.veval, sc.clr) as s:
+        s.RunSteps(4)
+        s.Sync()
+        st = gpu_state(s)
+    ref = O.State.new(p, sc.pos, sc.vel, sc.veval, sc.clr)
+    O.run(p, ref, 4, 0.0)
+    for k in FIELDS:
+        assert_bit_equal(st[k], getattr(ref, k), f"gridSrch 3 {k}")
+
+
+def test_phases_after_advance_use_the_stale_grid_like_the_reference():
+    """ComputePressure after Advance (no re-sort) reads the advanced positions
+    through the old grid, as the reference would; the band codes no longer
+    match the positions, so the unpruned loop must run."""
+    sc = scenes.dam_break(n=4000, seed=16)
+    p = sc.params
+    with make_system(p, sc.pos, sc.vel, sc.veval, sc.clr) as s:
+        s.RunSteps(10)
+        s.InsertParticlesCUDA(); s.PrefixSumCellsCUDA(1); s.CountingSortFullCUDA()
+        s.ComputePressureCUDA(); s.ComputeForceCUDA()
+        s.AdvanceCUDA(s.time, p.dt, p.sim_scale)
+        s.ComputePressureCUDA(); s.ComputeForceCUDA()
+        s.Sync()
+        st = gpu_state(s)
+    ref = O.State.new(p, st["pos"], st["vel"], st["veval"], st["clr"])
+    ref.gcell, ref.gndx = st["gcell"].copy(), st["gndx"].copy()
+    ref.cnt[:-1], ref.off[:-1] = st["gridcnt"], st["gridoff"]
+    ref.cnt[-1] = (st["gcell"] == UNDEF).sum()
+    ref.off[-1] = ref.off[-2] + ref.cnt[-2]
+    O.density(p, ref)
+    assert_bit_equal(st["press"], ref.press, "stale-grid density")
+    O.force(p, ref)
+    assert_bit_equal(st["force"], ref.force, "stale-grid force")
