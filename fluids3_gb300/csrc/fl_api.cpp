@@ -17,6 +17,10 @@
 
 #include "fl_internal.h"
 
+// Pairs the density pass records per point for the force pass (HBM: 4 B
+// per entry, 192 B per point of capacity).
+static const int kPairListCap = 48;
+
 // ---------------------------------------------------------------------------
 // errors
 
@@ -139,6 +143,7 @@ static void free_all(fl_system *s) {
     for (int k = 0; k < F_COUNT; k++)
         for (int c = 0; c < 2; c++) cudaFree(s->f[k].p[c]);
     cudaFree(s->cell_pre); cudaFree(s->rank_tmp); cudaFree(s->src); cudaFree(s->upbits);
+    cudaFree(s->hitlist); cudaFree(s->hitcnt);
     free_grid(s);
     cudaFree(s->dev_err);
     cudaFree(s->time_dev);
@@ -191,6 +196,9 @@ extern "C" int fl_create(const fl_params *p, int max_points, fl_system **out) {
         if ((r = dalloc((void **)&s->src, 4 * np)) != FL_OK) break;
         s->D.upwords = (int)((np + 31) / 32 + 1);
         if ((r = dalloc((void **)&s->upbits, fl_upbits_bytes(s))) != FL_OK) break;
+        s->D.hcap = kPairListCap;
+        if ((r = dalloc((void **)&s->hitlist, 4 * ((np + 31) / 32) * 32 * (size_t)kPairListCap)) != FL_OK) break;
+        if ((r = dalloc((void **)&s->hitcnt, 4 * np)) != FL_OK) break;
         if ((r = dalloc((void **)&s->dev_err, 256)) != FL_OK) break;
         if ((r = dalloc((void **)&s->time_dev, 256)) != FL_OK) break;
         if ((r = alloc_grid(s)) != FL_OK) break;
@@ -249,6 +257,7 @@ static TimingState *detach_timing(fl_system *s) {
 static void reset_progress(fl_system *s) {
     s->have_insert = s->have_offsets = s->have_grid = 0;
     s->codes_valid = 0;
+    s->lists_valid = 0;
     s->offsets_inclusive = 0;
 }
 
@@ -261,10 +270,11 @@ extern "C" int fl_set_params(fl_system *s, const fl_params *p) {
         s->ncells = p->gridTotal;
         FL_TRY(alloc_grid(s));
     }
-    const int upwords = s->D.upwords;
+    const int upwords = s->D.upwords, hcap = s->D.hcap;
     s->P = *p;
     fl_make_dev_params(*p, &s->D);
     s->D.upwords = upwords;
+    s->D.hcap = hcap;
     destroy_graph(s);
     reset_progress(s);
     return FL_OK;
@@ -497,6 +507,7 @@ extern "C" int fl_insert_particles(fl_system *s, uint32_t *gcell, uint32_t *gndx
     FL_TRY(fl_launch_scatter_index(s));
     FL_TRY(fl_launch_sort_cells(s, 0));
     s->codes_valid = 0;
+    s->lists_valid = 0;
     s->have_insert = 1;
     s->have_offsets = 0;
     s->have_grid = 0;
@@ -524,6 +535,7 @@ extern "C" int fl_counting_sort_full(fl_system *s, float *ppos) {
         return fl_fail(FL_ERR_STATE, "fl_counting_sort_full before insert and prefix sum");
     FL_TRY(fl_launch_gather_all(s));
     for (int k = 0; k < F_COUNT; k++) flip(s, k);
+    s->lists_valid = 0;
     FL_TRY(fl_launch_band_codes(s));
     s->have_grid = 1;
     s->have_insert = 0;   // the pre-sort cell list no longer matches the order
@@ -546,7 +558,8 @@ extern "C" int fl_compute_force(fl_system *s) {
 extern "C" int fl_advance(fl_system *s, float time, float dt, float ss) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_advance: null system");
     if (!s->have_grid) return fl_fail(FL_ERR_STATE, "fl_advance before fl_counting_sort_full");
-    s->codes_valid = 0;   // positions move; their band codes no longer hold
+    s->codes_valid = 0;   // positions move; their band codes and pair lists no longer hold
+    s->lists_valid = 0;
     return fl_launch_advance(s, time, dt, ss);
 }
 
@@ -578,6 +591,7 @@ static int run_step(fl_system *s, TimingState *t) {
     FL_TRY(fl_launch_force_advance(s, s->P.dt));
     flip(s, F_POS); flip(s, F_VEVAL);
     s->codes_valid = 0;
+    s->lists_valid = 0;
     FL_TRY(record(s, t, 6));
     s->time_slot ^= 1;
     if (t) t->steps++;

@@ -45,6 +45,7 @@ struct DevParams {
     float band;
     int prune;           // 1 when gridSrch == 2
     int upwords;         // words per axis row of the upper-band slot flags
+    int hcap;            // pair-list capacity per point
     int adj[216];
 };
 
@@ -98,6 +99,12 @@ struct fl_system {
     // band codes in pos.w while codes_valid is set
     uint32_t *upbits;
     int codes_valid;
+
+    // pairs found by the density pass, reused by the force pass while the
+    // positions and grid are unchanged (lists_valid)
+    uint32_t *hitlist;     // ceil(N/32) * hcap * 32 entries
+    uint32_t *hitcnt;      // per point
+    int lists_valid;
 
     // m_Time on the device, double-buffered by step parity so a captured
     // graph replays with the time advancing: step k reads time_dev[k & 1]

@@ -429,22 +429,38 @@ __device__ __forceinline__ bool cand_next(CandIter &it, const DevParams &P,
     return true;
 }
 
+// Pair list written by the density pass: for point i (global thread i,
+// warp w = i / 32, lane l = i % 32) entry t lives at
+// ((w * hcap + t) * 32 + l), so a warp reading entry t of all its lanes
+// touches one 128-byte line. Entries past hcap are not stored; the count
+// still records every pair, and the force pass re-walks such warps.
+__device__ __forceinline__ size_t list_at(const DevParams &P, int i, uint32_t t) {
+    return ((size_t)(i >> 5) * (size_t)P.hcap + t) * 32u + (uint32_t)(i & 31);
+}
+
 // computePressure (fluids4.0/fluid_kernels.cu:112-149). FGRID is the
 // identity after a full sort (cu:83), so neighbour slots are read directly.
-template <bool PRUNE>
+// With LIST the slots of the pairs that pass 0 < d^2 < rd2 are recorded, in
+// visiting order, for the force pass (same positions, same test).
+template <bool PRUNE, bool LIST>
 __global__ void __launch_bounds__(kThreads)
 k_density(const __grid_constant__ DevParams P, int n, const float4 *__restrict__ pos,
           const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ off,
           const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
-          float *__restrict__ press) {
+          float *__restrict__ press, uint32_t *__restrict__ hitlist, uint32_t *__restrict__ hitcnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t gc = gcell[i];
-    if (gc == kUndef) { press[i] = 0.0f; return; }
+    if (gc == kUndef) {
+        press[i] = 0.0f;
+        if (LIST) hitcnt[i] = 0;
+        return;
+    }
     const int base = (int)gc - P.nadj;
     const float4 p = pos[i];
     const uint32_t my_code = __float_as_uint(p.w);
     float sum = 0.0f;
+    uint32_t nh = 0;
     for (int c = 0; c < P.gridAdjCnt; c++) {
         CandIter it;
         cand_begin<PRUNE>(it, P, c, base + P.adj[c], my_code, true, off, cnt, upbits);
@@ -456,12 +472,17 @@ k_density(const __grid_constant__ DevParams P, int n, const float4 *__restrict__
             if (dsq < P.rd2 && dsq > 0.0f) {
                 dsq = (P.rd2 - dsq) * P.d2;
                 sum += dsq * dsq * dsq;
+                if (LIST) {
+                    if (nh < (uint32_t)P.hcap) hitlist[list_at(P, i, nh)] = j;
+                    nh++;
+                }
             }
         }
     }
     sum = sum * P.pmass * P.poly6kern;
     if (sum == 0.0f) sum = 1.0f;
     press[i] = sum;
+    if (LIST) hitcnt[i] = nh;
 }
 
 // computeForce (fluids4.0/fluid_kernels.cu:180-217) in two stages per warp:
@@ -481,44 +502,54 @@ struct ForcePoint {
     float3 f;
 };
 
+// One pair's term, added in the reference's operation order
+// (fluid_kernels.cu:203-210); j is known to pass 0 < d^2 < rd2.
+__device__ __forceinline__ void add_pair_force(const DevParams &P, ForcePoint &fp, uint32_t j,
+                                               const float4 *__restrict__ pos,
+                                               const float4 *__restrict__ veval,
+                                               const float *__restrict__ press) {
+    const float4 q = pos[j];
+    const float dx = fp.p.x - q.x, dy = fp.p.y - q.y, dz = fp.p.z - q.z;
+    const float dsq = dx * dx + dy * dy + dz * dz;
+    const float r = sqrtf(dsq * P.d2);
+    const float dj = press[j];
+    const float pj = (dj - P.prest_dens) * P.pintstiff;
+    const float cr = P.psmoothradius - r;
+    const float pterm = P.sim_scale * -0.5f * cr * P.spikykern * (fp.pi + pj) / r;
+    const float4 vj = veval[j];
+    const float sx = dx * pterm + (vj.x - fp.vi.x) * P.vterm;
+    const float sy = dy * pterm + (vj.y - fp.vi.y) * P.vterm;
+    const float sz = dz * pterm + (vj.z - fp.vi.z) * P.vterm;
+    const float inv = 1.0f / (fp.di * dj);
+    fp.f.x += (sx * cr) * inv;
+    fp.f.y += (sy * cr) * inv;
+    fp.f.z += (sz * cr) * inv;
+}
+
 __device__ __forceinline__ void drain_hits(const DevParams &P, ForcePoint &fp, uint32_t &nhits,
                                            const uint32_t *hits, const float4 *__restrict__ pos,
                                            const float4 *__restrict__ veval,
                                            const float *__restrict__ press) {
     const uint32_t most = __reduce_max_sync(0xffffffffu, nhits);
-    for (uint32_t t = 0; t < most; t++) {
-        if (t < nhits) {
-            const uint32_t j = hits[t * kForceThreads];
-            const float4 q = pos[j];
-            const float dx = fp.p.x - q.x, dy = fp.p.y - q.y, dz = fp.p.z - q.z;
-            const float dsq = dx * dx + dy * dy + dz * dz;
-            const float r = sqrtf(dsq * P.d2);
-            const float dj = press[j];
-            const float pj = (dj - P.prest_dens) * P.pintstiff;
-            const float cr = P.psmoothradius - r;
-            const float pterm = P.sim_scale * -0.5f * cr * P.spikykern * (fp.pi + pj) / r;
-            const float4 vj = veval[j];
-            const float sx = dx * pterm + (vj.x - fp.vi.x) * P.vterm;
-            const float sy = dy * pterm + (vj.y - fp.vi.y) * P.vterm;
-            const float sz = dz * pterm + (vj.z - fp.vi.z) * P.vterm;
-            const float inv = 1.0f / (fp.di * dj);
-            fp.f.x += (sx * cr) * inv;
-            fp.f.y += (sy * cr) * inv;
-            fp.f.z += (sz * cr) * inv;
-        }
-    }
+    for (uint32_t t = 0; t < most; t++)
+        if (t < nhits) add_pair_force(P, fp, hits[t * kForceThreads], pos, veval, press);
     nhits = 0;
 }
 
-// The force on point i (all 32 lanes of the warp must call this).
-template <bool PRUNE>
+// The force on point i (all 32 lanes of the warp must call this). With
+// LIST the pairs come from the density pass's list (every lane draining its
+// own list in step); a warp with a point whose pairs overflowed the list
+// walks its candidates again instead.
+template <bool PRUNE, bool LIST>
 __device__ __forceinline__ float3 force_of(const DevParams &P, int i, bool active, uint32_t gc,
                                            const float4 *__restrict__ pos,
                                            const float4 *__restrict__ veval,
                                            const float *__restrict__ press,
                                            const uint32_t *__restrict__ off,
                                            const uint32_t *__restrict__ cnt,
-                                           const uint32_t *__restrict__ upbits) {
+                                           const uint32_t *__restrict__ upbits,
+                                           const uint32_t *__restrict__ hitlist,
+                                           const uint32_t *__restrict__ hitcnt) {
     __shared__ uint32_t s_hits[kHitCap * kForceThreads];
     uint32_t *hits = s_hits + threadIdx.x;
     ForcePoint fp;
@@ -532,6 +563,15 @@ __device__ __forceinline__ float3 force_of(const DevParams &P, int i, bool activ
         fp.pi = (fp.di - P.prest_dens) * P.pintstiff;
         my_code = __float_as_uint(fp.p.w);
         base = (int)gc - P.nadj;
+    }
+    if (LIST) {
+        const uint32_t nh = active ? hitcnt[i] : 0u;
+        if (!__any_sync(0xffffffffu, nh > (uint32_t)P.hcap)) {
+            const uint32_t most = __reduce_max_sync(0xffffffffu, nh);
+            for (uint32_t t = 0; t < most; t++)
+                if (t < nh) add_pair_force(P, fp, hitlist[list_at(P, i, t)], pos, veval, press);
+            return fp.f;
+        }
     }
     uint32_t nhits = 0;
     for (int c = 0; c < P.gridAdjCnt; c++) {
@@ -555,17 +595,19 @@ __device__ __forceinline__ float3 force_of(const DevParams &P, int i, bool activ
     return fp.f;
 }
 
-template <bool PRUNE>
+template <bool PRUNE, bool LIST>
 __global__ void __launch_bounds__(kForceThreads)
 k_force(const __grid_constant__ DevParams P, int n, const float4 *__restrict__ pos,
         const float4 *__restrict__ veval, const float *__restrict__ press,
         const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ off,
         const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
+        const uint32_t *__restrict__ hitlist, const uint32_t *__restrict__ hitcnt,
         float4 *__restrict__ force) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t gc = (i < n) ? gcell[i] : kUndef;
     const bool active = gc != kUndef;
-    const float3 f = force_of<PRUNE>(P, i, active, gc, pos, veval, press, off, cnt, upbits);
+    const float3 f = force_of<PRUNE, LIST>(P, i, active, gc, pos, veval, press, off, cnt, upbits,
+                                           hitlist, hitcnt);
     if (i < n) force[i] = active ? make_float4(f.x, f.y, f.z, 0.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
@@ -672,13 +714,14 @@ k_advance(const __grid_constant__ DevParams P, int n, float time, float dt, floa
 // Force then advance for one point: the last two phases of Run fused.
 // Neighbour reads come from pos_in/veval_in; the new position and evaluated
 // velocity go to the other copies, velocity and force are updated in place.
-template <bool PRUNE>
+template <bool PRUNE, bool LIST>
 __global__ void __launch_bounds__(kForceThreads)
 k_force_advance(const __grid_constant__ DevParams P, int n, float *time_dev, int slot, float dt,
                 const float4 *__restrict__ pos_in, const float4 *__restrict__ veval_in,
                 const float *__restrict__ press, const uint32_t *__restrict__ gcell,
                 const uint32_t *__restrict__ off, const uint32_t *__restrict__ cnt,
                 const uint32_t *__restrict__ upbits,
+                const uint32_t *__restrict__ hitlist, const uint32_t *__restrict__ hitcnt,
                 float4 *__restrict__ vel, float4 *__restrict__ force,
                 float4 *__restrict__ pos_out, float4 *__restrict__ veval_out,
                 uint32_t *__restrict__ err) {
@@ -687,7 +730,8 @@ k_force_advance(const __grid_constant__ DevParams P, int n, float *time_dev, int
     if (i == 0) time_dev[slot ^ 1] = time + dt;
     const uint32_t gc = (i < n) ? gcell[i] : kUndef;
     const bool active = gc != kUndef;
-    const float3 f = force_of<PRUNE>(P, i, active, gc, pos_in, veval_in, press, off, cnt, upbits);
+    const float3 f = force_of<PRUNE, LIST>(P, i, active, gc, pos_in, veval_in, press, off, cnt, upbits,
+                                           hitlist, hitcnt);
     if (i >= n) return;
     if (!active) {
         force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -833,30 +877,45 @@ int fl_launch_band_codes(fl_system *s) {
 
 int fl_launch_density(fl_system *s) {
     if (s->n == 0) return FL_OK;
-    auto kern = use_prune(s) ? k_density<true> : k_density<false>;
+    auto kern = use_prune(s) ? k_density<true, true> : k_density<false, true>;
     kern<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(
         s->D, s->n, s->f[F_POS].cur<float4>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt,
-        s->upbits, s->f[F_PRESS].cur<float>());
+        s->upbits, s->f[F_PRESS].cur<float>(), s->hitlist, s->hitcnt);
     FL_LAUNCH_CHECK("density");
+    s->lists_valid = 1;
     return FL_OK;
+}
+
+template <bool LIST>
+static void force_kernels(bool prune, decltype(&k_force<true, true>) *kf,
+                          decltype(&k_force_advance<true, true>) *kfa) {
+    *kf = prune ? k_force<true, LIST> : k_force<false, LIST>;
+    *kfa = prune ? k_force_advance<true, LIST> : k_force_advance<false, LIST>;
 }
 
 int fl_launch_force(fl_system *s) {
     if (s->n == 0) return FL_OK;
-    auto kern = use_prune(s) ? k_force<true> : k_force<false>;
-    kern<<<blocks_for(s->n, kForceThreads), kForceThreads, 0, s->stream>>>(
+    decltype(&k_force<true, true>) kf;
+    decltype(&k_force_advance<true, true>) kfa;
+    if (s->lists_valid) force_kernels<true>(use_prune(s), &kf, &kfa);
+    else force_kernels<false>(use_prune(s), &kf, &kfa);
+    kf<<<blocks_for(s->n, kForceThreads), kForceThreads, 0, s->stream>>>(
         s->D, s->n, s->f[F_POS].cur<float4>(), s->f[F_VEVAL].cur<float4>(),
         s->f[F_PRESS].cur<float>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt, s->upbits,
-        s->f[F_FORCE].cur<float4>());
+        s->hitlist, s->hitcnt, s->f[F_FORCE].cur<float4>());
     FL_LAUNCH_CHECK("force");
     return FL_OK;
 }
 
 int fl_launch_force_advance(fl_system *s, float dt) {
-    auto kern = use_prune(s) ? k_force_advance<true> : k_force_advance<false>;
-    kern<<<blocks_for(s->n > 0 ? s->n : 1, kForceThreads), kForceThreads, 0, s->stream>>>(
+    decltype(&k_force<true, true>) kf;
+    decltype(&k_force_advance<true, true>) kfa;
+    if (s->lists_valid) force_kernels<true>(use_prune(s), &kf, &kfa);
+    else force_kernels<false>(use_prune(s), &kf, &kfa);
+    kfa<<<blocks_for(s->n > 0 ? s->n : 1, kForceThreads), kForceThreads, 0, s->stream>>>(
         s->D, s->n, s->time_dev, s->time_slot, dt, s->f[F_POS].cur<float4>(), s->f[F_VEVAL].cur<float4>(),
         s->f[F_PRESS].cur<float>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt, s->upbits,
+        s->hitlist, s->hitcnt,
         s->f[F_VEL].cur<float4>(), s->f[F_FORCE].cur<float4>(),
         s->f[F_POS].nxt<float4>(), s->f[F_VEVAL].nxt<float4>(), s->dev_err);
     FL_LAUNCH_CHECK("force_advance");
