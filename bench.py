@@ -150,15 +150,16 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel: str):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+def ncu_record(kernel: str) -> dict:
+    """The committed ncu figures for `kernel` (DRAM bytes per launch, observed
+    bound, issue activity), if any."""
     f = ROOT / "profiles" / "traffic.json"
     if not f.exists():
-        return None
+        return {}
     try:
-        return json.loads(f.read_text()).get(kernel, {}).get("dram_bytes_per_launch")
+        return json.loads(f.read_text()).get(kernel, {})
     except ValueError:
-        return None
+        return {}
 
 
 # ---------------------------------------------------------------------------
@@ -370,10 +371,14 @@ def our_arm(args, rank, world, local_rank):
     algo = ALGO_BYTES[dominant] * n_in
     achieved = algo / (dur_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
-    traffic = ncu_traffic(dominant)
+    rec = ncu_record(dominant)
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": f"of {peak_kind}", "traffic": traffic,
-                "algorithmic_bytes_per_launch": algo, "mean_launch_ms": dur_ms}
+                "frac": achieved / peak, "peak_source": f"of {peak_kind}",
+                "traffic": rec.get("dram_bytes_per_launch"),
+                "algorithmic_bytes_per_launch": algo, "mean_launch_ms": dur_ms,
+                "bound_observed": rec.get("bound_observed"),
+                "issue_active_pct_ncu": rec.get("issue_active_pct"),
+                "profile": "profiles/ncu_wave_tank_4m.md"}
     step_bytes = sum(ALGO_BYTES[k] for k in ALGO_BYTES) * n_in + 12 * (p.gridTotal + 1)
     cpu = None
     if not args.no_cpu_baseline:
