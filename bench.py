@@ -71,6 +71,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=None, help="steps in the e2e region (default: min(K, 20))")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-scenes", type=int, default=256,
+                    help="scenes in the batched-vs-one-at-a-time comparison (0 skips it)")
+    ap.add_argument("--batch-steps", type=int, default=20)
     return ap.parse_args()
 
 
@@ -248,6 +251,58 @@ def reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def batched_comparison(args):
+    """The batched multi-scene workload: `args.batch_scenes` scenes of
+    2,048..65,536 points (log-uniform), each with its own box, grid,
+    viscosity and rest density, stepped (a) together as one batched system
+    and (b) one at a time, each as its own plain system -- same steps, same
+    timing protocol (graph replay, segments restarting from the warm state).
+    Every scene's final state is compared bit for bit between (a) and (b)."""
+    import fluids3_gb300 as F
+    from fluids3_gb300 import scenes
+
+    scs = scenes.batch_scenes(args.batch_scenes)
+    total = sum(sc.n for sc in scs)
+    k = args.batch_steps
+    seg = args.segment
+    cat = scenes.concat(scs)
+    b = F.FluidSystem.batch([sc.params for sc in scs], [sc.n for sc in scs])
+    b.SetParticles(cat["pos"], cat["vel"], cat["veval"], clr=cat["clr"])
+    b.RunSteps(max(args.warmup, 3))
+    b.SaveCheckpoint(0)
+    ms_b = b.TimeSteps(k, graph=True, restart_every=seg, restart_slot=0)
+    b.Sync()
+    st_b = {f: b.GetBuffer(getattr(F, "F" + f.upper())) for f in ("pos", "vel", "veval", "gcell")}
+    infos = [b.SceneInfo(q) for q in range(len(scs))]
+    b.close()
+    ms_seq = 0.0
+    same = 0
+    for q, sc in enumerate(scs):
+        s = F.FluidSystem(sc.params, sc.n)
+        s.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
+        s.RunSteps(max(args.warmup, 3))
+        s.SaveCheckpoint(0)
+        ms_seq += s.TimeSteps(k, graph=True, restart_every=seg, restart_slot=0)
+        s.Sync()
+        a, n = infos[q]["point_base"], infos[q]["n"]
+        ok = True
+        for f in st_b:
+            got = st_b[f][a:a + n].copy()
+            if f == "gcell":   # batched cells index the concatenated grid
+                got[got != 0xFFFFFFFF] -= np.uint32(infos[q]["cell_base"])
+            ok = ok and np.array_equal(s.GetBuffer(getattr(F, "F" + f.upper())).view(np.uint32),
+                                       got.view(np.uint32))
+        same += int(ok)
+        s.close()
+    vb = total * k / (ms_b / 1e3) / 1e6
+    vs = total * k / (ms_seq / 1e3) / 1e6
+    return {"scenes": len(scs), "points": total, "steps": k, "value": vb, "unit": METRIC,
+            "one_at_a_time_value": vs, "speedup": vb / vs, "ms_per_step": ms_b / k,
+            "one_at_a_time_ms_per_step": ms_seq / k, "scenes_bit_identical": same,
+            "workload": "scenes log-uniform 2,048..65,536 points, fill U[0.2,0.6] of own box, "
+                        "visc U[0.1,0.5], rest density U[500,700], dam-break parameters otherwise"}
+
+
 def config_of(scene, args):
     p = scene.params
     return {"workload": f"{scene.name}: {scene.n:,}-point SPH wave tank (dam break with X- wall forcing, "
@@ -365,6 +420,7 @@ def our_arm(args, rank, world, local_rank):
     if rank != 0:
         return
 
+    batched = batched_comparison(args) if args.batch_scenes > 0 else None
     value = world * scene.n * args.steps / (ms / 1e3) / 1e6
     dominant = max((k for k in phases if k != "scan"), key=lambda k: phases[k])
     dur_ms = phases[dominant]
@@ -397,6 +453,7 @@ def our_arm(args, rank, world, local_rank):
         "cpu_baseline": cpu,
         "e2e": {"value": world * n * e2e_steps / e2e_s / 1e6, "unit": METRIC, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+        "batched": batched,
         "clocks": clocks.summary(t0, t1),
         "gpu_launches": KERNELS_PER_STEP * args.steps,
         "device_status": status,

@@ -27,6 +27,10 @@ SIGNATURES = [
     ("fl_params_derive", C.c_int, [C.POINTER(FlParams)]),
     ("fl_create", C.c_int, [C.POINTER(FlParams), C.c_int, C.POINTER(vp)]),
     ("fl_destroy", C.c_int, [vp]),
+    ("fl_batch_create", C.c_int, [C.POINTER(FlParams), C.POINTER(C.c_int), C.c_int, C.POINTER(vp)]),
+    ("fl_num_scenes", C.c_int, [vp]),
+    ("fl_batch_scene_info", C.c_int, [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                      C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("fl_set_params", C.c_int, [vp, C.POINTER(FlParams)]),
     ("fl_get_params", C.c_int, [vp, C.POINTER(FlParams)]),
     ("fl_num_points", C.c_int, [vp]),

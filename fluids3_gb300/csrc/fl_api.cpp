@@ -114,7 +114,7 @@ static size_t grid_block_bytes(const fl_system *s) {
 
 static int alloc_grid(fl_system *s) {
     const size_t tile = fl_scan_tile();
-    const size_t entries = (size_t)s->ncells + 1;
+    const size_t entries = (size_t)s->gcells;
     s->scan_tiles = (int)((entries + tile - 1) / tile);
     s->grid_pad = (size_t)s->scan_tiles * tile;
     void *blk = nullptr, *off = nullptr;
@@ -144,6 +144,8 @@ static void free_all(fl_system *s) {
         for (int c = 0; c < 2; c++) cudaFree(s->f[k].p[c]);
     cudaFree(s->cell_pre); cudaFree(s->rank_tmp); cudaFree(s->src); cudaFree(s->upbits);
     cudaFree(s->hitlist); cudaFree(s->hitcnt);
+    cudaFree(s->d_scenes); cudaFree(s->point_scene); cudaFree(s->cell_scene);
+    free(s->scene_point_base); free(s->scene_n); free(s->scene_cell_base); free(s->scene_ncells);
     free_grid(s);
     cudaFree(s->dev_err);
     cudaFree(s->time_dev);
@@ -184,6 +186,8 @@ extern "C" int fl_create(const fl_params *p, int max_points, fl_system **out) {
         fl_make_dev_params(*p, &s->D);
         s->max_points = max_points;
         s->ncells = p->gridTotal;
+        s->gcells = p->gridTotal + 1;
+        s->nscenes = 1;
         const size_t np = (size_t)(max_points > 0 ? max_points : 1);
         const size_t esz[F_COUNT] = {16, 16, 16, 16, 4, 4, 4, 4};
         for (int k = 0; k < F_COUNT && r == FL_OK; k++) {
@@ -231,6 +235,120 @@ extern "C" int fl_create(const fl_params *p, int max_points, fl_system **out) {
     return FL_OK;
 }
 
+// ---------------------------------------------------------------------------
+// batched systems
+
+extern "C" int fl_batch_create(const fl_params *params, const int *counts, int nscenes, fl_system **out) {
+    if (!params || !counts || !out) return fl_fail(FL_ERR_ARG, "fl_batch_create: null argument");
+    *out = nullptr;
+    if (nscenes < 1 || nscenes > 65535)
+        return fl_fail(FL_ERR_ARG, "fl_batch_create: %d scenes (1..65535)", nscenes);
+    long long npts = 0, ncell = 0, gcell = 0;
+    int all_prune = 1;
+    for (int k = 0; k < nscenes; k++) {
+        FL_TRY(check_derived(&params[k]));
+        if (counts[k] < 0) return fl_fail(FL_ERR_ARG, "fl_batch_create: scene %d count < 0", k);
+        if (params[k].dt != params[0].dt)
+            return fl_fail(FL_ERR_PARAMS, "fl_batch_create: scene %d has dt %g, scene 0 %g (the batch shares one clock)",
+                           k, (double)params[k].dt, (double)params[0].dt);
+        npts += counts[k];
+        ncell += params[k].gridTotal;
+        gcell += params[k].gridTotal + 1;
+        if (params[k].gridSrch != 2) all_prune = 0;
+    }
+    if (npts > (1LL << 31) - 1 || gcell > (1LL << 30))
+        return fl_fail(FL_ERR_PARAMS, "fl_batch_create: %lld points / %lld cell entries exceed the limits", npts, gcell);
+
+    // allocate as one big system over the concatenation, then install the scene table
+    fl_params p0 = params[0];
+    p0.gridTotal = (int)ncell;                      // reference-layout cells (all scenes)
+    p0.gridRes[0] = (int)ncell; p0.gridRes[1] = 1; p0.gridRes[2] = 1;
+    fl_system *s = nullptr;
+    FL_TRY(fl_create(&p0, (int)npts, &s));
+    int r = FL_OK;
+    do {
+        s->P = params[0];
+        s->batched = 1;
+        s->nscenes = nscenes;
+        free_grid(s);
+        s->ncells = (int)ncell;
+        s->gcells = (int)gcell;
+        if ((r = alloc_grid(s)) != FL_OK) break;
+        s->scene_point_base = (int *)calloc(nscenes, sizeof(int));
+        s->scene_n = (int *)calloc(nscenes, sizeof(int));
+        s->scene_cell_base = (int *)calloc(nscenes, sizeof(int));
+        s->scene_ncells = (int *)calloc(nscenes, sizeof(int));
+        std::vector<DevParams> tab(nscenes);
+        std::vector<uint16_t> pscene((size_t)(npts > 0 ? npts : 1)), cscene((size_t)gcell);
+        if (!s->scene_point_base || !s->scene_n || !s->scene_cell_base || !s->scene_ncells) {
+            r = fl_fail(FL_ERR_NOMEM, "fl_batch_create: host allocation failed");
+            break;
+        }
+        long long pb = 0, cb = 0;
+        for (int k = 0; k < nscenes; k++) {
+            fl_make_dev_params(params[k], &tab[k]);
+            tab[k].cell_base = (int)cb;
+            tab[k].upwords = s->D.upwords;
+            tab[k].hcap = s->D.hcap;
+            tab[k].prune = all_prune;
+            s->scene_point_base[k] = (int)pb;
+            s->scene_n[k] = counts[k];
+            s->scene_cell_base[k] = (int)cb;
+            s->scene_ncells[k] = params[k].gridTotal;
+            for (long long i = 0; i < counts[k]; i++) pscene[(size_t)(pb + i)] = (uint16_t)k;
+            for (long long c = 0; c <= params[k].gridTotal; c++) cscene[(size_t)(cb + c)] = (uint16_t)k;
+            pb += counts[k];
+            cb += params[k].gridTotal + 1;
+        }
+        // launch-wide constants come from scene 0's block
+        const int upwords = s->D.upwords, hcap = s->D.hcap;
+        s->D = tab[0];
+        s->D.upwords = upwords;
+        s->D.hcap = hcap;
+        s->D.prune = all_prune;
+        if ((r = dalloc((void **)&s->d_scenes, sizeof(DevParams) * nscenes)) != FL_OK) break;
+        if ((r = dalloc((void **)&s->point_scene, sizeof(uint16_t) * pscene.size())) != FL_OK) break;
+        if ((r = dalloc((void **)&s->cell_scene, sizeof(uint16_t) * cscene.size())) != FL_OK) break;
+        if (cudaMemcpy(s->d_scenes, tab.data(), sizeof(DevParams) * nscenes, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(s->point_scene, pscene.data(), sizeof(uint16_t) * pscene.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(s->cell_scene, cscene.data(), sizeof(uint16_t) * cscene.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+            r = fl_fail(FL_ERR_CUDA, "fl_batch_create: scene table upload failed");
+            break;
+        }
+        if (cudaStreamSynchronize(s->stream) != cudaSuccess) {
+            r = fl_fail(FL_ERR_CUDA, "fl_batch_create: %s", cudaGetErrorString(cudaGetLastError()));
+            break;
+        }
+    } while (0);
+    if (r != FL_OK) {
+        fl_destroy(s);
+        return r;
+    }
+    *out = s;
+    return FL_OK;
+}
+
+extern "C" int fl_batch_scene_info(const fl_system *s, int scene, int *point_base, int *n, int *cell_base,
+                                   int *ncells) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_batch_scene_info: null system");
+    if (scene < 0 || scene >= s->nscenes) return fl_fail(FL_ERR_ARG, "fl_batch_scene_info: scene %d", scene);
+    int pb = 0, np = s->n, cb = 0, nc = s->ncells;
+    if (s->batched) {
+        pb = s->scene_point_base[scene];
+        np = s->scene_n[scene];
+        nc = s->scene_ncells[scene];
+        cb = 0;
+        for (int k = 0; k < scene; k++) cb += s->scene_ncells[k];   // reference-layout position
+    }
+    if (point_base) *point_base = pb;
+    if (n) *n = np;
+    if (cell_base) *cell_base = cb;
+    if (ncells) *ncells = nc;
+    return FL_OK;
+}
+
+extern "C" int fl_num_scenes(const fl_system *s) { return s ? s->nscenes : 0; }
+
 extern "C" int fl_destroy(fl_system *s) {
     if (!s) return FL_OK;
     cudaStreamSynchronize(s->stream);
@@ -265,9 +383,12 @@ extern "C" int fl_set_params(fl_system *s, const fl_params *p) {
     if (!s || !p) return fl_fail(FL_ERR_ARG, "fl_set_params: null argument");
     FL_TRY(check_derived(p));
     FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (s->batched)
+        return fl_fail(FL_ERR_STATE, "fl_set_params: a batched system keeps the parameters it was created with");
     if (p->gridTotal != s->ncells) {
         free_grid(s);
         s->ncells = p->gridTotal;
+        s->gcells = p->gridTotal + 1;
         FL_TRY(alloc_grid(s));
     }
     const int upwords = s->D.upwords, hcap = s->D.hcap;
@@ -354,6 +475,9 @@ extern "C" int fl_set_particles(fl_system *s, int n, const float *pos, const flo
     if (n < 0) return fl_fail(FL_ERR_ARG, "fl_set_particles: n < 0");
     if (n > s->max_points)
         return fl_fail(FL_ERR_CAPACITY, "fl_set_particles: %d points exceed capacity %d", n, s->max_points);
+    if (s->batched && n != s->max_points)
+        return fl_fail(FL_ERR_ARG, "fl_set_particles: a batched system takes all %d points (scenes concatenated)",
+                       s->max_points);
     destroy_graph(s);
     s->n = n;
     if (n > 0) {
@@ -410,26 +534,29 @@ static int export_to_device(fl_system *s, int id, void *dev) {
     const int fi = field_of(id);
     if (id == FL_FPOS || id == FL_FVEL || id == FL_FVEVAL || id == FL_FFORCE)
         return fl_launch_pack3(s, s->f[fi].cur<float4>(), (float *)dev, s->n);
+    if (id == FL_FGCELL && s->batched) return fl_launch_gcell_ref(s, (uint32_t *)dev);
     if (fi >= 0) {
         FL_CUDA_TRY(cudaMemcpyAsync(dev, s->f[fi].cur<void>(), 4 * (size_t)s->n,
                                     cudaMemcpyDeviceToDevice, s->stream));
         return FL_OK;
     }
-    if (id == FL_FGRIDCNT) {
-        FL_CUDA_TRY(cudaMemcpyAsync(dev, s->cnt, 4 * (size_t)s->ncells, cudaMemcpyDeviceToDevice, s->stream));
-        return FL_OK;
-    }
-    if (id == FL_FGRIDOFF) {
-        FL_CUDA_TRY(cudaMemcpyAsync(dev, s->off, 4 * (size_t)s->ncells, cudaMemcpyDeviceToDevice, s->stream));
+    if (id == FL_FGRIDCNT || id == FL_FGRIDOFF) {
+        // reference layout: each scene's C cells, without its out-of-range bin
+        const uint32_t *srcg = (id == FL_FGRIDCNT) ? s->cnt : s->off;
+        size_t at = 0;
+        for (int sc = 0; sc < s->nscenes; sc++) {
+            const int base = s->batched ? s->scene_cell_base[sc] : 0;
+            const int c = s->batched ? s->scene_ncells[sc] : s->ncells;
+            FL_CUDA_TRY(cudaMemcpyAsync((uint32_t *)dev + at, srcg + base, 4 * (size_t)c,
+                                        cudaMemcpyDeviceToDevice, s->stream));
+            at += (size_t)c;
+        }
         return FL_OK;
     }
     if (id == FL_FGRID) {
-        // identity over the in-range slots (countingSortFull sets FGRID[s] = s, cu:83)
-        uint32_t n_in = 0;
-        FL_CUDA_TRY(cudaMemcpyAsync(&n_in, s->off + s->ncells, 4, cudaMemcpyDeviceToHost, s->stream));
-        FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
-        if (!s->have_grid) n_in = 0;
-        return fl_launch_grid_identity(s, (uint32_t *)dev, s->n, (int)n_in);
+        // identity over the in-range sorted slots (countingSortFull sets FGRID[s] = s, cu:83)
+        return fl_launch_grid_identity(s, (uint32_t *)dev, s->n,
+                                       s->have_grid ? s->f[F_GCELL].cur<uint32_t>() : nullptr);
     }
     return fl_fail(FL_ERR_ARG, "unknown buffer id %d", id);
 }
@@ -447,7 +574,10 @@ extern "C" int fl_get_buffer(fl_system *s, int id, void *host, size_t bytes) {
     if (id == FL_FGRIDOFF && s->offsets_inclusive) {
         // zero_offsets = 0 asks for the inclusive scan: off[c] + cnt[c]
         std::vector<uint32_t> cnt(s->ncells);
-        FL_CUDA_TRY(cudaMemcpy(cnt.data(), s->cnt, 4 * (size_t)s->ncells, cudaMemcpyDeviceToHost));
+        FL_TRY(export_to_device(s, FL_FGRIDCNT, s->stage));
+        FL_CUDA_TRY(cudaMemcpyAsync(cnt.data(), s->stage, 4 * (size_t)s->ncells, cudaMemcpyDeviceToHost,
+                                    s->stream));
+        FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
         uint32_t *o = (uint32_t *)host;
         for (int c = 0; c < s->ncells; c++) o[c] += cnt[c];
     }
@@ -470,6 +600,8 @@ extern "C" int fl_import_device(fl_system *s, int n, const void *dev_pos, const 
     if (!s || !dev_pos) return fl_fail(FL_ERR_ARG, "fl_import_device: null system or pos");
     if (n < 0 || n > s->max_points)
         return fl_fail(FL_ERR_CAPACITY, "fl_import_device: %d points (capacity %d)", n, s->max_points);
+    if (s->batched && n != s->max_points)
+        return fl_fail(FL_ERR_ARG, "fl_import_device: a batched system takes all %d points", s->max_points);
     destroy_graph(s);
     s->n = n;
     FL_TRY(fl_launch_unpack3(s, (const float *)dev_pos, s->f[F_POS].cur<float4>(), n));
@@ -503,7 +635,7 @@ extern "C" int fl_insert_particles(fl_system *s, uint32_t *gcell, uint32_t *gndx
     FL_TRY(clear_grid(s));
     FL_TRY(fl_launch_insert(s, s->f[F_GCELL].cur<uint32_t>()));
     // canonical gndx: offsets, arrival-order index scatter, per-cell sort
-    FL_TRY(fl_launch_scan(s, s->ncells + 1, 0));
+    FL_TRY(fl_launch_scan(s, s->gcells, 0));
     FL_TRY(fl_launch_scatter_index(s));
     FL_TRY(fl_launch_sort_cells(s, 0));
     s->codes_valid = 0;
@@ -513,14 +645,14 @@ extern "C" int fl_insert_particles(fl_system *s, uint32_t *gcell, uint32_t *gndx
     s->have_grid = 0;
     FL_TRY(readback(s, gcell, s->f[F_GCELL].cur<void>(), 4 * (size_t)s->n));
     FL_TRY(readback(s, gndx, s->f[F_GNDX].cur<void>(), 4 * (size_t)s->n));
-    FL_TRY(readback(s, gcnt, s->cnt, 4 * (size_t)s->ncells));
+    if (gcnt) FL_TRY(fl_get_buffer(s, FL_FGRIDCNT, gcnt, 4 * (size_t)s->ncells));
     return FL_OK;
 }
 
 extern "C" int fl_prefix_sum_cells(fl_system *s, uint32_t *goff, int zero_offsets) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_prefix_sum_cells: null system");
     if (!s->have_insert) return fl_fail(FL_ERR_STATE, "fl_prefix_sum_cells before fl_insert_particles");
-    FL_TRY(fl_launch_scan(s, s->ncells + 1, 1));
+    FL_TRY(fl_launch_scan(s, s->gcells, 1));
     s->have_offsets = 1;
     s->offsets_inclusive = zero_offsets ? 0 : 1;
     if (goff) FL_TRY(fl_get_buffer(s, FL_FGRIDOFF, goff, 4 * (size_t)s->ncells));
@@ -579,7 +711,7 @@ static int run_step(fl_system *s, TimingState *t) {
     FL_TRY(clear_grid(s));
     FL_TRY(fl_launch_insert(s, nullptr));
     FL_TRY(record(s, t, 1));
-    FL_TRY(fl_launch_scan(s, s->ncells + 1, 0));
+    FL_TRY(fl_launch_scan(s, s->gcells, 0));
     FL_TRY(record(s, t, 2));
     FL_TRY(fl_launch_scatter_index(s));
     FL_TRY(record(s, t, 3));

@@ -46,10 +46,20 @@ struct DevParams {
     int prune;           // 1 when gridSrch == 2
     int upwords;         // words per axis row of the upper-band slot flags
     int hcap;            // pair-list capacity per point
+    int cell_base;       // first internal cell entry of this scene (0 for a single scene)
     int adj[216];
 };
 
 void fl_make_dev_params(const fl_params &p, DevParams *d);
+
+// Scene table of a batched system: per-scene parameter blocks and the
+// scene of every point slot and internal cell entry. `params` is null for a
+// single-scene system, whose kernels take their parameters by value.
+struct SceneTab {
+    const DevParams *params;
+    const uint16_t *point_scene;
+    const uint16_t *cell_scene;
+};
 
 // One particle field held twice in HBM. Gathers (the counting sort) and the
 // fused force+advance pass write the copy that is not live and then flip,
@@ -71,8 +81,16 @@ struct fl_system {
     DevParams D;
     int max_points;
     int n;                 // live point count
-    int ncells;            // C
+    int ncells;            // C (reference-layout cells; summed over scenes when batched)
+    int gcells;            // internal cell entries: C + 1 per scene (the extra one: out-of-range bin)
     float time;
+
+    // batched systems: nscenes > 1 or batched != 0
+    int batched;
+    int nscenes;
+    DevParams *d_scenes;   // device table, one block per scene
+    uint16_t *point_scene, *cell_scene;
+    int *scene_point_base, *scene_n, *scene_cell_base, *scene_ncells;   // host copies
 
     Field f[F_COUNT];      // pos/vel/veval/force: float4; press: float; clr/gcell/gndx: uint
 
@@ -156,7 +174,8 @@ int fl_launch_force_advance(fl_system *s, float dt);
 int fl_launch_advance(fl_system *s, float time, float dt, float ss);
 int fl_launch_pack3(fl_system *s, const float4 *src, float *dst, int n);
 int fl_launch_unpack3(fl_system *s, const float *src, float4 *dst, int n);
-int fl_launch_grid_identity(fl_system *s, uint32_t *dst, int n, int n_in);
+int fl_launch_grid_identity(fl_system *s, uint32_t *dst, int n, const uint32_t *gcell);
+int fl_launch_gcell_ref(fl_system *s, uint32_t *dst);
 int fl_launch_integrity(fl_system *s, unsigned long long *bad_dev);
 size_t fl_scan_tile();
 size_t fl_upbits_bytes(const fl_system *s);

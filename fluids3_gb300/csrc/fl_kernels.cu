@@ -98,17 +98,23 @@ __device__ __forceinline__ uint32_t lower_axes(int k) {
 // the group's base plus its position among the group's lanes. The rank is
 // only an intermediate: the canonical within-cell order is fixed later by
 // k_sort_cells.
+// Batched systems: a point's cell is offset by its scene's cell_base, so
+// every scene owns a contiguous range of cell entries (its out-of-range bin
+// last) and one scan over all of them yields each scene's segments.
+template <bool BATCH>
 __global__ void __launch_bounds__(kThreads)
-k_insert(const __grid_constant__ DevParams P, int n, const float4 *__restrict__ pos,
+k_insert(const __grid_constant__ DevParams P0, const SceneTab T, int n, const float4 *__restrict__ pos,
          uint32_t *__restrict__ cell_out, uint32_t *__restrict__ rank_out,
          uint32_t *__restrict__ gcell_out, uint32_t *__restrict__ cnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < n;
     uint32_t cell = 0;
     if (valid) {
-        cell = cell_of(P, pos[i]);
+        const DevParams &P = BATCH ? T.params[T.point_scene[i]] : P0;
+        const uint32_t local = cell_of(P, pos[i]);
+        cell = (uint32_t)P.cell_base + local;
         cell_out[i] = cell;
-        if (gcell_out) gcell_out[i] = (cell == (uint32_t)P.ncells) ? kUndef : cell;
+        if (gcell_out) gcell_out[i] = (local == (uint32_t)P.ncells) ? kUndef : cell;
     }
     const unsigned active = __ballot_sync(0xffffffffu, valid);
     if (!valid) return;
@@ -180,28 +186,39 @@ struct SortArgs {
     float4 *pos_out, *vel_out, *veval_out;
     uint32_t *clr_out, *gcell_out, *gndx_out;
     uint32_t *upbits;                  // mode 1 with pruning: per-slot upper-band flags
-    int ncells;
+    int gcells;                        // internal cell entries (all scenes, bins included)
     int prune;
-    DevParams P;
+    SceneTab T;
+    DevParams P;                       // single-scene parameters
+};
+
+// The cell a sorting warp owns: its scene's parameters, its entry index
+// (global), its index within the scene's grid, and whether it is the
+// scene's out-of-range bin.
+struct CellCtx {
+    const DevParams *P;
+    int c, local;
+    bool overflow;
 };
 
 // Writes slot o+k of cell c from pre-sort point i; returns the band code
 // (mode 1 with pruning) so the caller can build the cell's masks.
 template <int MODE>
-__device__ __forceinline__ uint32_t emit_slot(const SortArgs &a, int c, uint32_t o, uint32_t k, uint32_t i) {
+__device__ __forceinline__ uint32_t emit_slot(const SortArgs &a, const CellCtx &cx, uint32_t o, uint32_t k,
+                                              uint32_t i) {
     if (MODE == 0) {
         a.gndx_pre[i] = k;
         return 0u;
     } else {
         const uint32_t s = o + k;
         float4 p = a.pos_in[i];
-        const uint32_t code = a.prune ? band_code(a.P, c, p) : 0u;
+        const uint32_t code = a.prune ? band_code(*cx.P, cx.local, p) : 0u;
         p.w = __uint_as_float(code);
         a.pos_out[s] = p;
         a.vel_out[s] = a.vel_in[i];
         a.veval_out[s] = a.veval_in[i];
         a.clr_out[s] = a.clr_in[i];
-        a.gcell_out[s] = (c == a.ncells) ? kUndef : (uint32_t)c;
+        a.gcell_out[s] = cx.overflow ? kUndef : (uint32_t)cx.c;
         a.gndx_out[s] = k;
         return code;
     }
@@ -209,19 +226,19 @@ __device__ __forceinline__ uint32_t emit_slot(const SortArgs &a, int c, uint32_t
 
 // Emit slots o .. o+m-1 of cell c from the sorted src (all lanes call).
 template <int MODE>
-__device__ __forceinline__ void emit_range(const SortArgs &a, int c, uint32_t o, uint32_t m) {
+__device__ __forceinline__ void emit_range(const SortArgs &a, const CellCtx &cx, uint32_t o, uint32_t m) {
     const unsigned lane = lane_id();
     for (uint32_t kb = 0; kb < m; kb += 32) {
         const uint32_t k = kb + lane;
         const bool valid = k < m;
         uint32_t code = 0;
-        if (valid) code = emit_slot<MODE>(a, c, o, k, a.src[o + k]);
-        if (MODE == 1 && a.prune) publish_upbits(a.P, a.upbits, o + kb, code, valid);
+        if (valid) code = emit_slot<MODE>(a, cx, o, k, a.src[o + k]);
+        if (MODE == 1 && a.prune) publish_upbits(*cx.P, a.upbits, o + kb, code, valid);
     }
 }
 
 template <int MODE, int K>
-__device__ __forceinline__ void sort_segment(const SortArgs &a, int c, uint32_t o, uint32_t m) {
+__device__ __forceinline__ void sort_segment(const SortArgs &a, const CellCtx &cx, uint32_t o, uint32_t m) {
     const unsigned lane = lane_id();
     uint32_t v[K];
 #pragma unroll
@@ -234,9 +251,9 @@ __device__ __forceinline__ void sort_segment(const SortArgs &a, int c, uint32_t 
         uint32_t code = 0;
         if (lane < m) {
             if (MODE == 0) a.src[o + lane] = v[0];
-            code = emit_slot<MODE>(a, c, o, lane, v[0]);
+            code = emit_slot<MODE>(a, cx, o, lane, v[0]);
         }
-        if (MODE == 1 && a.prune) publish_upbits(a.P, a.upbits, o, code, lane < m);
+        if (MODE == 1 && a.prune) publish_upbits(*cx.P, a.upbits, o, code, lane < m);
     } else {
 #pragma unroll
         for (int r = 0; r < K; r++) {
@@ -244,7 +261,7 @@ __device__ __forceinline__ void sort_segment(const SortArgs &a, int c, uint32_t 
             if (e < m) a.src[o + e] = v[r];
         }
         __syncwarp();
-        emit_range<MODE>(a, c, o, m);
+        emit_range<MODE>(a, cx, o, m);
     }
 }
 
@@ -262,7 +279,7 @@ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t *a, uint32_t 
 }
 
 template <int MODE>
-__device__ void sort_segment_dense(const SortArgs &a, int c, uint32_t o, uint32_t m) {
+__device__ void sort_segment_dense(const SortArgs &a, const CellCtx &cx, uint32_t o, uint32_t m) {
     const unsigned lane = lane_id();
     constexpr uint32_t kChunk = 128;
     for (uint32_t cb = 0; cb < m; cb += kChunk) {
@@ -295,34 +312,48 @@ __device__ void sort_segment_dense(const SortArgs &a, int c, uint32_t o, uint32_
     __syncwarp();
     for (uint32_t k = lane; k < m; k += 32) a.src[o + k] = a.scratch[o + k];
     __syncwarp();
-    emit_range<MODE>(a, c, o, m);
+    emit_range<MODE>(a, cx, o, m);
 }
 
-template <int MODE>
+template <bool BATCH>
+__device__ __forceinline__ CellCtx cell_ctx(const DevParams &P0, const SceneTab &T, int c) {
+    CellCtx cx;
+    cx.P = BATCH ? &T.params[T.cell_scene[c]] : &P0;
+    cx.c = c;
+    cx.local = c - cx.P->cell_base;
+    cx.overflow = cx.local == cx.P->ncells;
+    return cx;
+}
+
+template <int MODE, bool BATCH>
 __global__ void __launch_bounds__(kThreads)
 k_sort_cells(const __grid_constant__ SortArgs a) {
     const int c = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
-    if (c > a.ncells) return;
+    if (c >= a.gcells) return;
     const uint32_t m = a.cnt[c];
     if (m == 0) return;
     const uint32_t o = a.off[c];
-    if (m <= 32) sort_segment<MODE, 1>(a, c, o, m);
-    else if (m <= 64) sort_segment<MODE, 2>(a, c, o, m);
-    else if (m <= 128) sort_segment<MODE, 4>(a, c, o, m);
-    else sort_segment_dense<MODE>(a, c, o, m);
+    const CellCtx cx = cell_ctx<BATCH>(a.P, a.T, c);
+    if (m <= 32) sort_segment<MODE, 1>(a, cx, o, m);
+    else if (m <= 64) sort_segment<MODE, 2>(a, cx, o, m);
+    else if (m <= 128) sort_segment<MODE, 4>(a, cx, o, m);
+    else sort_segment_dense<MODE>(a, cx, o, m);
 }
 
 // Band codes and upper-band slot flags for an already sorted grid
 // (phase-API path, after k_gather_all): warp per cell, codes into pos.w.
+template <bool BATCH>
 __global__ void __launch_bounds__(kThreads)
-k_band_codes(const __grid_constant__ DevParams P, const uint32_t *__restrict__ off,
-             const uint32_t *__restrict__ cnt, float4 *__restrict__ pos,
-             uint32_t *__restrict__ upbits) {
+k_band_codes(const __grid_constant__ DevParams P0, const SceneTab T, int gcells,
+             const uint32_t *__restrict__ off, const uint32_t *__restrict__ cnt,
+             float4 *__restrict__ pos, uint32_t *__restrict__ upbits) {
     const int c = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
-    if (c >= P.ncells) return;
+    if (c >= gcells) return;
     const uint32_t m = cnt[c];
     if (m == 0) return;
     const uint32_t o = off[c];
+    const CellCtx cx = cell_ctx<BATCH>(P0, T, c);
+    const DevParams &P = *cx.P;
     const unsigned lane = lane_id();
     for (uint32_t kb = 0; kb < m; kb += 32) {
         const uint32_t k = kb + lane;
@@ -330,7 +361,7 @@ k_band_codes(const __grid_constant__ DevParams P, const uint32_t *__restrict__ o
         uint32_t code = 0;
         if (valid) {
             float4 p = pos[o + k];
-            code = band_code(P, c, p);
+            code = band_code(P, cx.local, p);
             p.w = __uint_as_float(code);
             pos[o + k] = p;
         }
@@ -442,14 +473,15 @@ __device__ __forceinline__ size_t list_at(const DevParams &P, int i, uint32_t t)
 // identity after a full sort (cu:83), so neighbour slots are read directly.
 // With LIST the slots of the pairs that pass 0 < d^2 < rd2 are recorded, in
 // visiting order, for the force pass (same positions, same test).
-template <bool PRUNE, bool LIST>
+template <bool PRUNE, bool LIST, bool BATCH>
 __global__ void __launch_bounds__(kThreads)
-k_density(const __grid_constant__ DevParams P, int n, const float4 *__restrict__ pos,
+k_density(const __grid_constant__ DevParams P0, const SceneTab T, int n, const float4 *__restrict__ pos,
           const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ off,
           const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
           float *__restrict__ press, uint32_t *__restrict__ hitlist, uint32_t *__restrict__ hitcnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const DevParams &P = BATCH ? T.params[T.point_scene[i]] : P0;
     const uint32_t gc = gcell[i];
     if (gc == kUndef) {
         press[i] = 0.0f;
@@ -595,15 +627,16 @@ __device__ __forceinline__ float3 force_of(const DevParams &P, int i, bool activ
     return fp.f;
 }
 
-template <bool PRUNE, bool LIST>
+template <bool PRUNE, bool LIST, bool BATCH>
 __global__ void __launch_bounds__(kForceThreads)
-k_force(const __grid_constant__ DevParams P, int n, const float4 *__restrict__ pos,
+k_force(const __grid_constant__ DevParams P0, const SceneTab T, int n, const float4 *__restrict__ pos,
         const float4 *__restrict__ veval, const float *__restrict__ press,
         const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ off,
         const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
         const uint32_t *__restrict__ hitlist, const uint32_t *__restrict__ hitcnt,
         float4 *__restrict__ force) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const DevParams &P = (BATCH && i < n) ? T.params[T.point_scene[i]] : P0;
     const uint32_t gc = (i < n) ? gcell[i] : kUndef;
     const bool active = gc != kUndef;
     const float3 f = force_of<PRUNE, LIST>(P, i, active, gc, pos, veval, press, off, cnt, upbits,
@@ -693,12 +726,15 @@ __device__ __forceinline__ float3 xyz(float4 v) { return make_float3(v.x, v.y, v
 __device__ __forceinline__ float4 f4(float3 v) { return make_float4(v.x, v.y, v.z, 0.0f); }
 
 // advanceParticles (fluids4.0/fluid_kernels.cu:332-420), in place.
+template <bool BATCH>
 __global__ void __launch_bounds__(kThreads)
-k_advance(const __grid_constant__ DevParams P, int n, float time, float dt, float ss,
+k_advance(const __grid_constant__ DevParams P0, const SceneTab T, int n, float time, float dt, float ss,
           const uint32_t *__restrict__ gcell, const float4 *__restrict__ force,
           float4 *__restrict__ pos, float4 *__restrict__ vel, float4 *__restrict__ veval) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const DevParams &P = BATCH ? T.params[T.point_scene[i]] : P0;
+    if (BATCH) ss = P.sim_scale;   // each scene advances with its own scale
     if (gcell[i] == kUndef) {
         pos[i] = make_float4(-1000.f, -1000.f, -1000.f, 0.f);
         vel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -714,9 +750,10 @@ k_advance(const __grid_constant__ DevParams P, int n, float time, float dt, floa
 // Force then advance for one point: the last two phases of Run fused.
 // Neighbour reads come from pos_in/veval_in; the new position and evaluated
 // velocity go to the other copies, velocity and force are updated in place.
-template <bool PRUNE, bool LIST>
+template <bool PRUNE, bool LIST, bool BATCH>
 __global__ void __launch_bounds__(kForceThreads)
-k_force_advance(const __grid_constant__ DevParams P, int n, float *time_dev, int slot, float dt,
+k_force_advance(const __grid_constant__ DevParams P0, const SceneTab T, int n, float *time_dev, int slot,
+                float dt,
                 const float4 *__restrict__ pos_in, const float4 *__restrict__ veval_in,
                 const float *__restrict__ press, const uint32_t *__restrict__ gcell,
                 const uint32_t *__restrict__ off, const uint32_t *__restrict__ cnt,
@@ -728,6 +765,7 @@ k_force_advance(const __grid_constant__ DevParams P, int n, float *time_dev, int
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const float time = time_dev[slot];
     if (i == 0) time_dev[slot ^ 1] = time + dt;
+    const DevParams &P = (BATCH && i < n) ? T.params[T.point_scene[i]] : P0;
     const uint32_t gc = (i < n) ? gcell[i] : kUndef;
     const bool active = gc != kUndef;
     const float3 f = force_of<PRUNE, LIST>(P, i, active, gc, pos_in, veval_in, press, off, cnt, upbits,
@@ -763,25 +801,38 @@ __global__ void k_unpack3(int n, const float *__restrict__ src, float4 *__restri
     dst[i] = make_float4(src[3 * i + 0], src[3 * i + 1], src[3 * i + 2], 0.0f);
 }
 
-__global__ void k_grid_identity(int n, int n_in, uint32_t *__restrict__ dst) {
+// FGCELL readback of a batched system: internal cell entries count one
+// out-of-range bin per earlier scene; the reference layout does not.
+__global__ void k_gcell_ref(int n, const uint32_t *__restrict__ gcell, const uint16_t *__restrict__ scene,
+                            uint32_t *__restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    dst[i] = (i < n_in) ? (uint32_t)i : kUndef;
+    const uint32_t g = gcell[i];
+    out[i] = (g == kUndef) ? kUndef : g - (uint32_t)scene[i];
+}
+
+__global__ void k_grid_identity(int n, const uint32_t *__restrict__ gcell, uint32_t *__restrict__ dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    dst[i] = gcell ? ((gcell[i] != kUndef) ? (uint32_t)i : kUndef) : kUndef;
 }
 
 // IntegrityCheck (fluids4.0/fluid_system.cpp:2426-2453): every sorted slot of
 // cell g must carry gcell == g and gndx == its rank; tail slots must be UNDEF.
-__global__ void k_integrity(int ncells, int n, const uint32_t *__restrict__ off,
-                            const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ gcell,
-                            const uint32_t *__restrict__ gndx, unsigned long long *bad) {
+template <bool BATCH>
+__global__ void k_integrity(const __grid_constant__ DevParams P0, const SceneTab T, int gcells, int n,
+                            const uint32_t *__restrict__ off, const uint32_t *__restrict__ cnt,
+                            const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ gndx,
+                            unsigned long long *bad) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g > ncells) return;
+    if (g >= gcells) return;
+    const CellCtx cx = cell_ctx<BATCH>(P0, T, g);
     const uint32_t o = off[g], m = cnt[g];
     unsigned long long b = 0;
     for (uint32_t k = 0; k < m; k++) {
         const uint32_t s = o + k;
         if (s >= (uint32_t)n) { b++; continue; }
-        const uint32_t want = (g == ncells) ? kUndef : (uint32_t)g;
+        const uint32_t want = cx.overflow ? kUndef : (uint32_t)g;
         if (gcell[s] != want || gndx[s] != k) b++;
     }
     if (b) atomicAdd(bad, b);
@@ -801,10 +852,20 @@ inline int blocks_for(long long n, int threads) { return (int)((n + threads - 1)
             return fl_fail(FL_ERR_CUDA, "%s launch: %s", name, cudaGetErrorString(_e)); \
     } while (0)
 
+static SceneTab scene_tab(const fl_system *s) {
+    SceneTab t;
+    t.params = s->batched ? s->d_scenes : nullptr;
+    t.point_scene = s->point_scene;
+    t.cell_scene = s->cell_scene;
+    return t;
+}
+
 int fl_launch_insert(fl_system *s, uint32_t *gcell_pre_or_null) {
     if (s->n == 0) return FL_OK;
-    k_insert<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(
-        s->D, s->n, s->f[F_POS].cur<float4>(), s->cell_pre, s->rank_tmp, gcell_pre_or_null, s->cnt);
+    auto kern = s->batched ? k_insert<true> : k_insert<false>;
+    kern<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(
+        s->D, scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->cell_pre, s->rank_tmp, gcell_pre_or_null,
+        s->cnt);
     FL_LAUNCH_CHECK("insert");
     return FL_OK;
 }
@@ -820,15 +881,17 @@ int fl_launch_scatter_index(fl_system *s) {
 int fl_launch_sort_cells(fl_system *s, int mode) {
     SortArgs a = {};
     a.off = s->off; a.cnt = s->cnt; a.src = s->src; a.scratch = s->rank_tmp;
-    a.ncells = s->ncells;
+    a.gcells = s->gcells;
     a.P = s->D;
+    a.T = scene_tab(s);
     a.prune = (mode == 1) ? s->D.prune : 0;
     a.upbits = s->upbits;
     const int warps_per_block = kThreads / 32;
-    const int grid = blocks_for((long long)s->ncells + 1, warps_per_block);
+    const int grid = blocks_for((long long)s->gcells, warps_per_block);
     if (mode == 0) {
         a.gndx_pre = s->f[F_GNDX].cur<uint32_t>();
-        k_sort_cells<0><<<grid, kThreads, 0, s->stream>>>(a);
+        auto kern = s->batched ? k_sort_cells<0, true> : k_sort_cells<0, false>;
+        kern<<<grid, kThreads, 0, s->stream>>>(a);
     } else {
         a.pos_in = s->f[F_POS].cur<float4>(); a.pos_out = s->f[F_POS].nxt<float4>();
         a.vel_in = s->f[F_VEL].cur<float4>(); a.vel_out = s->f[F_VEL].nxt<float4>();
@@ -837,7 +900,8 @@ int fl_launch_sort_cells(fl_system *s, int mode) {
         a.gcell_out = s->f[F_GCELL].nxt<uint32_t>();
         a.gndx_out = s->f[F_GNDX].nxt<uint32_t>();
         if (a.prune) FL_CUDA_TRY(cudaMemsetAsync(s->upbits, 0, fl_upbits_bytes(s), s->stream));
-        k_sort_cells<1><<<grid, kThreads, 0, s->stream>>>(a);
+        auto kern = s->batched ? k_sort_cells<1, true> : k_sort_cells<1, false>;
+        kern<<<grid, kThreads, 0, s->stream>>>(a);
         s->codes_valid = s->D.prune;
     }
     FL_LAUNCH_CHECK("sort_cells");
@@ -860,47 +924,55 @@ int fl_launch_gather_all(fl_system *s) {
 
 size_t fl_upbits_bytes(const fl_system *s) { return 3 * sizeof(uint32_t) * (size_t)s->D.upwords; }
 
-// Pruned neighbour passes need gridSrch == 2 and band codes that match the
-// live positions (set by the fused sort or fl_launch_band_codes).
+// Pruned neighbour passes need gridSrch == 2 (every scene of a batch) and
+// band codes that match the live positions (set by the fused sort or
+// fl_launch_band_codes).
 static bool use_prune(const fl_system *s) { return s->D.prune && s->codes_valid; }
 
 int fl_launch_band_codes(fl_system *s) {
     if (!s->D.prune) { s->codes_valid = 0; return FL_OK; }
-    const int grid = blocks_for((long long)s->ncells, kThreads / 32);
+    const int grid = blocks_for((long long)s->gcells, kThreads / 32);
     FL_CUDA_TRY(cudaMemsetAsync(s->upbits, 0, fl_upbits_bytes(s), s->stream));
-    k_band_codes<<<grid, kThreads, 0, s->stream>>>(s->D, s->off, s->cnt, s->f[F_POS].cur<float4>(),
-                                                     s->upbits);
+    auto kern = s->batched ? k_band_codes<true> : k_band_codes<false>;
+    kern<<<grid, kThreads, 0, s->stream>>>(s->D, scene_tab(s), s->gcells, s->off, s->cnt,
+                                          s->f[F_POS].cur<float4>(), s->upbits);
     FL_LAUNCH_CHECK("band_codes");
     s->codes_valid = 1;
     return FL_OK;
 }
 
+template <bool BATCH>
+static auto density_kernel(bool prune) {
+    return prune ? k_density<true, true, BATCH> : k_density<false, true, BATCH>;
+}
+
 int fl_launch_density(fl_system *s) {
     if (s->n == 0) return FL_OK;
-    auto kern = use_prune(s) ? k_density<true, true> : k_density<false, true>;
+    auto kern = s->batched ? density_kernel<true>(use_prune(s)) : density_kernel<false>(use_prune(s));
     kern<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(
-        s->D, s->n, s->f[F_POS].cur<float4>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt,
+        s->D, scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt,
         s->upbits, s->f[F_PRESS].cur<float>(), s->hitlist, s->hitcnt);
     FL_LAUNCH_CHECK("density");
     s->lists_valid = 1;
     return FL_OK;
 }
 
-template <bool LIST>
-static void force_kernels(bool prune, decltype(&k_force<true, true>) *kf,
-                          decltype(&k_force_advance<true, true>) *kfa) {
-    *kf = prune ? k_force<true, LIST> : k_force<false, LIST>;
-    *kfa = prune ? k_force_advance<true, LIST> : k_force_advance<false, LIST>;
+template <bool LIST, bool BATCH>
+static auto force_kernel(bool prune) {
+    return prune ? k_force<true, LIST, BATCH> : k_force<false, LIST, BATCH>;
+}
+template <bool LIST, bool BATCH>
+static auto force_advance_kernel(bool prune) {
+    return prune ? k_force_advance<true, LIST, BATCH> : k_force_advance<false, LIST, BATCH>;
 }
 
 int fl_launch_force(fl_system *s) {
     if (s->n == 0) return FL_OK;
-    decltype(&k_force<true, true>) kf;
-    decltype(&k_force_advance<true, true>) kfa;
-    if (s->lists_valid) force_kernels<true>(use_prune(s), &kf, &kfa);
-    else force_kernels<false>(use_prune(s), &kf, &kfa);
-    kf<<<blocks_for(s->n, kForceThreads), kForceThreads, 0, s->stream>>>(
-        s->D, s->n, s->f[F_POS].cur<float4>(), s->f[F_VEVAL].cur<float4>(),
+    const bool pr = use_prune(s);
+    auto kern = s->lists_valid ? (s->batched ? force_kernel<true, true>(pr) : force_kernel<true, false>(pr))
+                               : (s->batched ? force_kernel<false, true>(pr) : force_kernel<false, false>(pr));
+    kern<<<blocks_for(s->n, kForceThreads), kForceThreads, 0, s->stream>>>(
+        s->D, scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->f[F_VEVAL].cur<float4>(),
         s->f[F_PRESS].cur<float>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt, s->upbits,
         s->hitlist, s->hitcnt, s->f[F_FORCE].cur<float4>());
     FL_LAUNCH_CHECK("force");
@@ -908,14 +980,14 @@ int fl_launch_force(fl_system *s) {
 }
 
 int fl_launch_force_advance(fl_system *s, float dt) {
-    decltype(&k_force<true, true>) kf;
-    decltype(&k_force_advance<true, true>) kfa;
-    if (s->lists_valid) force_kernels<true>(use_prune(s), &kf, &kfa);
-    else force_kernels<false>(use_prune(s), &kf, &kfa);
-    kfa<<<blocks_for(s->n > 0 ? s->n : 1, kForceThreads), kForceThreads, 0, s->stream>>>(
-        s->D, s->n, s->time_dev, s->time_slot, dt, s->f[F_POS].cur<float4>(), s->f[F_VEVAL].cur<float4>(),
-        s->f[F_PRESS].cur<float>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt, s->upbits,
-        s->hitlist, s->hitcnt,
+    const bool pr = use_prune(s);
+    auto kern = s->lists_valid
+                    ? (s->batched ? force_advance_kernel<true, true>(pr) : force_advance_kernel<true, false>(pr))
+                    : (s->batched ? force_advance_kernel<false, true>(pr) : force_advance_kernel<false, false>(pr));
+    kern<<<blocks_for(s->n > 0 ? s->n : 1, kForceThreads), kForceThreads, 0, s->stream>>>(
+        s->D, scene_tab(s), s->n, s->time_dev, s->time_slot, dt, s->f[F_POS].cur<float4>(),
+        s->f[F_VEVAL].cur<float4>(), s->f[F_PRESS].cur<float>(), s->f[F_GCELL].cur<uint32_t>(), s->off,
+        s->cnt, s->upbits, s->hitlist, s->hitcnt,
         s->f[F_VEL].cur<float4>(), s->f[F_FORCE].cur<float4>(),
         s->f[F_POS].nxt<float4>(), s->f[F_VEVAL].nxt<float4>(), s->dev_err);
     FL_LAUNCH_CHECK("force_advance");
@@ -924,8 +996,9 @@ int fl_launch_force_advance(fl_system *s, float dt) {
 
 int fl_launch_advance(fl_system *s, float time, float dt, float ss) {
     if (s->n == 0) return FL_OK;
-    k_advance<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(
-        s->D, s->n, time, dt, ss, s->f[F_GCELL].cur<uint32_t>(), s->f[F_FORCE].cur<float4>(),
+    auto kern = s->batched ? k_advance<true> : k_advance<false>;
+    kern<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(
+        s->D, scene_tab(s), s->n, time, dt, ss, s->f[F_GCELL].cur<uint32_t>(), s->f[F_FORCE].cur<float4>(),
         s->f[F_POS].cur<float4>(), s->f[F_VEL].cur<float4>(), s->f[F_VEVAL].cur<float4>());
     FL_LAUNCH_CHECK("advance");
     return FL_OK;
@@ -945,16 +1018,27 @@ int fl_launch_unpack3(fl_system *s, const float *src, float4 *dst, int n) {
     return FL_OK;
 }
 
-int fl_launch_grid_identity(fl_system *s, uint32_t *dst, int n, int n_in) {
+int fl_launch_gcell_ref(fl_system *s, uint32_t *dst) {
+    if (s->n == 0) return FL_OK;
+    k_gcell_ref<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(s->n, s->f[F_GCELL].cur<uint32_t>(),
+                                                                         s->point_scene, dst);
+    FL_LAUNCH_CHECK("gcell_ref");
+    return FL_OK;
+}
+
+// FGRID readback: the identity on in-range sorted slots, GRID_UNDEF elsewhere
+// (gcell null: no sort yet, everything UNDEF).
+int fl_launch_grid_identity(fl_system *s, uint32_t *dst, int n, const uint32_t *gcell) {
     if (n == 0) return FL_OK;
-    k_grid_identity<<<blocks_for(n, kThreads), kThreads, 0, s->stream>>>(n, n_in, dst);
+    k_grid_identity<<<blocks_for(n, kThreads), kThreads, 0, s->stream>>>(n, gcell, dst);
     FL_LAUNCH_CHECK("grid_identity");
     return FL_OK;
 }
 
 int fl_launch_integrity(fl_system *s, unsigned long long *bad_dev) {
-    k_integrity<<<blocks_for((long long)s->ncells + 1, kThreads), kThreads, 0, s->stream>>>(
-        s->ncells, s->n, s->off, s->cnt, s->f[F_GCELL].cur<uint32_t>(),
+    auto kern = s->batched ? k_integrity<true> : k_integrity<false>;
+    kern<<<blocks_for((long long)s->gcells, kThreads), kThreads, 0, s->stream>>>(
+        s->D, scene_tab(s), s->gcells, s->n, s->off, s->cnt, s->f[F_GCELL].cur<uint32_t>(),
         s->f[F_GNDX].cur<uint32_t>(), bad_dev);
     FL_LAUNCH_CHECK("integrity");
     return FL_OK;

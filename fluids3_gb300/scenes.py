@@ -11,6 +11,9 @@ Workloads:
   dam_break      32,768 points, 32^3 lattice, box (-30,0,-30)..(30,60,30)
   wave_tank      4,000,000 points filling the low-x 40% of a ~330-unit box,
                  X- wall forcing at frequency 0.2, amplitude 0.3
+  batch_scenes   256 independent scenes, 2,048..65,536 points each
+                 (log-uniform), each a block filling 20..60% of its own box,
+                 with its own viscosity (0.1..0.5) and rest density (500..700)
 """
 from __future__ import annotations
 
@@ -146,3 +149,46 @@ def wave_tank(n: int = 4_000_000, seed: int = 2, steps: int = 1000,
     params = make_params(bmin, bmax, bound_wall_force=wall_force, bound_wall_freq=wall_freq)
     pos = lattice_block(n, (margin, margin, margin), cnt_x, cnt_z, s, seed)
     return _finish("wave_tank_4m" if n == 4_000_000 else f"wave_tank_{n}", params, pos, steps, bmin, bmax)
+
+
+def _draws(seed: int, stream: int, n: int) -> np.ndarray:
+    return uniform01(seed, 100 + stream, n).astype(np.float64)
+
+
+def block_scene(n: int, fill: float, seed: int, name: str, steps: int = 100, **overrides) -> Scene:
+    """A dam-break block of n points filling the low-x fraction `fill` of a
+    cubic box scaled to hold it (block spans the box's full y and z)."""
+    s = lattice_spacing()
+    margin = 4.0
+    edge = float(s) * (n / fill) ** (1.0 / 3.0)
+    cnt_z = max(1, int((edge - 2 * margin) / float(s)))
+    cnt_x = max(1, int(round(fill * edge / float(s))))
+    layers = -(-n // (cnt_x * cnt_z))
+    lx = (cnt_x * float(s) + 2 * margin) / fill
+    lz = cnt_z * float(s) + 2 * margin
+    ly = max(layers * float(s) + 2 * margin, lz)
+    bmin, bmax = (0.0, 0.0, 0.0), (round(lx, 1), round(ly, 1), round(lz, 1))
+    params = make_params(bmin, bmax, **overrides)
+    pos = lattice_block(n, (margin, margin, margin), cnt_x, cnt_z, s, seed)
+    return _finish(name, params, pos, steps, bmin, bmax)
+
+
+def batch_scenes(nscenes: int = 256, seed: int = 3, nmin: int = 2048, nmax: int = 65536,
+                 steps: int = 500) -> list[Scene]:
+    """Scenes of uneven sizes: point counts log-uniform in [nmin, nmax], fill
+    fraction U[0.2, 0.6], viscosity U[0.1, 0.5], rest density U[500, 700];
+    the other parameters are the dam-break set."""
+    u = [_draws(seed, k, nscenes) for k in range(4)]
+    out = []
+    for k in range(nscenes):
+        n = int(round(np.exp(np.log(nmin) + u[0][k] * (np.log(nmax) - np.log(nmin)))))
+        fill = 0.2 + 0.4 * u[1][k]
+        visc = float(np.float32(0.1 + 0.4 * u[2][k]))
+        rest = float(np.float32(500.0 + 200.0 * u[3][k]))
+        out.append(block_scene(n, fill, seed * 1000 + k, f"scene_{k}", steps, pvisc=visc, prest_dens=rest))
+    return out
+
+
+def concat(scenes: list) -> dict:
+    """The scenes' arrays concatenated in scene order (the batched layout)."""
+    return {k: np.concatenate([getattr(sc, k) for sc in scenes]) for k in ("pos", "vel", "veval", "clr")}

@@ -81,6 +81,28 @@ class FluidSystem:
         call("fl_create", C.byref(params), int(max_points), C.byref(self._h))
         self.max_points = int(max_points)
 
+    @classmethod
+    def batch(cls, params: list, counts: list) -> "FluidSystem":
+        """Many scenes stepped together (fl_batch_create): params[k] derived,
+        counts[k] points of scene k; points are passed and read back as all
+        scenes' arrays concatenated in scene order."""
+        self = cls.__new__(cls)
+        self._h = C.c_void_p()
+        arr = (FlParams * len(params))(*params)
+        cnt = (C.c_int * len(counts))(*[int(c) for c in counts])
+        call("fl_batch_create", arr, cnt, len(params), C.byref(self._h))
+        self.max_points = int(sum(counts))
+        return self
+
+    def NumScenes(self) -> int:
+        return lib().fl_num_scenes(self._h)
+
+    def SceneInfo(self, scene: int) -> dict:
+        """point_base, n, cell_base, ncells of `scene` in the concatenated layout."""
+        v = [C.c_int() for _ in range(4)]
+        call("fl_batch_scene_info", self._h, int(scene), *[C.byref(x) for x in v])
+        return dict(point_base=v[0].value, n=v[1].value, cell_base=v[2].value, ncells=v[3].value)
+
     # -- lifetime -------------------------------------------------------------
     def close(self) -> None:
         if self._h:

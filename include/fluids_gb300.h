@@ -152,6 +152,25 @@ int fl_grid_total(const fl_system *s);
 int fl_get_time(const fl_system *s, float *t);
 int fl_set_time(fl_system *s, float t);
 
+/* ---- batched systems ------------------------------------------------------
+ * Many independent scenes -- each with its own domain, grid and parameters
+ * -- stepped together: every phase is one launch over the concatenation of
+ * all scenes' points (scene 0 first), each scene owning a contiguous range
+ * of cell entries, so one scan over all of them yields every scene's sorted
+ * segment. counts[k] points of scene k, params[k] derived; all scenes share
+ * dt (one clock). The handle works with every call above and below: buffers
+ * read back as the scenes' arrays concatenated (FGRIDCNT/FGRIDOFF: each
+ * scene's C cells in turn; FGCELL indexes that concatenated grid; FGRIDOFF
+ * holds offsets into the concatenated point order). fl_set_particles/fl_import_device take all points at once.
+ * Each scene's results are bit-identical to stepping it alone. */
+int fl_batch_create(const fl_params *params, const int *counts, int nscenes, fl_system **out);
+int fl_num_scenes(const fl_system *s);
+/* Where scene `scene` lives: first point and point count in the
+ * concatenated point order, first cell and cell count in the concatenated
+ * reference-layout grid. A single-scene system is scene 0. */
+int fl_batch_scene_info(const fl_system *s, int scene, int *point_base, int *n, int *cell_base,
+                        int *ncells);
+
 /* ---- data movement (fluid.h host layout: float3 packed 12 B, uint 4 B) --- */
 
 /* TransferToCUDA (cpp:2312-2321): n points from host SoA arrays. pos is
