@@ -53,7 +53,7 @@ void fl_make_dev_params(const fl_params &p, DevParams *d) {
     d->rd2 = p.rd2; d->d2 = p.d2; d->pmass = p.pmass; d->poly6kern = p.poly6kern;
     d->psmoothradius = p.psmoothradius; d->prest_dens = p.prest_dens;
     d->pintstiff = p.pintstiff; d->sim_scale = p.sim_scale;
-    d->spikykern = p.spikykern; d->vterm = p.vterm;
+    d->spikykern = p.spikykern; d->vterm = p.vterm; d->lapkern = p.lapkern;
     d->pradius = p.pradius; d->bound_slope = p.bound_slope; d->bound_stiff = p.bound_stiff;
     d->bound_damp = p.bound_damp; d->bound_friction = p.bound_friction;
     d->bound_wall_force = p.bound_wall_force; d->bound_wall_freq = p.bound_wall_freq;
@@ -85,7 +85,7 @@ static int check_derived(const fl_params *p) {
 // ---------------------------------------------------------------------------
 // allocation
 
-static int dalloc(void **p, size_t bytes) {
+int fl_dalloc(void **p, size_t bytes) {
     *p = nullptr;
     if (bytes == 0) bytes = 16;
     cudaError_t e = cudaMalloc(p, bytes);
@@ -118,8 +118,8 @@ static int alloc_grid(fl_system *s) {
     s->scan_tiles = (int)((entries + tile - 1) / tile);
     s->grid_pad = (size_t)s->scan_tiles * tile;
     void *blk = nullptr, *off = nullptr;
-    FL_TRY(dalloc(&blk, grid_block_bytes(s)));
-    int r = dalloc(&off, s->grid_pad * sizeof(uint32_t));
+    FL_TRY(fl_dalloc(&blk, grid_block_bytes(s)));
+    int r = fl_dalloc(&off, s->grid_pad * sizeof(uint32_t));
     if (r != FL_OK) { cudaFree(blk); return r; }
     s->cnt = (uint32_t *)blk;
     s->scan_ticket = (uint32_t *)((char *)blk + s->grid_pad * sizeof(uint32_t));
@@ -140,6 +140,7 @@ static void destroy_graph(fl_system *s) {
 
 static void free_all(fl_system *s) {
     destroy_graph(s);
+    fl_tape_free(s);
     for (int k = 0; k < F_COUNT; k++)
         for (int c = 0; c < 2; c++) cudaFree(s->f[k].p[c]);
     cudaFree(s->cell_pre); cudaFree(s->rank_tmp); cudaFree(s->src); cudaFree(s->upbits);
@@ -192,19 +193,19 @@ extern "C" int fl_create(const fl_params *p, int max_points, fl_system **out) {
         const size_t esz[F_COUNT] = {16, 16, 16, 16, 4, 4, 4, 4};
         for (int k = 0; k < F_COUNT && r == FL_OK; k++) {
             s->f[k].esz = esz[k];
-            for (int c = 0; c < 2 && r == FL_OK; c++) r = dalloc(&s->f[k].p[c], esz[k] * np);
+            for (int c = 0; c < 2 && r == FL_OK; c++) r = fl_dalloc(&s->f[k].p[c], esz[k] * np);
         }
         if (r != FL_OK) break;
-        if ((r = dalloc((void **)&s->cell_pre, 4 * np)) != FL_OK) break;
-        if ((r = dalloc((void **)&s->rank_tmp, 4 * np)) != FL_OK) break;
-        if ((r = dalloc((void **)&s->src, 4 * np)) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&s->cell_pre, 4 * np)) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&s->rank_tmp, 4 * np)) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&s->src, 4 * np)) != FL_OK) break;
         s->D.upwords = (int)((np + 31) / 32 + 1);
-        if ((r = dalloc((void **)&s->upbits, fl_upbits_bytes(s))) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&s->upbits, fl_upbits_bytes(s))) != FL_OK) break;
         s->D.hcap = kPairListCap;
-        if ((r = dalloc((void **)&s->hitlist, 4 * ((np + 31) / 32) * 32 * (size_t)kPairListCap)) != FL_OK) break;
-        if ((r = dalloc((void **)&s->hitcnt, 4 * np)) != FL_OK) break;
-        if ((r = dalloc((void **)&s->dev_err, 256)) != FL_OK) break;
-        if ((r = dalloc((void **)&s->time_dev, 256)) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&s->hitlist, 4 * ((np + 31) / 32) * 32 * (size_t)kPairListCap)) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&s->hitcnt, 4 * np)) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&s->dev_err, 256)) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&s->time_dev, 256)) != FL_OK) break;
         if ((r = alloc_grid(s)) != FL_OK) break;
         if (cudaMemsetAsync(s->dev_err, 0, 256, s->stream) != cudaSuccess ||
             cudaMemsetAsync(s->time_dev, 0, 256, s->stream) != cudaSuccess) {
@@ -306,9 +307,9 @@ extern "C" int fl_batch_create(const fl_params *params, const int *counts, int n
         s->D.upwords = upwords;
         s->D.hcap = hcap;
         s->D.prune = all_prune;
-        if ((r = dalloc((void **)&s->d_scenes, sizeof(DevParams) * nscenes)) != FL_OK) break;
-        if ((r = dalloc((void **)&s->point_scene, sizeof(uint16_t) * pscene.size())) != FL_OK) break;
-        if ((r = dalloc((void **)&s->cell_scene, sizeof(uint16_t) * cscene.size())) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&s->d_scenes, sizeof(DevParams) * nscenes)) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&s->point_scene, sizeof(uint16_t) * pscene.size())) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&s->cell_scene, sizeof(uint16_t) * cscene.size())) != FL_OK) break;
         if (cudaMemcpy(s->d_scenes, tab.data(), sizeof(DevParams) * nscenes, cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemcpy(s->point_scene, pscene.data(), sizeof(uint16_t) * pscene.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemcpy(s->cell_scene, cscene.data(), sizeof(uint16_t) * cscene.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -372,7 +373,8 @@ static TimingState *detach_timing(fl_system *s) {
     return t;
 }
 
-static void reset_progress(fl_system *s) {
+void fl_reset_progress(fl_system *s) {
+    fl_tape_touch(s);
     s->have_insert = s->have_offsets = s->have_grid = 0;
     s->codes_valid = 0;
     s->lists_valid = 0;
@@ -397,7 +399,7 @@ extern "C" int fl_set_params(fl_system *s, const fl_params *p) {
     s->D.upwords = upwords;
     s->D.hcap = hcap;
     destroy_graph(s);
-    reset_progress(s);
+    fl_reset_progress(s);
     return FL_OK;
 }
 
@@ -442,12 +444,12 @@ extern "C" void *fl_stream(fl_system *s) { return s ? (void *)s->stream : nullpt
 // ---------------------------------------------------------------------------
 // data movement
 
-static int ensure_stage(fl_system *s, size_t bytes) {
+int fl_ensure_stage(fl_system *s, size_t bytes) {
     if (bytes <= s->stage_bytes) return FL_OK;
     cudaFree(s->stage);
     s->stage = nullptr;
     s->stage_bytes = 0;
-    FL_TRY(dalloc(&s->stage, bytes));
+    FL_TRY(fl_dalloc(&s->stage, bytes));
     s->stage_bytes = bytes;
     return FL_OK;
 }
@@ -483,7 +485,7 @@ extern "C" int fl_set_particles(fl_system *s, int n, const float *pos, const flo
     if (n > 0) {
         // one staging slice per float3 field, then unpack to float4 on device
         const size_t v3 = 12 * (size_t)n;
-        FL_TRY(ensure_stage(s, 4 * v3));
+        FL_TRY(fl_ensure_stage(s, 4 * v3));
         const float *src3[4] = {pos, vel, veval, force};
         const int fid[4] = {F_POS, F_VEL, F_VEVAL, F_FORCE};
         for (int k = 0; k < 4; k++) {
@@ -506,7 +508,7 @@ extern "C" int fl_set_particles(fl_system *s, int n, const float *pos, const flo
     }
     // the caller may reuse its host arrays on return
     FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
-    reset_progress(s);
+    fl_reset_progress(s);
     return FL_OK;
 }
 
@@ -567,7 +569,7 @@ extern "C" int fl_get_buffer(fl_system *s, int id, void *host, size_t bytes) {
     FL_TRY(buffer_bytes(s, id, &need));
     if (bytes < need) return fl_fail(FL_ERR_ARG, "fl_get_buffer: %zu bytes < %zu needed", bytes, need);
     if (need == 0) return FL_OK;
-    FL_TRY(ensure_stage(s, need));
+    FL_TRY(fl_ensure_stage(s, need));
     FL_TRY(export_to_device(s, id, s->stage));
     FL_CUDA_TRY(cudaMemcpyAsync(host, s->stage, need, cudaMemcpyDeviceToHost, s->stream));
     FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
@@ -609,7 +611,7 @@ extern "C" int fl_import_device(fl_system *s, int n, const void *dev_pos, const 
     else FL_CUDA_TRY(cudaMemsetAsync(s->f[F_VEL].cur<void>(), 0, 16 * (size_t)n, s->stream));
     if (dev_veval) FL_TRY(fl_launch_unpack3(s, (const float *)dev_veval, s->f[F_VEVAL].cur<float4>(), n));
     else FL_CUDA_TRY(cudaMemsetAsync(s->f[F_VEVAL].cur<void>(), 0, 16 * (size_t)n, s->stream));
-    reset_progress(s);
+    fl_reset_progress(s);
     return FL_OK;
 }
 
@@ -632,6 +634,7 @@ static int readback(fl_system *s, void *host, const void *dev, size_t bytes) {
 
 extern "C" int fl_insert_particles(fl_system *s, uint32_t *gcell, uint32_t *gndx, uint32_t *gcnt) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_insert_particles: null system");
+    fl_tape_touch(s);
     FL_TRY(clear_grid(s));
     FL_TRY(fl_launch_insert(s, s->f[F_GCELL].cur<uint32_t>()));
     // canonical gndx: offsets, arrival-order index scatter, per-cell sort
@@ -651,6 +654,7 @@ extern "C" int fl_insert_particles(fl_system *s, uint32_t *gcell, uint32_t *gndx
 
 extern "C" int fl_prefix_sum_cells(fl_system *s, uint32_t *goff, int zero_offsets) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_prefix_sum_cells: null system");
+    fl_tape_touch(s);
     if (!s->have_insert) return fl_fail(FL_ERR_STATE, "fl_prefix_sum_cells before fl_insert_particles");
     FL_TRY(fl_launch_scan(s, s->gcells, 1));
     s->have_offsets = 1;
@@ -663,6 +667,7 @@ static void flip(fl_system *s, int k) { s->f[k].live ^= 1; }
 
 extern "C" int fl_counting_sort_full(fl_system *s, float *ppos) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_counting_sort_full: null system");
+    fl_tape_touch(s);
     if (!s->have_insert || !s->have_offsets)
         return fl_fail(FL_ERR_STATE, "fl_counting_sort_full before insert and prefix sum");
     FL_TRY(fl_launch_gather_all(s));
@@ -677,18 +682,21 @@ extern "C" int fl_counting_sort_full(fl_system *s, float *ppos) {
 
 extern "C" int fl_compute_pressure(fl_system *s) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_compute_pressure: null system");
+    fl_tape_touch(s);
     if (!s->have_grid) return fl_fail(FL_ERR_STATE, "fl_compute_pressure before fl_counting_sort_full");
     return fl_launch_density(s);
 }
 
 extern "C" int fl_compute_force(fl_system *s) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_compute_force: null system");
+    fl_tape_touch(s);
     if (!s->have_grid) return fl_fail(FL_ERR_STATE, "fl_compute_force before fl_counting_sort_full");
     return fl_launch_force(s);
 }
 
 extern "C" int fl_advance(fl_system *s, float time, float dt, float ss) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_advance: null system");
+    fl_tape_touch(s);
     if (!s->have_grid) return fl_fail(FL_ERR_STATE, "fl_advance before fl_counting_sort_full");
     s->codes_valid = 0;   // positions move; their band codes and pair lists no longer hold
     s->lists_valid = 0;
@@ -707,6 +715,8 @@ static int record(fl_system *s, TimingState *t, int k) {
 static int run_step(fl_system *s, TimingState *t) {
     // InsertParticles, PrefixSumCells, CountingSortFull, ComputePressure,
     // ComputeForce + Advance (cpp:507-515) as six launches.
+    const bool taped = fl_tape_recording(s) != 0;
+    if (taped) FL_TRY(fl_tape_pre_step(s));
     FL_TRY(record(s, t, 0));
     FL_TRY(clear_grid(s));
     FL_TRY(fl_launch_insert(s, nullptr));
@@ -727,6 +737,21 @@ static int run_step(fl_system *s, TimingState *t) {
     FL_TRY(record(s, t, 6));
     s->time_slot ^= 1;
     if (t) t->steps++;
+    if (taped) FL_TRY(fl_tape_post_step(s));
+    return FL_OK;
+}
+
+int fl_step_fused(fl_system *s) { return run_step(s, nullptr); }
+
+int fl_recompute_step(fl_system *s) {
+    FL_TRY(clear_grid(s));
+    FL_TRY(fl_launch_insert(s, nullptr));
+    FL_TRY(fl_launch_scan(s, s->gcells, 0));
+    FL_TRY(fl_launch_scatter_index(s));
+    FL_TRY(fl_launch_sort_cells(s, 1));
+    flip(s, F_POS); flip(s, F_VEL); flip(s, F_VEVAL); flip(s, F_CLR); flip(s, F_GCELL); flip(s, F_GNDX);
+    FL_TRY(fl_launch_density(s));
+    FL_TRY(fl_launch_force(s));
     return FL_OK;
 }
 
@@ -794,7 +819,7 @@ static int capture_pair(fl_system *s) {
 extern "C" int fl_run_steps(fl_system *s, int nsteps) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_run_steps: null system");
     if (nsteps < 0) return fl_fail(FL_ERR_ARG, "fl_run_steps: nsteps < 0");
-    if (s->timing) {   // timed steps stay eager so each launch is bracketed
+    if (s->timing || fl_tape_recording(s)) {   // timed or taped steps stay eager (per-step hooks)
         for (int k = 0; k < nsteps; k++) FL_TRY(fl_run(s));
         return FL_OK;
     }
@@ -828,8 +853,8 @@ extern "C" int fl_checkpoint_save(fl_system *s, int slot) {
         return fl_fail(FL_ERR_ARG, "fl_checkpoint_save: slot %d outside [0, %d)", slot, FL_MAX_CHECKPOINTS);
     const size_t np = (size_t)(s->max_points > 0 ? s->max_points : 1);
     if (!s->ckpt_time[slot]) {
-        for (int k = 0; k < F_COUNT; k++) FL_TRY(dalloc(&s->ckpt[slot][k], s->f[k].esz * np));
-        FL_TRY(dalloc((void **)&s->ckpt_time[slot], 256));
+        for (int k = 0; k < F_COUNT; k++) FL_TRY(fl_dalloc(&s->ckpt[slot][k], s->f[k].esz * np));
+        FL_TRY(fl_dalloc((void **)&s->ckpt_time[slot], 256));
     }
     for (int k = 0; k < F_COUNT; k++)
         if (s->n > 0)
@@ -856,7 +881,7 @@ extern "C" int fl_checkpoint_restore(fl_system *s, int slot) {
                                 cudaMemcpyDeviceToDevice, s->stream));
     s->time = s->ckpt_host_time[slot];
     s->time_host_valid = s->ckpt_host_valid[slot];
-    reset_progress(s);
+    fl_reset_progress(s);
     return FL_OK;
 }
 
@@ -888,7 +913,7 @@ extern "C" int fl_sync(fl_system *s) {
 extern "C" int fl_integrity_check(fl_system *s, int64_t *bad) {
     if (!s || !bad) return fl_fail(FL_ERR_ARG, "fl_integrity_check: null argument");
     if (!s->have_grid) return fl_fail(FL_ERR_STATE, "fl_integrity_check needs a sorted grid");
-    FL_TRY(ensure_stage(s, 16));
+    FL_TRY(fl_ensure_stage(s, 16));
     FL_CUDA_TRY(cudaMemsetAsync(s->stage, 0, 8, s->stream));
     FL_TRY(fl_launch_integrity(s, (unsigned long long *)s->stage));
     unsigned long long v = 0;

@@ -34,6 +34,7 @@ struct DevParams {
     int nadj;            // (resZ + 1) * resX + 1: corner offset of the search block
     float rd2, d2, pmass, poly6kern;
     float psmoothradius, prest_dens, pintstiff, sim_scale, spikykern, vterm;
+    float lapkern;       // viscosity Laplacian constant (vterm = lapkern * visc); the adjoint's visc partial
     float pradius, bound_slope, bound_stiff, bound_damp, bound_friction;
     float bound_wall_force, bound_wall_freq;
     float3 bound_min, bound_max, gravity;
@@ -151,6 +152,9 @@ struct fl_system {
     float ckpt_host_time[FL_MAX_CHECKPOINTS];
     int ckpt_host_valid[FL_MAX_CHECKPOINTS];
 
+    // adjoint tape (fl_tape.cpp), null until fl_tape_begin
+    struct fl_tape *tape;
+
     // per-phase event timing (PERF_PUSH/PERF_POP of Run, cpp:507-515)
     int timing;
     cudaEvent_t ev[8];
@@ -158,7 +162,50 @@ struct fl_system {
     int phase_runs;
 };
 
-// ---- launch wrappers (fl_kernels.cu, fl_scan.cu) ---------------------------
+inline SceneTab fl_scene_tab(const fl_system *s) {
+    SceneTab t;
+    t.params = s->batched ? s->d_scenes : nullptr;
+    t.point_scene = s->point_scene;
+    t.cell_scene = s->cell_scene;
+    return t;
+}
+
+#define FL_LAUNCH_CHECK(name)                                                   \
+    do {                                                                        \
+        cudaError_t _e = cudaGetLastError();                                    \
+        if (_e != cudaSuccess)                                                  \
+            return fl_fail(FL_ERR_CUDA, "%s launch: %s", name, cudaGetErrorString(_e)); \
+    } while (0)
+
+// ---- host runtime entry points shared with the adjoint (fl_api.cpp) -------
+int fl_dalloc(void **p, size_t bytes);
+int fl_ensure_stage(fl_system *s, size_t bytes);
+void fl_reset_progress(fl_system *s);
+// One fused Run step reading the device time slot (no timing events).
+int fl_step_fused(fl_system *s);
+// The forward state of one step short of the advance: insert, scan, sort
+// (gathering pos/vel/veval/clr), density and force into the live copies.
+int fl_recompute_step(fl_system *s);
+
+// ---- adjoint tape (fl_tape.cpp) --------------------------------------------
+int fl_tape_recording(const fl_system *s);
+int fl_tape_pre_step(fl_system *s);
+int fl_tape_post_step(fl_system *s);
+// A state change outside Run (new particles, parameters, a restore, a phase
+// call): the tape no longer describes the steps that led to the state.
+void fl_tape_touch(fl_system *s);
+void fl_tape_free(fl_system *s);
+
+// ---- launch wrappers (fl_kernels.cu, fl_scan.cu, fl_adjoint.cu) ------------
+int fl_launch_adj_advance(fl_system *s, const float *time_ptr, const float4 *xo_b, const float4 *vo_b,
+                          const float4 *eo_b, float4 *xa, float4 *ea, float4 *fb, float4 *v_out);
+int fl_launch_adj_force(fl_system *s, const float4 *fb, float4 *xa, const float4 *ea, float *rb, float4 *pc,
+                        float4 *e_out);
+int fl_launch_adj_density(fl_system *s, const float *rb, const float4 *xa, float4 *x_out);
+int fl_param_chunks(int max_scene_points);
+int fl_launch_param_reduce(fl_system *s, const float4 *pc, const int *sbase, const int *sn, int nchunks,
+                           double *partial, double *acc);
+int fl_launch_compose(fl_system *s, int n, const uint32_t *src, const uint32_t *in, uint32_t *out);
 int fl_launch_insert(fl_system *s, uint32_t *gcell_pre_or_null);
 int fl_launch_scan(fl_system *s, int count, int clear_status);
 int fl_launch_scatter_index(fl_system *s);

@@ -251,6 +251,46 @@ class FluidSystem:
         call("fl_integrity_check", self._h, C.byref(bad))
         return int(bad.value)
 
+    # -- adjoint (no counterpart in the reference) ----------------------------
+    def TapeBegin(self, max_steps: int, every: int = 1) -> None:
+        """Record the Run steps that follow (up to ``max_steps``; a checkpoint of
+        the state every ``every`` steps) for Backward."""
+        call("fl_tape_begin", self._h, int(max_steps), int(every))
+
+    def TapeSteps(self) -> int:
+        return int(lib().fl_tape_steps(self._h))
+
+    def TapeOrder(self) -> np.ndarray:
+        """Per current slot, the point's index when recording began."""
+        out = np.empty(self.NumPoints(), np.uint32)
+        if out.size:
+            call("fl_tape_order", self._h, _ptr(out))
+        return out
+
+    def Backward(self, dpos=None, dvel=None, dveval=None, want_state: bool = True):
+        """Reverse pass over the recorded steps. ``d*``: dL/d(final pos, vel,
+        veval) as (N,3) arrays in the current slot order (None = zero), or device
+        pointers (int). Returns (gpos, gvel, gveval, gparams): dL/d(initial
+        state) in the order of the recording's start, and per scene
+        dL/d(pvisc, prest_dens, pintstiff) as an (nscenes, 3) float64 array."""
+        n = self.NumPoints()
+
+        def arg(a):
+            if a is None or isinstance(a, int):
+                return a
+            a = np.ascontiguousarray(a, dtype=np.float32).reshape(n, 3)
+            keep.append(a)
+            return _ptr(a)
+
+        keep: list = []
+        outs = [np.empty((n, 3), np.float32) for _ in range(3)] if want_state else [None] * 3
+        gp = np.zeros((self.NumScenes(), 3), np.float64)
+        call("fl_backward", self._h, arg(dpos), arg(dvel), arg(dveval), *[_ptr(o) for o in outs], _ptr(gp))
+        return outs[0], outs[1], outs[2], gp
+
+    def TapeEnd(self) -> None:
+        call("fl_tape_end", self._h)
+
     # -- timing ---------------------------------------------------------------
     def SetTiming(self, enable: bool) -> None:
         call("fl_set_timing", self._h, 1 if enable else 0)

@@ -262,6 +262,40 @@ int fl_time_steps(fl_system *s, int nsteps, int use_graph, int restart_every, in
                   double *ms);
 int fl_get_phase_times(fl_system *s, double ms[8], int *steps);
 
+/* ---- adjoint of the fused step -------------------------------------------
+ * No counterpart in the reference (its step has no derivative). The
+ * reverse-mode derivative of a run of fl_run / fl_run_steps steps with
+ * respect to the particle state at its start and to three parameters
+ * (pvisc, prest_dens, pintstiff), for optimisation and inverse problems
+ * over the same simulation. The integer structure of each step (cells, the
+ * sort, which pairs interact, which walls and limits act) is piecewise
+ * constant and carries no derivative.
+ *
+ * fl_tape_begin opens a tape for up to max_steps steps: every Run step
+ * from then on saves the state before it every `every` steps (48 B per
+ * point each; every > 1 trades memory for a replay of each segment during
+ * fl_backward) and its time. Changing the state outside Run while recording
+ * (fl_set_particles, fl_import_device, fl_set_params, fl_checkpoint_restore,
+ * a phase call) invalidates the tape; fl_set_time does not. A step beyond
+ * max_steps fails with FL_ERR_CAPACITY. Steps run eagerly while recording.
+ *
+ * fl_backward takes dL/d(final FPOS, FVEL, FVEVAL) in the current slot
+ * order (fluid.h float3 layout, n x 3 floats; NULL = zero) and returns
+ * dL/d(initial FPOS, FVEL, FVEVAL) in the order the points had when
+ * recording began (NULL = not wanted) and, per scene, dL/d(pvisc,
+ * prest_dens, pintstiff) as 3 doubles (gparams[3 * scene + k]; NULL = not
+ * wanted). Vector arguments may be host or device memory. The live state is
+ * left as it was, except that the phase API needs a fresh
+ * fl_insert_particles. The result is deterministic (no atomics).
+ * fl_tape_order gives, per current slot, the point's index when recording
+ * began (n uint32, host or device). fl_tape_steps: steps recorded. */
+int fl_tape_begin(fl_system *s, int max_steps, int every);
+int fl_tape_steps(const fl_system *s);
+int fl_tape_order(fl_system *s, uint32_t *order);
+int fl_backward(fl_system *s, const float *dpos, const float *dvel, const float *dveval,
+                float *gpos, float *gvel, float *gveval, double *gparams);
+int fl_tape_end(fl_system *s);
+
 /* ---- allocation-free scan ------------------------------------------------
  * No counterpart in the reference. For host applications that cannot let a
  * library allocate device memory -- an engine or plugin host that owns the

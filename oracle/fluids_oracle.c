@@ -109,6 +109,36 @@ void orc_density(const fl_params *p, int n, const float *pos, const uint32_t *gc
     }
 }
 
+/* The pairs computePressure's loop accepts (0 < d^2 < rd2), per sorted
+ * point in visiting order, as CSR: point i's neighbour slots are
+ * nbr[poff[i] .. poff[i+1]). With nbr null only poff is filled (a counting
+ * pass); the frozen structure of the FP64 adjoint model (adjoint64.c). */
+void orc_pairs(const fl_params *p, int n, const float *pos, const uint32_t *gcell,
+               const uint32_t *off, const uint32_t *cnt, uint32_t *poff, uint32_t *nbr) {
+    const int nadj = (1 * p->gridRes[2] + 1) * p->gridRes[0] + 1;
+    uint32_t k = 0;
+    for (int i = 0; i < n; i++) {
+        poff[i] = k;
+        if (gcell[i] == UNDEF) continue;
+        const int base = (int)gcell[i] - nadj;
+        const float *xi = pos + 3 * i;
+        for (int c = 0; c < p->gridAdjCnt; c++) {
+            const int cell = base + p->gridAdj[c];
+            const uint32_t j1 = off[cell] + cnt[cell];
+            for (uint32_t j = off[cell]; j < j1; j++) {
+                const float *xj = pos + 3 * j;
+                const float dx = xi[0] - xj[0], dy = xi[1] - xj[1], dz = xi[2] - xj[2];
+                const float dsq = dx * dx + dy * dy + dz * dz;
+                if (dsq < p->rd2 && dsq > 0.0f) {
+                    if (nbr) nbr[k] = j;
+                    k++;
+                }
+            }
+        }
+    }
+    poff[n] = k;
+}
+
 /* computeForce (fluids4.0/fluid_kernels.cu:180-217); the float3 operators
  * of cutil_math.h expand component-wise, and '/ s' is '* (1.0f / s)'. */
 void orc_force(const fl_params *p, int n, const float *pos, const float *veval,

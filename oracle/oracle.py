@@ -255,3 +255,115 @@ class RefKernels:
         t = C.c_float(time)
         self.lib.ref_run(self.n, steps, C.byref(t), C.c_float(self.params.dt), threads)
         return float(t.value)
+
+
+# ---------------------------------------------------------------------------
+# FP64 adjoint model (adjoint64.c): the step with its integer structure
+# frozen, evaluated in double, and its hand-written reverse pass.
+
+@dataclass
+class Frozen:
+    """The integer structure of `steps` FP32 oracle steps: per step the sort
+    permutation (slot -> pre-sort index), the in-range flags and the pairs
+    (CSR over sorted slots), the time, and the state before the step."""
+    n: int
+    steps: int
+    perm: np.ndarray     # (T, n) uint32
+    inr: np.ndarray      # (T, n) uint8
+    poff: np.ndarray     # (T, n + 1) uint32
+    pnbr: np.ndarray     # concatenated uint32
+    pbase: np.ndarray    # (T + 1,) uint64 offsets of each step's pairs in pnbr
+    time: np.ndarray     # (T,) float64
+    states: np.ndarray   # (T, 3, n, 3) float64: x, v, e before each step
+
+
+def _adj_lib():
+    lib = orc()
+    if not getattr(lib, "_adj_ready", False):
+        vp, i = C.c_void_p, C.c_int
+        lib.orc_pairs.argtypes = [vp, i, vp, vp, vp, vp, vp, vp]
+        lib.adj64_forward.argtypes = [vp, vp, i, i] + [vp] * 9
+        lib.adj64_backward.argtypes = [vp, vp, i, i] + [vp] * 14
+        lib._adj_ready = True
+    return lib
+
+
+def frozen_run(params, st: State, steps: int, time: float, states=None, times=None) -> Frozen:
+    """Run `steps` FP32 oracle steps on `st` (in place) and record their structure.
+    With `states` (per step a (pos, vel, veval) float32 triple, e.g. read back
+    from another implementation) each step starts from the given state, and
+    `times` (per step) replaces the oracle's own clock."""
+    lib = _adj_lib()
+    n = st.n
+    perm = np.zeros((steps, n), np.uint32)
+    inr = np.zeros((steps, n), np.uint8)
+    poff = np.zeros((steps, n + 1), np.uint32)
+    nbrs, times_out = [], np.zeros(steps, np.float64)
+    C_ = params.gridTotal
+    given = states
+    states = np.zeros((steps, 3, n, 3), np.float64)
+    for t in range(steps):
+        if given is not None:
+            st.pos, st.vel, st.veval = (np.array(a, np.float32).reshape(n, 3) for a in given[t])
+        if times is not None:
+            time = float(times[t])
+        states[t, 0], states[t, 1], states[t, 2] = st.pos, st.vel, st.veval
+        times_out[t] = time
+        insert(params, st)
+        prefix_sum(params, st)
+        cell = np.where(st.gcell == 0xFFFFFFFF, C_, st.gcell).astype(np.int64)
+        slot = st.off[cell].astype(np.int64) + st.gndx
+        perm[t, slot] = np.arange(n, dtype=np.uint32)
+        counting_sort(params, st)
+        inr[t] = (st.gcell != 0xFFFFFFFF)
+        lib.orc_pairs(C.byref(params), n, _p(st.pos), _p(st.gcell), _p(st.off), _p(st.cnt),
+                      _p(poff[t]), None)
+        nbr = np.zeros(int(poff[t, n]), np.uint32)
+        lib.orc_pairs(C.byref(params), n, _p(st.pos), _p(st.gcell), _p(st.off), _p(st.cnt),
+                      _p(poff[t]), _p(nbr))
+        nbrs.append(nbr)
+        density(params, st)
+        force(params, st)
+        advance(params, st, time, params.dt, params.sim_scale)
+        time = float(np.float32(np.float32(time) + np.float32(params.dt)))
+    pbase = np.zeros(steps + 1, np.uint64)
+    pbase[1:] = np.cumsum([a.size for a in nbrs])
+    pnbr = np.concatenate(nbrs) if nbrs else np.zeros(0, np.uint32)
+    return Frozen(n=n, steps=steps, perm=perm, inr=inr, poff=poff, pnbr=pnbr, pbase=pbase,
+                  time=times_out, states=states)
+
+
+def _theta(theta):
+    return None if theta is None else np.ascontiguousarray(theta, np.float64)
+
+
+def adj64_forward(params, fz: Frozen, x0, v0, e0, theta=None):
+    """The FP64 frozen-structure forward from (x0, v0, e0): the final (x, v, e).
+    theta = (visc, rest density, IntStiff) overrides the parameter block."""
+    x, v, e = (np.array(a, np.float64).reshape(fz.n, 3) for a in (x0, v0, e0))
+    th = _theta(theta)
+    _adj_lib().adj64_forward(C.byref(params), _p(th), fz.n, fz.steps, _p(fz.perm), _p(fz.inr),
+                             _p(fz.poff), _p(fz.pnbr), _p(fz.pbase), _p(fz.time), _p(x), _p(v), _p(e))
+    return x, v, e
+
+
+def adj64_backward(params, fz: Frozen, xb, vb, eb, x0=None, v0=None, e0=None, theta=None,
+                   use_states: bool = True):
+    """dL/d(x0, v0, e0) and dL/d(visc, rest density, IntStiff) from dL/d(final
+    x, v, e). With use_states the model is linearised around the recorded
+    (FP32) states; else around its own FP64 forward from (x0, v0, e0)."""
+    n = fz.n
+    xb, vb, eb = (np.array(a, np.float64).reshape(n, 3) for a in (xb, vb, eb))
+    g = np.zeros(3, np.float64)
+    th = _theta(theta)
+    if use_states:
+        st = np.ascontiguousarray(fz.states)
+        z = fz.states[0] if fz.steps else np.zeros((3, n, 3))
+        x0, v0, e0 = z[0], z[1], z[2]
+    else:
+        st = None
+    x0, v0, e0 = (np.ascontiguousarray(a, np.float64).reshape(n, 3) for a in (x0, v0, e0))
+    _adj_lib().adj64_backward(C.byref(params), _p(th), n, fz.steps, _p(fz.perm), _p(fz.inr), _p(fz.poff),
+                              _p(fz.pnbr), _p(fz.pbase), _p(fz.time), _p(st), _p(x0), _p(v0), _p(e0),
+                              _p(xb), _p(vb), _p(eb), _p(g))
+    return xb, vb, eb, g

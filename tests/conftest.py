@@ -24,7 +24,8 @@ def _ensure_built():
     from fluids3_gb300 import build as B
     B.build()
     from oracle import oracle as O
-    if not O.ORACLE_LIB.exists():
+    srcs = [O.HERE / "fluids_oracle.c", O.HERE / "adjoint64.c", O.HERE / "build_oracle.sh"]
+    if not O.ORACLE_LIB.exists() or any(f.stat().st_mtime > O.ORACLE_LIB.stat().st_mtime for f in srcs):
         O.build(ref=False)
 
 

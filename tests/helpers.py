@@ -64,3 +64,28 @@ def force_rel_err(got, ref64, scale64, mask) -> float:
     err = np.linalg.norm(g - r, axis=1)
     s = np.where(s > 0, s, 1.0)
     return float(np.max(err / s)) if r.size else 0.0
+
+
+def stirred_state(sc, warm_steps, seed):
+    """A scene advanced `warm_steps` FP32 oracle steps, then stirred so that
+    every branch of the advance is taken: some velocities above the speed
+    limit, some points pushed against every wall."""
+    from oracle import oracle as O
+    p = sc.params
+    st = O.State.new(p, sc.pos, sc.vel, sc.veval, sc.clr)
+    t = O.run(p, st, warm_steps, 0.0) if warm_steps else 0.0
+    rng = np.random.default_rng(seed)
+    n = st.n
+    fast = rng.choice(n, n // 20, replace=False)
+    st.vel[fast] *= np.float32(1.0)
+    st.vel[fast] += rng.normal(0.0, 3.0, (fast.size, 3)).astype(np.float32)
+    lo = np.array(p.bound_min, np.float32)
+    hi = np.array(p.bound_max, np.float32)
+    wall = rng.choice(n, 12, replace=False)
+    for k, i in enumerate(wall):
+        ax = k % 3
+        low = (k // 3) % 2 == 0
+        st.pos[i, ax] = (lo[ax] + np.float32(0.3)) if low else (hi[ax] - np.float32(0.3))
+        # moving into the wall: the damping term pushes |accel| past AccelLimit
+        st.veval[i, ax] = np.float32(-2.0 if low else 2.0) if k < 6 else np.float32(0.0)
+    return st, t
