@@ -1,9 +1,10 @@
 """Builds libfluids_gb300.so in-tree with nvcc for sm_103a.
 
 Each translation unit compiles in its own nvcc process (in parallel), then
-one nvcc call links the shared library next to this file. Kernel units are
-compiled with --fmad=false (no FMA contraction), host units with
--ffp-contract=off, so every float expression rounds as written.
+one nvcc call links the shared library next to this file. Forward kernel
+units are compiled with --fmad=false (no FMA contraction), host units with
+-ffp-contract=off, so every float expression rounds as written; the adjoint
+unit keeps contraction on.
 """
 from __future__ import annotations
 
@@ -24,6 +25,10 @@ COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
           f"-I{INCLUDE}", f"-I{CSRC}"]
 CU_FLAGS = ARCH + COMMON + ["--fmad=false", "-Xptxas", "-v"]
 CPP_FLAGS = COMMON
+# The adjoint kernels have no bit-exact target: FMA contraction on. Their
+# decisions shared with the forward use explicitly rounded operations.
+CONTRACTED = {"fl_adjoint.cu"}
+CU_FLAGS_CONTRACTED = ARCH + COMMON + ["-Xptxas", "-v"]
 
 
 def nvcc() -> str:
@@ -39,7 +44,10 @@ def sources() -> list[Path]:
 
 def _compile(src: Path) -> tuple[Path, str]:
     obj = BUILD / (src.name + ".o")
-    flags = CU_FLAGS if src.suffix == ".cu" else CPP_FLAGS
+    if src.suffix == ".cu":
+        flags = CU_FLAGS_CONTRACTED if src.name in CONTRACTED else CU_FLAGS
+    else:
+        flags = CPP_FLAGS
     cmd = [nvcc(), *flags, "-c", str(src), "-o", str(obj)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:

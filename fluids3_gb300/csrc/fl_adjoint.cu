@@ -20,9 +20,10 @@
 //                   through the permutation) and the direct parts of dL/dX, dL/dE
 //   k_adj_force     per point s, over its own pairs (s the owner) and its
 //                   reverse pairs (the points whose search block holds s):
-//                   dL/dX, dL/dE, dL/drho and the parameter partials
-//   k_adj_density   per point, own and reverse pairs: the density's share of
-//                   dL/dX, written through the permutation
+//                   dL/dX, dL/dE, dL/drho and the parameter partials; records
+//                   the reverse pairs it finds
+//   k_adj_density   per point, own and reverse pairs (both from lists): the
+//                   density's share of dL/dX, written through the permutation
 //   k_param_*       deterministic per-scene sums of the parameter partials
 // Every sum is a per-thread gather (no atomics), so the result is
 // bit-reproducible from run to run. The search block of a point in cell c
@@ -37,59 +38,85 @@ namespace {
 #include "fl_device.cuh"
 
 constexpr int kAdjThreads = 128;
+
+// One kernel instantiation serves single-scene and batched systems (the
+// scene table is null for a single scene), so a scene's adjoint is the same
+// machine code, and the same bits, alone or in a batch.
+__device__ __forceinline__ const DevParams &scene_params(const DevParams &P0, const SceneTab &T, int s) {
+    return T.params ? T.params[T.point_scene[s]] : P0;
+}
 constexpr int kReduceThreads = 256;
 constexpr int kReduceChunk = 4096;   // points per partial-sum block
 
 __device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ float3 sub3(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ float3 axpy3(float a, float3 x, float3 y) {
-    return make_float3(a * x.x + y.x, a * x.y + y.y, a * x.z + y.z);
+
+// This file is compiled with FMA contraction on (the adjoint has no
+// bit-exact target). The branch decisions it shares with the forward --
+// which pairs pass 0 < d^2 < rd2, which walls act, whether the limits
+// clamp -- are evaluated with explicitly rounded operations (__fmul_rn,
+// __fadd_rn, never contracted) in advanceParticles' order, so they match the
+// forward's (compiled without contraction) bit for bit.
+__device__ __forceinline__ float dsq_rn(float dx, float dy, float dz) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }
 
-// Acceleration before the AccelLimit clamp: advanceParticles' wall, force
-// and gravity terms (fluid_kernels.cu:343-400) in the forward's order.
-__device__ __forceinline__ float3 accel_before_clamp(const DevParams &P, float time, float ss, float3 f,
-                                                     float3 pos, float3 ve) {
-    float3 a = make_float3(f.x * P.pmass, f.y * P.pmass, f.z * P.pmass);
-    float diff, adj;
-    diff = P.pradius - (pos.y - (P.bound_min.y + (pos.x - P.bound_min.x) * P.bound_slope)) * ss;
-    if (diff > kEpsilon) {
-        float3 nrm = make_float3(-P.bound_slope, 1.0f - P.bound_slope, 0.0f);
-        adj = P.bound_stiff * diff - P.bound_damp * (nrm.x * ve.x + nrm.y * ve.y + nrm.z * ve.z);
-        nrm.x *= adj; nrm.y *= adj; nrm.z *= adj;
-        a.x += nrm.x - ve.x * P.bound_friction;
-        a.y += nrm.y - ve.y * P.bound_friction;
-        a.z += nrm.z - ve.z * P.bound_friction;
+// advanceParticles' wall distances (fluid_kernels.cu:356-397).
+struct Walls {
+    float ylo, yhi, xlo, xhi, zlo, zhi;
+    float wall, ph;
+};
+
+__device__ __forceinline__ Walls wall_terms(const DevParams &P, float time, float ss, float3 pos) {
+    Walls w;
+    w.ylo = __fsub_rn(P.pradius, __fmul_rn(__fsub_rn(pos.y, __fadd_rn(P.bound_min.y,
+                      __fmul_rn(__fsub_rn(pos.x, P.bound_min.x), P.bound_slope))), ss));
+    w.yhi = __fsub_rn(P.pradius, __fmul_rn(__fsub_rn(P.bound_max.y, pos.y), ss));
+    w.ph = __fadd_rn(__fmul_rn(time, P.bound_wall_freq), __fdiv_rn(pos.z, 400.f));
+    w.wall = __fmul_rn(__fadd_rn(__fmul_rn(sinf(w.ph), 0.5f), 0.5f), P.bound_wall_force);
+    w.xlo = __fsub_rn(P.pradius, __fmul_rn(__fsub_rn(pos.x, __fadd_rn(P.bound_min.x, w.wall)), ss));
+    w.xhi = __fsub_rn(P.pradius, __fmul_rn(__fsub_rn(P.bound_max.x, pos.x), ss));
+    w.zlo = __fsub_rn(P.pradius, __fmul_rn(__fsub_rn(pos.z, P.bound_min.z), ss));
+    w.zhi = __fsub_rn(P.pradius, __fmul_rn(__fsub_rn(P.bound_max.z, pos.z), ss));
+    return w;
+}
+
+// Acceleration before the AccelLimit clamp (fluid_kernels.cu:343-400),
+// rounded like the forward: force times mass, the wall terms, gravity.
+// (Terms the forward multiplies by a zero normal component only add a
+// signed zero and are left out; the squared length is unchanged.)
+__device__ __forceinline__ float3 accel_before_clamp(const DevParams &P, const Walls &w, float3 f, float3 ve) {
+    float3 a = make_float3(__fmul_rn(f.x, P.pmass), __fmul_rn(f.y, P.pmass), __fmul_rn(f.z, P.pmass));
+    const float kb = P.bound_stiff, kd = P.bound_damp, fr = P.bound_friction;
+    if (w.ylo > kEpsilon) {
+        const float nx = -P.bound_slope, ny = __fsub_rn(1.0f, P.bound_slope);
+        const float dot = __fadd_rn(__fadd_rn(__fmul_rn(nx, ve.x), __fmul_rn(ny, ve.y)), __fmul_rn(0.0f, ve.z));
+        const float adj = __fsub_rn(__fmul_rn(kb, w.ylo), __fmul_rn(kd, dot));
+        a.x = __fadd_rn(a.x, __fsub_rn(__fmul_rn(nx, adj), __fmul_rn(ve.x, fr)));
+        a.y = __fadd_rn(a.y, __fsub_rn(__fmul_rn(ny, adj), __fmul_rn(ve.y, fr)));
+        a.z = __fadd_rn(a.z, __fsub_rn(__fmul_rn(0.0f, adj), __fmul_rn(ve.z, fr)));
     }
-    diff = P.pradius - (P.bound_max.y - pos.y) * ss;
-    if (diff > kEpsilon) {
-        float3 nrm = make_float3(0.0f, -1.0f, 0.0f);
-        adj = P.bound_stiff * diff - P.bound_damp * (nrm.x * ve.x + nrm.y * ve.y + nrm.z * ve.z);
-        nrm.x *= adj; nrm.y *= adj; nrm.z *= adj;
-        a.x += nrm.x - ve.x * P.bound_friction;
-        a.y += nrm.y - ve.y * P.bound_friction;
-        a.z += nrm.z - ve.z * P.bound_friction;
+    if (w.yhi > kEpsilon) {
+        const float adj = __fsub_rn(__fmul_rn(kb, w.yhi), __fmul_rn(kd, -ve.y));
+        a.x = __fadd_rn(a.x, __fsub_rn(0.0f, __fmul_rn(ve.x, fr)));
+        a.y = __fadd_rn(a.y, __fsub_rn(-adj, __fmul_rn(ve.y, fr)));
+        a.z = __fadd_rn(a.z, __fsub_rn(0.0f, __fmul_rn(ve.z, fr)));
     }
-    const float wall = (sinf(time * P.bound_wall_freq + pos.z / 400.f) * 0.5f + 0.5f) * P.bound_wall_force;
-    diff = P.pradius - (pos.x - (P.bound_min.x + wall)) * ss;
-    if (diff > kEpsilon) a.x += wall * P.bound_stiff * diff - P.bound_damp * ve.x;
-    diff = P.pradius - (P.bound_max.x - pos.x) * ss;
-    if (diff > kEpsilon) a.x += -(P.bound_stiff * diff - P.bound_damp * (-ve.x));
-    diff = P.pradius - (pos.z - P.bound_min.z) * ss;
-    if (diff > kEpsilon) a.z += P.bound_stiff * diff - P.bound_damp * ve.z;
-    diff = P.pradius - (P.bound_max.z - pos.z) * ss;
-    if (diff > kEpsilon) a.z += -(P.bound_stiff * diff - P.bound_damp * (-ve.z));
-    a.x += P.gravity.x; a.y += P.gravity.y; a.z += P.gravity.z;
+    if (w.xlo > kEpsilon)
+        a.x = __fadd_rn(a.x, __fsub_rn(__fmul_rn(__fmul_rn(w.wall, kb), w.xlo), __fmul_rn(kd, ve.x)));
+    if (w.xhi > kEpsilon) a.x = __fadd_rn(a.x, -__fsub_rn(__fmul_rn(kb, w.xhi), __fmul_rn(kd, -ve.x)));
+    if (w.zlo > kEpsilon) a.z = __fadd_rn(a.z, __fsub_rn(__fmul_rn(kb, w.zlo), __fmul_rn(kd, ve.z)));
+    if (w.zhi > kEpsilon) a.z = __fadd_rn(a.z, -__fsub_rn(__fmul_rn(kb, w.zhi), __fmul_rn(kd, -ve.z)));
+    a.x = __fadd_rn(a.x, P.gravity.x);
+    a.y = __fadd_rn(a.y, P.gravity.y);
+    a.z = __fadd_rn(a.z, P.gravity.z);
     return a;
 }
 
 // Adjoint of the wall terms: given ab = dL/da, adds (da/dX)^T ab to xb and
 // (da/dE)^T ab to eb, with each wall active where the forward found it so.
-__device__ __forceinline__ void walls_adjoint(const DevParams &P, float time, float ss, float3 pos, float3 ab,
+__device__ __forceinline__ void walls_adjoint(const DevParams &P, const Walls &w, float ss, float3 ab,
                                               float3 &xb, float3 &eb) {
-    float diff;
-    diff = P.pradius - (pos.y - (P.bound_min.y + (pos.x - P.bound_min.x) * P.bound_slope)) * ss;
-    if (diff > kEpsilon) {
+    if (w.ylo > kEpsilon) {
         const float nx = -P.bound_slope, ny = 1.0f - P.bound_slope;
         const float nab = nx * ab.x + ny * ab.y;   // (d a / d adj) . ab
         xb.x += P.bound_stiff * nab * (ss * P.bound_slope);
@@ -98,35 +125,28 @@ __device__ __forceinline__ void walls_adjoint(const DevParams &P, float time, fl
         eb.y += -P.bound_damp * ny * nab - P.bound_friction * ab.y;
         eb.z += -P.bound_friction * ab.z;
     }
-    diff = P.pradius - (P.bound_max.y - pos.y) * ss;
-    if (diff > kEpsilon) {
+    if (w.yhi > kEpsilon) {
         const float nab = -ab.y;
         xb.y += P.bound_stiff * nab * ss;
         eb.y += P.bound_damp * nab - P.bound_friction * ab.y;
         eb.x -= P.bound_friction * ab.x;
         eb.z -= P.bound_friction * ab.z;
     }
-    const float ph = time * P.bound_wall_freq + pos.z / 400.f;
-    const float wall = (sinf(ph) * 0.5f + 0.5f) * P.bound_wall_force;
-    diff = P.pradius - (pos.x - (P.bound_min.x + wall)) * ss;
-    if (diff > kEpsilon) {
-        const float dwall = cosf(ph) * 0.5f * P.bound_wall_force / 400.f;
-        xb.x -= ab.x * wall * P.bound_stiff * ss;
-        xb.z += ab.x * P.bound_stiff * dwall * (diff + wall * ss);
+    if (w.xlo > kEpsilon) {
+        const float dwall = cosf(w.ph) * 0.5f * P.bound_wall_force / 400.f;
+        xb.x -= ab.x * w.wall * P.bound_stiff * ss;
+        xb.z += ab.x * P.bound_stiff * dwall * (w.xlo + w.wall * ss);
         eb.x -= P.bound_damp * ab.x;
     }
-    diff = P.pradius - (P.bound_max.x - pos.x) * ss;
-    if (diff > kEpsilon) {
+    if (w.xhi > kEpsilon) {
         xb.x -= ab.x * P.bound_stiff * ss;
         eb.x -= P.bound_damp * ab.x;
     }
-    diff = P.pradius - (pos.z - P.bound_min.z) * ss;
-    if (diff > kEpsilon) {
+    if (w.zlo > kEpsilon) {
         xb.z -= ab.z * P.bound_stiff * ss;
         eb.z -= P.bound_damp * ab.z;
     }
-    diff = P.pradius - (P.bound_max.z - pos.z) * ss;
-    if (diff > kEpsilon) {
+    if (w.zhi > kEpsilon) {
         xb.z -= ab.z * P.bound_stiff * ss;
         eb.z -= P.bound_damp * ab.z;
     }
@@ -144,18 +164,17 @@ __device__ __forceinline__ float3 clamp_adjoint(float3 u, float L, float3 ub) {
 // the step's outputs (slot order). Out: dL/dF (fb), the direct parts of
 // dL/dX (xa) and dL/dE (ea), and dL/dV, written through the permutation
 // to pre-sort index src[s].
-template <bool BATCH>
 __global__ void __launch_bounds__(kAdjThreads)
 k_adj_advance(const __grid_constant__ DevParams P0, const SceneTab T, int n, const float *time_ptr, float dt,
               const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ src,
               const float4 *__restrict__ X, const float4 *__restrict__ V, const float4 *__restrict__ E,
-              const float4 *__restrict__ F,
+              const float4 *__restrict__ F, const float *__restrict__ rho,
               const float4 *__restrict__ xo_b, const float4 *__restrict__ vo_b, const float4 *__restrict__ eo_b,
               float4 *__restrict__ xa, float4 *__restrict__ ea, float4 *__restrict__ fb,
-              float4 *__restrict__ v_out) {
+              float4 *__restrict__ v_out, float2 *__restrict__ rr) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
-    const DevParams &P = BATCH ? T.params[T.point_scene[s]] : P0;
+    const DevParams &P = scene_params(P0, T, s);
     const float3 xb_o = xyz(xo_b[s]), vb_o = xyz(vo_b[s]), eb_o = xyz(eo_b[s]);
     const uint32_t dst = src[s];
     if (gcell[s] == kUndef) {
@@ -164,22 +183,26 @@ k_adj_advance(const __grid_constant__ DevParams P0, const SceneTab T, int n, con
         ea[s] = f4(eb_o);
         fb[s] = make_float4(0.f, 0.f, 0.f, 0.f);
         v_out[dst] = make_float4(0.f, 0.f, 0.f, 0.f);
+        rr[s] = make_float2(0.f, 0.f);
         return;
     }
+    const float rho_s = rho[s];
+    rr[s] = make_float2(rho_s, 1.0f / rho_s);   // density and its reciprocal for the pair passes
     const float ss = P.sim_scale;
     const float time = *time_ptr;
     const float3 pos = xyz(X[s]), vel = xyz(V[s]), ve = xyz(E[s]);
-    const float3 a = accel_before_clamp(P, time, ss, xyz(F[s]), pos, ve);
+    const Walls w = wall_terms(P, time, ss, pos);
+    const float3 a = accel_before_clamp(P, w, xyz(F[s]), ve);
     const float dts = dt / ss;
     // v' feeds x' (dt/ss), e' (1/2) and v'; V feeds v' and e' (1/2)
     const float3 vt = make_float3(vb_o.x + 0.5f * eb_o.x + dts * xb_o.x, vb_o.y + 0.5f * eb_o.y + dts * xb_o.y,
                                   vb_o.z + 0.5f * eb_o.z + dts * xb_o.z);
     float3 ab = make_float3(dt * vt.x, dt * vt.y, dt * vt.z);
     float3 vb = make_float3(vt.x + 0.5f * eb_o.x, vt.y + 0.5f * eb_o.y, vt.z + 0.5f * eb_o.z);
-    if (a.x * a.x + a.y * a.y + a.z * a.z > P.AL2) ab = clamp_adjoint(a, P.AL, ab);
-    if (vel.x * vel.x + vel.y * vel.y + vel.z * vel.z > P.VL2) vb = clamp_adjoint(vel, P.VL, vb);
+    if (dsq_rn(a.x, a.y, a.z) > P.AL2) ab = clamp_adjoint(a, P.AL, ab);
+    if (dsq_rn(vel.x, vel.y, vel.z) > P.VL2) vb = clamp_adjoint(vel, P.VL, vb);
     float3 xb = xb_o, eb = make_float3(0.f, 0.f, 0.f);
-    walls_adjoint(P, time, ss, pos, ab, xb, eb);
+    walls_adjoint(P, w, ss, ab, xb, eb);
     xa[s] = f4(xb);
     ea[s] = f4(eb);
     fb[s] = make_float4(P.pmass * ab.x, P.pmass * ab.y, P.pmass * ab.z, 0.f);
@@ -188,44 +211,93 @@ k_adj_advance(const __grid_constant__ DevParams P0, const SceneTab T, int n, con
 
 // One pair's force adjoint. The owner o's force gets
 //   t = (pterm D + vterm dE) B,  D = X_o - X_j,  dE = E_j - E_o,
-// and fo = dL/dF_o. Returns dL/dD; the caller adds it to the owner's dL/dX
-// and subtracts it from the neighbour's.
-struct PairAdj {
-    float3 dD;        // dL/dD
-    float eB;         // vterm B: dL/dE_j = +eB fo, dL/dE_o = -eB fo
-    float rho_common; // B (D.fo) A c kappa / r: dL/drho for both ends (before the B/rho term)
-    float SF;         // (pterm D + vterm dE) . fo
-    float B;
-    float DF, dEF, AcR;   // parameter partials: D.fo, dE.fo, A c / r
+// with fo = dL/dF_o:
+//   dL/dD      = B pterm fo + (B (D.fo) kP - (sv.fo) kB) D,
+//                sv = pterm D + vterm dE, kP = -A Pp h d2 / r^3, kB = d2 / (r rho_o rho_j)
+//   dL/dE_j    = +vterm B fo,  dL/dE_o = -vterm B fo
+//   dL/drho    = B (D.fo) A c kappa / r - (sv.fo) B / rho   (for either end, its own rho)
+// Every term is unchanged when D and dE both change sign, so a pair is
+// evaluated in the orientation of the point s the thread owns
+// (D = X_s - X_q, dE = E_q - E_s) whichever end owns it; the reverse role
+// then enters with the opposite sign. No divisions: r from one reciprocal
+// square root, 1/(rho_s rho_q) from per-point reciprocals.
+constexpr uint32_t kRevFlag = 0x80000000u;    // entry: a reverse pair only (q owns s)
+constexpr uint32_t kBothFlag = 0x40000000u;   // entry: an own pair that is also reverse (same cell)
+constexpr uint32_t kSlotMask = 0x3fffffffu;
+
+struct PairGeo {
+    float3 D, sv;
+    float B, pterm, AcR, kP, kB;
 };
 
-__device__ __forceinline__ PairAdj pair_adjoint(const DevParams &P, float3 D, float3 dE, float dsq,
-                                                float rho_o, float rho_j, float3 fo) {
-    PairAdj o;
-    const float r = sqrtf(dsq * P.d2);
+__device__ __forceinline__ PairGeo pair_geometry(const DevParams &P, float3 D, float3 dE, float dsq, float rho_s,
+                                                 float rho_q, float irr) {
+    PairGeo g;
+    const float r2 = dsq * P.d2;
+    const float ir = rsqrtf(r2);
+    const float r = r2 * ir;
     const float c = P.psmoothradius - r;
     const float A = P.sim_scale * -0.5f * P.spikykern;
-    const float Pp = ((rho_o - P.prest_dens) + (rho_j - P.prest_dens)) * P.pintstiff;
-    const float AcR = A * c / r;
-    const float pterm = AcR * Pp;
-    const float RR = rho_o * rho_j;
-    const float B = c / RR;
-    const float3 sv = make_float3(pterm * D.x + P.vterm * dE.x, pterm * D.y + P.vterm * dE.y,
-                                  pterm * D.z + P.vterm * dE.z);
-    const float DF = dot3(D, fo);
-    const float SF = dot3(sv, fo);
-    // d pterm / dD = -A Pp h d2 / r^3 D;  d B / dD = -(d2 / r) / RR D
-    const float r3 = r * r * r;
-    const float kD = B * DF * (-A * Pp * P.psmoothradius * P.d2 / r3) + SF * (-(P.d2 / r) / RR);
-    o.dD = make_float3(B * pterm * fo.x + kD * D.x, B * pterm * fo.y + kD * D.y, B * pterm * fo.z + kD * D.z);
-    o.eB = P.vterm * B;
-    o.rho_common = B * DF * AcR * P.pintstiff;
-    o.SF = SF;
-    o.B = B;
-    o.DF = DF;
-    o.dEF = dot3(dE, fo);
-    o.AcR = AcR;
-    return o;
+    const float Pp = ((rho_s - P.prest_dens) + (rho_q - P.prest_dens)) * P.pintstiff;
+    g.D = D;
+    g.AcR = A * c * ir;
+    g.pterm = g.AcR * Pp;
+    g.B = c * irr;
+    g.sv = make_float3(g.pterm * D.x + P.vterm * dE.x, g.pterm * D.y + P.vterm * dE.y,
+                       g.pterm * D.z + P.vterm * dE.z);
+    g.kP = -A * Pp * P.psmoothradius * P.d2 * (ir * ir * ir);
+    g.kB = P.d2 * ir * irr;
+    return g;
+}
+
+// Per point: accumulated adjoints of one force-adjoint pass.
+struct AdjAcc {
+    float3 x, e;
+    float r, gv, gr, gk;
+};
+
+// The cotangent f of one pair's force, entering s's accumulators with sign
+// sg (+1: s owns the pair and f = dL/dF_s; -1: q owns it and f = dL/dF_q).
+// Returns f . D for the parameter partials.
+__device__ __forceinline__ float apply_cotangent(const DevParams &P, AdjAcc &a, const PairGeo &g, float3 f, float sg,
+                                                 float irs) {
+    const float DF = dot3(g.D, f);
+    const float SF = dot3(g.sv, f);
+    const float k = g.B * DF * g.kP - SF * g.kB;
+    const float bp = g.B * g.pterm;
+    a.x.x += sg * (bp * f.x + k * g.D.x);
+    a.x.y += sg * (bp * f.y + k * g.D.y);
+    a.x.z += sg * (bp * f.z + k * g.D.z);
+    const float ke = sg * P.vterm * g.B;
+    a.e.x -= ke * f.x; a.e.y -= ke * f.y; a.e.z -= ke * f.z;
+    a.r += sg * (g.B * DF * g.AcR * P.pintstiff - SF * g.B * irs);
+    return DF;
+}
+
+// One entry of s's pair list (own, reverse, or both).
+__device__ __forceinline__ void adj_pair(const DevParams &P, AdjAcc &a, float3 X, float3 Ev, float rs, float3 fs,
+                                         float irs, uint32_t entry, const float4 *__restrict__ pos,
+                                         const float4 *__restrict__ veval, const float2 *__restrict__ rr,
+                                         const float4 *__restrict__ fb) {
+    const bool rev_only = (entry & kRevFlag) != 0u;
+    const bool both = (entry & kBothFlag) != 0u;
+    const uint32_t q = entry & kSlotMask;
+    const float4 qp = pos[q];
+    const float3 D = make_float3(X.x - qp.x, X.y - qp.y, X.z - qp.z);
+    const float dsq = D.x * D.x + D.y * D.y + D.z * D.z;
+    const float4 qe = veval[q];
+    const float3 dE = make_float3(qe.x - Ev.x, qe.y - Ev.y, qe.z - Ev.z);
+    const float2 rq2 = rr[q];
+    const PairGeo g = pair_geometry(P, D, dE, dsq, rs, rq2.x, irs * rq2.y);
+    float3 fq = make_float3(0.f, 0.f, 0.f);
+    if (rev_only || both) fq = xyz(fb[q]);
+    const float DF = apply_cotangent(P, a, g, rev_only ? fq : fs, rev_only ? -1.0f : 1.0f, irs);
+    if (!rev_only) {
+        a.gv += P.lapkern * dot3(dE, fs) * g.B;
+        a.gr += g.B * DF * g.AcR * (-2.0f * P.pintstiff);
+        a.gk += g.B * DF * g.AcR * ((rs - P.prest_dens) + (rq2.x - P.prest_dens));
+    }
+    if (both) apply_cotangent(P, a, g, fq, -1.0f, irs);
 }
 
 // The reverse search block of a point in local cell lc: entry k of the
@@ -251,57 +323,163 @@ __device__ __forceinline__ void local_coords(const DevParams &P, int lc, int &cx
     cy = t / P.gridRes.z;
 }
 
-// Reverse of computeForce for point s: its own pairs (from the density
-// pass's list, or a walk when the list overflowed) and its reverse pairs.
-// Writes the complete dL/dE through the permutation, accumulates dL/dX
-// into xa, and stores dL/drho and the parameter partials
-// (dL/dvisc, dL/drest_density, dL/dIntStiff) of its own pairs.
-template <bool PRUNE, bool BATCH>
-__global__ void __launch_bounds__(kAdjThreads)
+// Candidates of a point's reverse search block, one at a time in
+// ascending cell-entry and slot order, leaving out the point's own cell
+// (its pairs there are symmetric: every own pair in the same cell is also a
+// reverse pair, taken from the own list instead). With pruning (gridSrch 2)
+// a cell that the block reaches into from below along some axes is skipped
+// unless the point lies within the band of its upper face on those axes
+// (`up`), and only members flagged within the band of their lower face on
+// those axes (lower-band rows of the slot flags) are visited, 32 slots per
+// flag word.
+struct RevIter {
+    int k, cx, cy, cz;
+    uint32_t code, up;
+    uint32_t w, w_last, lo, hi, bits;
+};
+
+template <bool PRUNE>
+__device__ __forceinline__ uint32_t rev_word(const RevIter &it, const DevParams &P,
+                                             const uint32_t *__restrict__ lobits, uint32_t w) {
+    uint32_t v = 0xffffffffu;
+    if (PRUNE) {
+        if (it.up & 1u) v &= lobits[w];
+        if (it.up & 2u) v &= lobits[(size_t)P.upwords + w];
+        if (it.up & 4u) v &= lobits[2 * (size_t)P.upwords + w];
+    }
+    if (w == (it.lo >> 5)) v &= 0xffffffffu << (it.lo & 31u);
+    if (w == it.w_last && (it.hi & 31u)) v &= 0xffffffffu >> (32u - (it.hi & 31u));
+    return v;
+}
+
+template <bool PRUNE>
+__device__ __forceinline__ void rev_begin(RevIter &it, const DevParams &P, uint32_t gc, uint32_t code, bool active) {
+    it.k = active ? 0 : P.gridAdjCnt;
+    it.code = code;
+    it.up = 0;
+    it.w = it.w_last = it.lo = it.hi = 0;
+    it.bits = 0;
+    local_coords(P, active ? (int)gc - P.cell_base : 0, it.cx, it.cy, it.cz);
+}
+
+template <bool PRUNE>
+__device__ __forceinline__ bool rev_next(RevIter &it, const DevParams &P, const uint32_t *__restrict__ off,
+                                         const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ lobits,
+                                         uint32_t &q) {
+    while (it.bits == 0) {
+        if (it.w < it.w_last) {
+            it.w++;
+            it.bits = rev_word<PRUNE>(it, P, lobits, it.w);
+            continue;
+        }
+        // next cell of the reverse block
+        bool found = false;
+        while (it.k < P.gridAdjCnt) {
+            uint32_t up;
+            const int k = it.k++;
+            const int lc = reverse_cell(P, it.cx, it.cy, it.cz, k, up);
+            if (lc < 0) continue;
+            const int R = P.gridSrch, sh = R - 2;
+            if (k % R == sh && (k / R) % R == sh && k / (R * R) == sh) continue;   // own cell
+            if (PRUNE && (it.code & up) != up) continue;
+            const int cell = P.cell_base + lc;
+            const uint32_t m = cnt[cell];
+            if (m == 0) continue;
+            it.up = up;
+            it.lo = off[cell];
+            it.hi = it.lo + m;
+            it.w = it.lo >> 5;
+            it.w_last = (it.hi - 1) >> 5;
+            it.bits = rev_word<PRUNE>(it, P, lobits, it.w);
+            found = true;
+            break;
+        }
+        if (!found) return false;
+    }
+    q = (it.w << 5) + (uint32_t)(__ffs(it.bits) - 1);
+    it.bits &= it.bits - 1u;
+    return true;
+}
+
+// Reverse of computeForce for point s (all 32 lanes of a warp call it).
+// First each lane walks its reverse block (the points whose search block
+// holds s, outside s's own cell) and records the reverse pairs it finds in
+// revlist; then the warp evaluates, in step, every lane's own pairs (the
+// density pass's list; those in the own cell are reverse pairs too) and
+// its recorded reverse pairs, so the long pair arithmetic runs with the
+// lanes busy. A lane whose own or reverse list overflowed evaluates those
+// pairs while walking them again. Writes the complete dL/dE through the
+// permutation, accumulates dL/dX into xa, stores dL/drho and the parameter
+// partials (dL/dvisc, dL/drest_density, dL/dIntStiff) of its own pairs;
+// revlist / revcnt stay for the density adjoint.
+template <bool PRUNE>
+__global__ void __launch_bounds__(kAdjThreads, 8)
 k_adj_force(const __grid_constant__ DevParams P0, const SceneTab T, int n,
-            const float4 *__restrict__ pos, const float4 *__restrict__ veval, const float *__restrict__ rho,
+            const float4 *__restrict__ pos, const float4 *__restrict__ veval, const float2 *__restrict__ rr,
             const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ off, const uint32_t *__restrict__ cnt,
             const uint32_t *__restrict__ upbits, const uint32_t *__restrict__ hitlist,
             const uint32_t *__restrict__ hitcnt, const uint32_t *__restrict__ src,
             const float4 *__restrict__ fb, float4 *__restrict__ xa, const float4 *__restrict__ ea,
-            float *__restrict__ rb, float4 *__restrict__ pc, float4 *__restrict__ e_out) {
+            float *__restrict__ rb, float4 *__restrict__ pc, float4 *__restrict__ e_out,
+            uint32_t *__restrict__ revlist, uint32_t *__restrict__ revcnt) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    const DevParams &P = BATCH ? T.params[T.point_scene[s]] : P0;
-    const uint32_t gc = gcell[s];
-    const uint32_t dst = src[s];
-    if (gc == kUndef) {
-        e_out[dst] = ea[s];
-        rb[s] = 0.0f;
-        pc[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-        return;
+    const DevParams &P = scene_params(P0, T, s < n ? s : 0);
+    const uint32_t gc = (s < n) ? gcell[s] : kUndef;
+    const bool active = gc != kUndef;
+    AdjAcc acc;
+    acc.x = acc.e = make_float3(0.f, 0.f, 0.f);
+    acc.r = acc.gv = acc.gr = acc.gk = 0.0f;
+    float3 X = make_float3(0.f, 0.f, 0.f), Ev = X, fs = X;
+    float rs = 1.0f, irs = 1.0f;
+    uint32_t my_code = 0, c_lo = 0, c_hi = 0;
+    if (active) {
+        const float4 p4 = pos[s];
+        X = xyz(p4);
+        my_code = __float_as_uint(p4.w);
+        Ev = xyz(veval[s]);
+        fs = xyz(fb[s]);
+        const float2 r2 = rr[s];
+        rs = r2.x;
+        irs = r2.y;
+        c_lo = off[gc];
+        c_hi = c_lo + cnt[gc];
     }
-    const float4 p4 = pos[s];
-    const float3 X = xyz(p4), Ev = xyz(veval[s]), fs = xyz(fb[s]);
-    const float rs = rho[s];
-    const uint32_t my_code = __float_as_uint(p4.w);
-    float3 xacc = make_float3(0.f, 0.f, 0.f), eacc = make_float3(0.f, 0.f, 0.f);
-    float racc = 0.0f, g_visc = 0.0f, g_rest = 0.0f, g_stiff = 0.0f;
+    const uint32_t hcap = (uint32_t)P.hcap;
+    const uint32_t *lobits = upbits + 3 * (size_t)P.upwords;
 
-    // own pairs: s is the owner, j its neighbour
-    auto own = [&](uint32_t j) {
-        const float4 q = pos[j];
-        const float3 D = sub3(X, xyz(q));
-        const float dsq = D.x * D.x + D.y * D.y + D.z * D.z;
-        const float rj = rho[j];
-        const float3 dE = sub3(xyz(veval[j]), Ev);
-        const PairAdj a = pair_adjoint(P, D, dE, dsq, rs, rj, fs);
-        xacc.x += a.dD.x; xacc.y += a.dD.y; xacc.z += a.dD.z;
-        eacc.x -= a.eB * fs.x; eacc.y -= a.eB * fs.y; eacc.z -= a.eB * fs.z;
-        racc += a.rho_common - a.SF * a.B / rs;
-        g_visc += P.lapkern * a.dEF * a.B;
-        g_rest += a.B * a.DF * a.AcR * (-2.0f * P.pintstiff);
-        g_stiff += a.B * a.DF * a.AcR * ((rs - P.prest_dens) + (rj - P.prest_dens));
-    };
-    const uint32_t nh = hitcnt[s];
-    if (nh <= (uint32_t)P.hcap) {
-        for (uint32_t t = 0; t < nh; t++) own(hitlist[list_at(P, s, t)]);
-    } else {
+    // reverse pairs outside the own cell -> revlist
+    uint32_t nrev = 0;
+    if (active) {
+        RevIter it;
+        rev_begin<PRUNE>(it, P, gc, my_code, true);
+        uint32_t q;
+        while (rev_next<PRUNE>(it, P, off, cnt, lobits, q)) {
+            const float4 qp = pos[q];
+            const float dsq = dsq_rn(qp.x - X.x, qp.y - X.y, qp.z - X.z);
+            if (dsq < P.rd2 && dsq > 0.0f) {
+                if (nrev < hcap) revlist[list_at(P, s, nrev)] = q;
+                nrev++;
+            }
+        }
+    }
+
+    // own pairs (own cell: both roles) and reverse pairs from the lists
+    auto own_entry = [&](uint32_t j) { return (j >= c_lo && j < c_hi) ? (j | kBothFlag) : j; };
+    const uint32_t nh = active ? hitcnt[s] : 0u;
+    const uint32_t n_own = (nh <= hcap) ? nh : 0u;
+    const uint32_t n_rev = (nrev <= hcap) ? nrev : 0u;
+    const uint32_t mine = n_own + n_rev;
+    const uint32_t most = __reduce_max_sync(0xffffffffu, mine);
+    for (uint32_t t = 0; t < most; t++) {
+        if (t < mine) {
+            const uint32_t e = (t < n_own) ? own_entry(hitlist[list_at(P, s, t)])
+                                           : (revlist[list_at(P, s, t - n_own)] | kRevFlag);
+            adj_pair(P, acc, X, Ev, rs, fs, irs, e, pos, veval, rr, fb);
+        }
+    }
+
+    // overflowed lists: walk again, evaluating as found
+    if (active && nh > hcap) {
         const int base = (int)gc - P.nadj;
         for (int c = 0; c < P.gridAdjCnt; c++) {
             CandIter it;
@@ -309,59 +487,56 @@ k_adj_force(const __grid_constant__ DevParams P0, const SceneTab T, int n,
             uint32_t j;
             while (cand_next<PRUNE>(it, P, upbits, j)) {
                 const float4 q = pos[j];
-                const float dx = p4.x - q.x, dy = p4.y - q.y, dz = p4.z - q.z;
-                const float dsq = dx * dx + dy * dy + dz * dz;
-                if (dsq < P.rd2 && dsq > 0.0f) own(j);
+                const float dsq = dsq_rn(X.x - q.x, X.y - q.y, X.z - q.z);
+                if (dsq < P.rd2 && dsq > 0.0f) adj_pair(P, acc, X, Ev, rs, fs, irs, own_entry(j), pos, veval, rr, fb);
             }
         }
     }
-
-    // reverse pairs: o is the owner, s its neighbour
-    int cx, cy, cz;
-    local_coords(P, (int)gc - P.cell_base, cx, cy, cz);
-    for (int k = 0; k < P.gridAdjCnt; k++) {
-        uint32_t up;
-        const int lc = reverse_cell(P, cx, cy, cz, k, up);
-        if (lc < 0) continue;
-        if (PRUNE && (my_code & up) != up) continue;   // too far from those upper faces
-        const int cell = P.cell_base + lc;
-        const uint32_t o0 = off[cell], o1 = o0 + cnt[cell];
-        for (uint32_t o = o0; o < o1; o++) {
-            const float4 q = pos[o];
-            if (PRUNE && ((__float_as_uint(q.w) >> 3) & up) != up) continue;
-            const float3 D = sub3(xyz(q), X);
-            const float dsq = D.x * D.x + D.y * D.y + D.z * D.z;
-            if (!(dsq < P.rd2 && dsq > 0.0f)) continue;
-            const float3 fo = xyz(fb[o]);
-            const float3 dE = sub3(Ev, xyz(veval[o]));
-            const PairAdj a = pair_adjoint(P, D, dE, dsq, rho[o], rs, fo);
-            xacc.x -= a.dD.x; xacc.y -= a.dD.y; xacc.z -= a.dD.z;
-            eacc.x += a.eB * fo.x; eacc.y += a.eB * fo.y; eacc.z += a.eB * fo.z;
-            racc += a.rho_common - a.SF * a.B / rs;
+    if (active && nrev > hcap) {
+        RevIter it;
+        rev_begin<PRUNE>(it, P, gc, my_code, true);
+        uint32_t q;
+        while (rev_next<PRUNE>(it, P, off, cnt, lobits, q)) {
+            const float4 qp = pos[q];
+            const float dsq = dsq_rn(qp.x - X.x, qp.y - X.y, qp.z - X.z);
+            if (dsq < P.rd2 && dsq > 0.0f) adj_pair(P, acc, X, Ev, rs, fs, irs, q | kRevFlag, pos, veval, rr, fb);
         }
     }
+
+    if (s >= n) return;
+    const uint32_t dst = src[s];
+    revcnt[s] = nrev;
+    if (!active) {
+        e_out[dst] = ea[s];
+        rb[s] = 0.0f;
+        pc[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
     const float4 x0 = xa[s], e0 = ea[s];
-    xa[s] = make_float4(x0.x + xacc.x, x0.y + xacc.y, x0.z + xacc.z, 0.f);
-    e_out[dst] = make_float4(e0.x + eacc.x, e0.y + eacc.y, e0.z + eacc.z, 0.f);
-    rb[s] = racc;
-    pc[s] = make_float4(g_visc, g_rest, g_stiff, 0.f);
+    xa[s] = make_float4(x0.x + acc.x.x, x0.y + acc.x.y, x0.z + acc.x.z, 0.f);
+    e_out[dst] = make_float4(e0.x + acc.e.x, e0.y + acc.e.y, e0.z + acc.e.z, 0.f);
+    rb[s] = acc.r;
+    pc[s] = make_float4(acc.gv, acc.gr, acc.gk, 0.f);
 }
 
 // Reverse of computePressure for point s: rho_o = m poly6 sum w^3 with
 // w = (rd2 - |D|^2) d2 gives dL/dD = -6 d2 w^2 (m poly6 dL/drho_o) D for
-// every pair of owner o. Own and reverse pairs as in k_adj_force; the
-// finished dL/dX goes through the permutation.
-template <bool PRUNE, bool BATCH>
+// every pair of owner o. Own pairs from the density pass's list (those in
+// the point's own cell are reverse pairs too), reverse pairs in the other
+// cells from the list k_adj_force recorded (a walk where either list
+// overflowed); the finished dL/dX goes through the permutation.
+template <bool PRUNE>
 __global__ void __launch_bounds__(kAdjThreads)
 k_adj_density(const __grid_constant__ DevParams P0, const SceneTab T, int n,
               const float4 *__restrict__ pos, const uint32_t *__restrict__ gcell,
               const uint32_t *__restrict__ off, const uint32_t *__restrict__ cnt,
               const uint32_t *__restrict__ upbits, const uint32_t *__restrict__ hitlist,
-              const uint32_t *__restrict__ hitcnt, const uint32_t *__restrict__ src,
+              const uint32_t *__restrict__ hitcnt, const uint32_t *__restrict__ revlist,
+              const uint32_t *__restrict__ revcnt, const uint32_t *__restrict__ src,
               const float *__restrict__ rb, const float4 *__restrict__ xa, float4 *__restrict__ x_out) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
-    const DevParams &P = BATCH ? T.params[T.point_scene[s]] : P0;
+    const DevParams &P = scene_params(P0, T, s);
     const uint32_t gc = gcell[s];
     const uint32_t dst = src[s];
     const float4 x0 = xa[s];
@@ -375,50 +550,57 @@ k_adj_density(const __grid_constant__ DevParams P0, const SceneTab T, int n,
     const float kmp = -6.0f * P.d2 * P.pmass * P.poly6kern;
     const float gs = kmp * rb[s];
     float3 xacc = make_float3(0.f, 0.f, 0.f);
+    // own pair (owner s): + gs w^2 (X_s - X_j)
     auto own = [&](uint32_t j) {
-        const float3 D = sub3(X, xyz(pos[j]));
-        const float dsq = D.x * D.x + D.y * D.y + D.z * D.z;
-        const float w = (P.rd2 - dsq) * P.d2;
+        const float4 q = pos[j];
+        const float3 D = make_float3(X.x - q.x, X.y - q.y, X.z - q.z);
+        const float w = (P.rd2 - (D.x * D.x + D.y * D.y + D.z * D.z)) * P.d2;
         const float k = gs * w * w;
         xacc.x += k * D.x; xacc.y += k * D.y; xacc.z += k * D.z;
     };
+    // reverse pair (owner o): - g_o w^2 (X_o - X_s)
+    auto rev = [&](uint32_t o) {
+        const float4 q = pos[o];
+        const float3 D = make_float3(q.x - X.x, q.y - X.y, q.z - X.z);
+        const float w = (P.rd2 - (D.x * D.x + D.y * D.y + D.z * D.z)) * P.d2;
+        const float k = kmp * rb[o] * w * w;
+        xacc.x -= k * D.x; xacc.y -= k * D.y; xacc.z -= k * D.z;
+    };
+    // own pairs; those in the own cell are reverse pairs as well
+    const uint32_t c_lo = off[gc], c_hi = c_lo + cnt[gc];
+    auto both = [&](uint32_t j) {
+        if (gs != 0.0f) own(j);
+        if (j >= c_lo && j < c_hi) rev(j);
+    };
     const uint32_t nh = hitcnt[s];
-    if (gs != 0.0f) {
-        if (nh <= (uint32_t)P.hcap) {
-            for (uint32_t t = 0; t < nh; t++) own(hitlist[list_at(P, s, t)]);
-        } else {
-            const int base = (int)gc - P.nadj;
-            for (int c = 0; c < P.gridAdjCnt; c++) {
-                CandIter it;
-                cand_begin<PRUNE>(it, P, c, base + P.adj[c], my_code, true, off, cnt, upbits);
-                uint32_t j;
-                while (cand_next<PRUNE>(it, P, upbits, j)) {
-                    const float4 q = pos[j];
-                    const float dx = p4.x - q.x, dy = p4.y - q.y, dz = p4.z - q.z;
-                    const float dsq = dx * dx + dy * dy + dz * dz;
-                    if (dsq < P.rd2 && dsq > 0.0f) own(j);
-                }
+    if (nh <= (uint32_t)P.hcap) {
+        for (uint32_t t = 0; t < nh; t++) both(hitlist[list_at(P, s, t)]);
+    } else {
+        const int base = (int)gc - P.nadj;
+        for (int c = 0; c < P.gridAdjCnt; c++) {
+            CandIter it;
+            cand_begin<PRUNE>(it, P, c, base + P.adj[c], my_code, true, off, cnt, upbits);
+            uint32_t j;
+            while (cand_next<PRUNE>(it, P, upbits, j)) {
+                const float4 q = pos[j];
+                const float dsq = dsq_rn(p4.x - q.x, p4.y - q.y, p4.z - q.z);
+                if (dsq < P.rd2 && dsq > 0.0f) both(j);
             }
         }
     }
-    int cx, cy, cz;
-    local_coords(P, (int)gc - P.cell_base, cx, cy, cz);
-    for (int k = 0; k < P.gridAdjCnt; k++) {
-        uint32_t up;
-        const int lc = reverse_cell(P, cx, cy, cz, k, up);
-        if (lc < 0) continue;
-        if (PRUNE && (my_code & up) != up) continue;
-        const int cell = P.cell_base + lc;
-        const uint32_t o0 = off[cell], o1 = o0 + cnt[cell];
-        for (uint32_t o = o0; o < o1; o++) {
+    // reverse pairs in the other cells: the force adjoint's list, or a walk
+    const uint32_t nr = revcnt[s];
+    if (nr <= (uint32_t)P.hcap) {
+        for (uint32_t t = 0; t < nr; t++) rev(revlist[list_at(P, s, t)]);
+    } else {
+        const uint32_t *lobits = upbits + 3 * (size_t)P.upwords;
+        RevIter it;
+        rev_begin<PRUNE>(it, P, gc, my_code, true);
+        uint32_t o;
+        while (rev_next<PRUNE>(it, P, off, cnt, lobits, o)) {
             const float4 q = pos[o];
-            if (PRUNE && ((__float_as_uint(q.w) >> 3) & up) != up) continue;
-            const float3 D = sub3(xyz(q), X);
-            const float dsq = D.x * D.x + D.y * D.y + D.z * D.z;
-            if (!(dsq < P.rd2 && dsq > 0.0f)) continue;
-            const float w = (P.rd2 - dsq) * P.d2;
-            const float k2 = kmp * rb[o] * w * w;
-            xacc.x -= k2 * D.x; xacc.y -= k2 * D.y; xacc.z -= k2 * D.z;
+            const float dsq = dsq_rn(q.x - X.x, q.y - X.y, q.z - X.z);
+            if (dsq < P.rd2 && dsq > 0.0f) rev(o);
         }
     }
     x_out[dst] = make_float4(x0.x + xacc.x, x0.y + xacc.y, x0.z + xacc.z, 0.f);
@@ -456,12 +638,15 @@ k_param_partial(const float4 *__restrict__ pc, const int *__restrict__ sbase, co
 
 __global__ void k_param_final(int nscenes, int nchunks, const double *__restrict__ partial,
                               double *__restrict__ acc) {
-    const int scene = blockIdx.x * blockDim.x + threadIdx.x;
+    // one warp per scene: lane l takes chunks l, l+32, ...; fixed shuffle tree
+    const int scene = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (scene >= nscenes) return;
+    const unsigned lane = threadIdx.x & 31u;
     for (int j = 0; j < 3; j++) {
         double t = 0.0;
-        for (int c = 0; c < nchunks; c++) t += partial[((size_t)scene * nchunks + c) * 3 + j];
-        acc[scene * 3 + j] += t;
+        for (int c = (int)lane; c < nchunks; c += 32) t += partial[((size_t)scene * nchunks + c) * 3 + j];
+        for (int d = 16; d > 0; d >>= 1) t += __shfl_xor_sync(0xffffffffu, t, d);
+        if (lane == 0) acc[scene * 3 + j] += t;
     }
 }
 
@@ -474,47 +659,72 @@ __global__ void k_compose(int n, const uint32_t *__restrict__ src, const uint32_
     out[s] = src ? (in ? in[src[s]] : src[s]) : (uint32_t)s;
 }
 
+// Up to three float4 arrays copied in one pass (tape saves and restores):
+// dst_k[i] = src_k[i] for k < count.
+struct Copy3 {
+    const float4 *src[3];
+    float4 *dst[3];
+    int count;
+};
+
+__global__ void __launch_bounds__(kThreads) k_copy3(int n, const __grid_constant__ Copy3 c) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int k = 0; k < c.count; k++) c.dst[k][i] = c.src[k][i];
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
 // Launch wrappers.
 
+int fl_launch_copy3(fl_system *s, int n, int count, const float4 *const *src, float4 *const *dst) {
+    if (n == 0 || count == 0) return FL_OK;
+    Copy3 c = {};
+    c.count = count;
+    for (int k = 0; k < count && k < 3; k++) { c.src[k] = src[k]; c.dst[k] = dst[k]; }
+    k_copy3<<<blocks_for(n, kThreads), kThreads, 0, s->stream>>>(n, c);
+    FL_LAUNCH_CHECK("copy3");
+    return FL_OK;
+}
+
 static bool adj_prune(const fl_system *s) { return s->D.prune && s->codes_valid; }
 
-int fl_launch_adj_advance(fl_system *s, const float *time_ptr, const float4 *xo_b, const float4 *vo_b,
-                          const float4 *eo_b, float4 *xa, float4 *ea, float4 *fb, float4 *v_out) {
+int fl_launch_adj_advance(fl_system *s, const float *time_ptr, const float4 *force, const float4 *xo_b,
+                          const float4 *vo_b, const float4 *eo_b, float4 *xa, float4 *ea, float4 *fb, float4 *v_out,
+                          float2 *rr) {
     if (s->n == 0) return FL_OK;
-    auto kern = s->batched ? k_adj_advance<true> : k_adj_advance<false>;
-    kern<<<blocks_for(s->n, kAdjThreads), kAdjThreads, 0, s->stream>>>(
+    k_adj_advance<<<blocks_for(s->n, kAdjThreads), kAdjThreads, 0, s->stream>>>(
         s->D, fl_scene_tab(s), s->n, time_ptr, s->P.dt, s->f[F_GCELL].cur<uint32_t>(), s->src,
         s->f[F_POS].cur<float4>(), s->f[F_VEL].cur<float4>(), s->f[F_VEVAL].cur<float4>(),
-        s->f[F_FORCE].cur<float4>(), xo_b, vo_b, eo_b, xa, ea, fb, v_out);
+        force, s->f[F_PRESS].cur<float>(), xo_b, vo_b, eo_b, xa, ea, fb, v_out, rr);
     FL_LAUNCH_CHECK("adj_advance");
     return FL_OK;
 }
 
-int fl_launch_adj_force(fl_system *s, const float4 *fb, float4 *xa, const float4 *ea, float *rb, float4 *pc,
-                        float4 *e_out) {
+int fl_launch_adj_force(fl_system *s, const float2 *rr, const float4 *fb, float4 *xa, const float4 *ea, float *rb,
+                        float4 *pc, float4 *e_out, uint32_t *revlist, uint32_t *revcnt) {
     if (s->n == 0) return FL_OK;
+    if (s->max_points > (int)kSlotMask)
+        return fl_fail(FL_ERR_CAPACITY, "adjoint: %d points (at most %u)", s->max_points, kSlotMask);
     const bool pr = adj_prune(s);
-    auto kern = s->batched ? (pr ? k_adj_force<true, true> : k_adj_force<false, true>)
-                           : (pr ? k_adj_force<true, false> : k_adj_force<false, false>);
+    auto kern = pr ? k_adj_force<true> : k_adj_force<false>;
     kern<<<blocks_for(s->n, kAdjThreads), kAdjThreads, 0, s->stream>>>(
         s->D, fl_scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->f[F_VEVAL].cur<float4>(),
-        s->f[F_PRESS].cur<float>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt, s->upbits, s->hitlist,
-        s->hitcnt, s->src, fb, xa, ea, rb, pc, e_out);
+        rr, s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt, s->upbits, s->hitlist,
+        s->hitcnt, s->src, fb, xa, ea, rb, pc, e_out, revlist, revcnt);
     FL_LAUNCH_CHECK("adj_force");
     return FL_OK;
 }
 
-int fl_launch_adj_density(fl_system *s, const float *rb, const float4 *xa, float4 *x_out) {
+int fl_launch_adj_density(fl_system *s, const uint32_t *revlist, const uint32_t *revcnt, const float *rb,
+                          const float4 *xa, float4 *x_out) {
     if (s->n == 0) return FL_OK;
     const bool pr = adj_prune(s);
-    auto kern = s->batched ? (pr ? k_adj_density<true, true> : k_adj_density<false, true>)
-                           : (pr ? k_adj_density<true, false> : k_adj_density<false, false>);
+    auto kern = pr ? k_adj_density<true> : k_adj_density<false>;
     kern<<<blocks_for(s->n, kAdjThreads), kAdjThreads, 0, s->stream>>>(
         s->D, fl_scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->f[F_GCELL].cur<uint32_t>(), s->off,
-        s->cnt, s->upbits, s->hitlist, s->hitcnt, s->src, rb, xa, x_out);
+        s->cnt, s->upbits, s->hitlist, s->hitcnt, revlist, revcnt, s->src, rb, xa, x_out);
     FL_LAUNCH_CHECK("adj_density");
     return FL_OK;
 }
@@ -529,7 +739,7 @@ int fl_launch_param_reduce(fl_system *s, const float4 *pc, const int *sbase, con
     dim3 grid((unsigned)nchunks, (unsigned)s->nscenes);
     k_param_partial<<<grid, kReduceThreads, 0, s->stream>>>(pc, sbase, sn, nchunks, partial);
     FL_LAUNCH_CHECK("param_partial");
-    k_param_final<<<blocks_for(s->nscenes, 128), 128, 0, s->stream>>>(s->nscenes, nchunks, partial, acc);
+    k_param_final<<<blocks_for(s->nscenes, 4), 128, 0, s->stream>>>(s->nscenes, nchunks, partial, acc);
     FL_LAUNCH_CHECK("param_final");
     return FL_OK;
 }

@@ -19,7 +19,7 @@
 
 // Pairs the density pass records per point for the force pass (HBM: 4 B
 // per entry, 192 B per point of capacity).
-static const int kPairListCap = 48;
+static const int kPairListCap = 128;
 
 // ---------------------------------------------------------------------------
 // errors
@@ -200,7 +200,8 @@ extern "C" int fl_create(const fl_params *p, int max_points, fl_system **out) {
         if ((r = fl_dalloc((void **)&s->rank_tmp, 4 * np)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&s->src, 4 * np)) != FL_OK) break;
         s->D.upwords = (int)((np + 31) / 32 + 1);
-        if ((r = fl_dalloc((void **)&s->upbits, fl_upbits_bytes(s))) != FL_OK) break;
+        // rows 0-2: upper-band flags; rows 3-5: lower-band flags (adjoint only)
+        if ((r = fl_dalloc((void **)&s->upbits, 2 * fl_upbits_bytes(s))) != FL_OK) break;
         s->D.hcap = kPairListCap;
         if ((r = fl_dalloc((void **)&s->hitlist, 4 * ((np + 31) / 32) * 32 * (size_t)kPairListCap)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&s->hitcnt, 4 * np)) != FL_OK) break;
@@ -748,10 +749,9 @@ int fl_recompute_step(fl_system *s) {
     FL_TRY(fl_launch_insert(s, nullptr));
     FL_TRY(fl_launch_scan(s, s->gcells, 0));
     FL_TRY(fl_launch_scatter_index(s));
-    FL_TRY(fl_launch_sort_cells(s, 1));
+    FL_TRY(fl_launch_sort_cells(s, 2));
     flip(s, F_POS); flip(s, F_VEL); flip(s, F_VEVAL); flip(s, F_CLR); flip(s, F_GCELL); flip(s, F_GNDX);
     FL_TRY(fl_launch_density(s));
-    FL_TRY(fl_launch_force(s));
     return FL_OK;
 }
 
@@ -773,9 +773,9 @@ static TimingState *active_timing(fl_system *s) {
 static int begin_run(fl_system *s) {
     if (!s->time_host_valid) return FL_OK;
     // host time is authoritative: publish it to the slot the next step reads
-    FL_CUDA_TRY(cudaMemcpyAsync(s->time_dev + s->time_slot, &s->time, sizeof(float),
-                                cudaMemcpyHostToDevice, s->stream));
-    return FL_OK;
+    // (as a kernel argument: a copy from pageable host memory could make the
+    // host wait for the stream)
+    return fl_launch_set_time(s, s->time_slot, s->time);
 }
 
 extern "C" int fl_run(fl_system *s) {

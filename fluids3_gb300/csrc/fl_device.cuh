@@ -59,6 +59,8 @@ __device__ __forceinline__ uint32_t band_code(const DevParams &P, int c, float4 
 // Upper-band flags of the sorted slots, one bit per slot and axis:
 // upbits[axis * upwords + (slot >> 5)] bit (slot & 31). Published by the
 // 32 lanes of a warp for 32 consecutive slots base + lane (all lanes call).
+// The adjoint's rebuilt steps also publish the lower-band flags (code bits
+// 3-5) into rows 3-5 the same way (upbits + 3 * upwords, `code >> 3`).
 __device__ __forceinline__ void publish_upbits(const DevParams &P, uint32_t *upbits, uint32_t base,
                                                uint32_t code, bool valid) {
     const unsigned lane = threadIdx.x & 31u;

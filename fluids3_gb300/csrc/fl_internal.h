@@ -114,8 +114,9 @@ struct fl_system {
     uint32_t *dev_err;     // device error word (FL_DEV_*)
 
     // per sorted slot and axis: is the point within `band` of its cell's
-    // upper face (3 rows of upwords 32-bit words); valid together with the
-    // band codes in pos.w while codes_valid is set
+    // upper face (rows 0-2 of upwords 32-bit words); valid together with the
+    // band codes in pos.w while codes_valid is set. Rows 3-5: the same for
+    // the lower face, filled only by the adjoint's rebuilt steps (sort mode 2)
     uint32_t *upbits;
     int codes_valid;
 
@@ -183,8 +184,9 @@ int fl_ensure_stage(fl_system *s, size_t bytes);
 void fl_reset_progress(fl_system *s);
 // One fused Run step reading the device time slot (no timing events).
 int fl_step_fused(fl_system *s);
-// The forward state of one step short of the advance: insert, scan, sort
-// (gathering pos/vel/veval/clr), density and force into the live copies.
+// The forward state of one step up to its densities: insert, scan, sort
+// (gathering pos/vel/veval/clr, publishing both band-flag sets) and density
+// (with pair lists) into the live copies.
 int fl_recompute_step(fl_system *s);
 
 // ---- adjoint tape (fl_tape.cpp) --------------------------------------------
@@ -197,20 +199,25 @@ void fl_tape_touch(fl_system *s);
 void fl_tape_free(fl_system *s);
 
 // ---- launch wrappers (fl_kernels.cu, fl_scan.cu, fl_adjoint.cu) ------------
-int fl_launch_adj_advance(fl_system *s, const float *time_ptr, const float4 *xo_b, const float4 *vo_b,
-                          const float4 *eo_b, float4 *xa, float4 *ea, float4 *fb, float4 *v_out);
-int fl_launch_adj_force(fl_system *s, const float4 *fb, float4 *xa, const float4 *ea, float *rb, float4 *pc,
-                        float4 *e_out);
-int fl_launch_adj_density(fl_system *s, const float *rb, const float4 *xa, float4 *x_out);
+int fl_launch_adj_advance(fl_system *s, const float *time_ptr, const float4 *force, const float4 *xo_b,
+                          const float4 *vo_b, const float4 *eo_b, float4 *xa, float4 *ea, float4 *fb, float4 *v_out,
+                          float2 *rr);
+int fl_launch_adj_force(fl_system *s, const float2 *rr, const float4 *fb, float4 *xa, const float4 *ea, float *rb,
+                        float4 *pc, float4 *e_out, uint32_t *revlist, uint32_t *revcnt);
+int fl_launch_adj_density(fl_system *s, const uint32_t *revlist, const uint32_t *revcnt, const float *rb,
+                          const float4 *xa, float4 *x_out);
 int fl_param_chunks(int max_scene_points);
 int fl_launch_param_reduce(fl_system *s, const float4 *pc, const int *sbase, const int *sn, int nchunks,
                            double *partial, double *acc);
 int fl_launch_compose(fl_system *s, int n, const uint32_t *src, const uint32_t *in, uint32_t *out);
+// dst[k][0..n) = src[k][0..n) for k < count (<= 3), one kernel pass
+int fl_launch_copy3(fl_system *s, int n, int count, const float4 *const *src, float4 *const *dst);
 int fl_launch_insert(fl_system *s, uint32_t *gcell_pre_or_null);
 int fl_launch_scan(fl_system *s, int count, int clear_status);
 int fl_launch_scatter_index(fl_system *s);
 // mode 0: rank only (sorted src + canonical gndx into f[F_GNDX].cur, pre-sort order)
 // mode 1: fused rank + gather of pos/vel/veval/clr/gcell/gndx into the nxt copies
+// mode 2: mode 1 that also publishes the lower-band slot flags (upbits rows 3-5)
 int fl_launch_sort_cells(fl_system *s, int mode);
 // gather every field cur -> nxt through src (phase-API counting sort)
 int fl_launch_gather_all(fl_system *s);
@@ -220,6 +227,7 @@ int fl_launch_force(fl_system *s);
 int fl_launch_force_advance(fl_system *s, float dt);
 int fl_launch_advance(fl_system *s, float time, float dt, float ss);
 int fl_launch_pack3(fl_system *s, const float4 *src, float *dst, int n);
+int fl_launch_set_time(fl_system *s, int slot, float value);
 int fl_launch_unpack3(fl_system *s, const float *src, float4 *dst, int n);
 int fl_launch_grid_identity(fl_system *s, uint32_t *dst, int n, const uint32_t *gcell);
 int fl_launch_gcell_ref(fl_system *s, uint32_t *dst);

@@ -159,7 +159,8 @@ __device__ __forceinline__ void emit_range(const SortArgs &a, const CellCtx &cx,
         const bool valid = k < m;
         uint32_t code = 0;
         if (valid) code = emit_slot<MODE>(a, cx, o, k, a.src[o + k]);
-        if (MODE == 1 && a.prune) publish_upbits(*cx.P, a.upbits, o + kb, code, valid);
+        if (MODE >= 1 && a.prune) publish_upbits(*cx.P, a.upbits, o + kb, code, valid);
+        if (MODE == 2 && a.prune) publish_upbits(*cx.P, a.upbits + 3 * (size_t)cx.P->upwords, o + kb, code >> 3, valid);
     }
 }
 
@@ -179,7 +180,8 @@ __device__ __forceinline__ void sort_segment(const SortArgs &a, const CellCtx &c
             a.src[o + lane] = v[0];   // canonical src in both modes (the adjoint reads it)
             code = emit_slot<MODE>(a, cx, o, lane, v[0]);
         }
-        if (MODE == 1 && a.prune) publish_upbits(*cx.P, a.upbits, o, code, lane < m);
+        if (MODE >= 1 && a.prune) publish_upbits(*cx.P, a.upbits, o, code, lane < m);
+        if (MODE == 2 && a.prune) publish_upbits(*cx.P, a.upbits + 3 * (size_t)cx.P->upwords, o, code >> 3, lane < m);
     } else {
 #pragma unroll
         for (int r = 0; r < K; r++) {
@@ -637,6 +639,8 @@ k_force_advance(const __grid_constant__ DevParams P0, const SceneTab T, int n, f
 }
 
 // ---------------------------------------------------------------------------
+__global__ void k_set_time(float *time_dev, float value) { *time_dev = value; }
+
 __global__ void k_pack3(int n, const float4 *__restrict__ src, float *__restrict__ dst) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -717,7 +721,7 @@ int fl_launch_sort_cells(fl_system *s, int mode) {
     a.gcells = s->gcells;
     a.P = s->D;
     a.T = fl_scene_tab(s);
-    a.prune = (mode == 1) ? s->D.prune : 0;
+    a.prune = (mode >= 1) ? s->D.prune : 0;
     a.upbits = s->upbits;
     const int warps_per_block = kThreads / 32;
     const int grid = blocks_for((long long)s->gcells, warps_per_block);
@@ -732,8 +736,10 @@ int fl_launch_sort_cells(fl_system *s, int mode) {
         a.clr_in = s->f[F_CLR].cur<uint32_t>(); a.clr_out = s->f[F_CLR].nxt<uint32_t>();
         a.gcell_out = s->f[F_GCELL].nxt<uint32_t>();
         a.gndx_out = s->f[F_GNDX].nxt<uint32_t>();
-        if (a.prune) FL_CUDA_TRY(cudaMemsetAsync(s->upbits, 0, fl_upbits_bytes(s), s->stream));
-        auto kern = s->batched ? k_sort_cells<1, true> : k_sort_cells<1, false>;
+        if (a.prune)
+            FL_CUDA_TRY(cudaMemsetAsync(s->upbits, 0, (mode == 2 ? 2 : 1) * fl_upbits_bytes(s), s->stream));
+        auto kern = (mode == 2) ? (s->batched ? k_sort_cells<2, true> : k_sort_cells<2, false>)
+                                : (s->batched ? k_sort_cells<1, true> : k_sort_cells<1, false>);
         kern<<<grid, kThreads, 0, s->stream>>>(a);
         s->codes_valid = s->D.prune;
     }
@@ -834,6 +840,12 @@ int fl_launch_advance(fl_system *s, float time, float dt, float ss) {
         s->D, fl_scene_tab(s), s->n, time, dt, ss, s->f[F_GCELL].cur<uint32_t>(), s->f[F_FORCE].cur<float4>(),
         s->f[F_POS].cur<float4>(), s->f[F_VEL].cur<float4>(), s->f[F_VEVAL].cur<float4>());
     FL_LAUNCH_CHECK("advance");
+    return FL_OK;
+}
+
+int fl_launch_set_time(fl_system *s, int slot, float value) {
+    k_set_time<<<1, 1, 0, s->stream>>>(s->time_dev + slot, value);
+    FL_LAUNCH_CHECK("set_time");
     return FL_OK;
 }
 

@@ -1,19 +1,21 @@
 // Adjoint tape and reverse pass of the fused step (no counterpart in the
 // reference, whose step has no derivative).
 //
-// While a tape is open every Run step (fl_run, fl_run_steps) first saves
-// what its reverse needs that cannot be rebuilt: the state before the step
-// (position, velocity, evaluated velocity: 48 B per point) every `every`
-// steps, and the step's time. fl_backward then walks the steps last to
-// first. For each step it rebuilds the forward state -- the sort, the
-// densities, the forces -- from the saved state (replaying the fused steps
-// of a checkpoint segment into a segment buffer when every > 1) and runs
-// the adjoint kernels (fl_adjoint.cu). Everything is deterministic, so the
-// rebuilt state is the recorded step's, bit for bit.
+// While a tape is open every Run step (fl_run, fl_run_steps) saves what
+// its reverse needs: the state before the step (position, velocity,
+// evaluated velocity: 48 B per point) every `every` steps, the step's time,
+// and with every = 1 the step's SPH force (16 B per point). fl_backward
+// then walks the steps last to first. With every > 1 it first replays each
+// checkpoint segment's fused steps, saving every step's state and force in
+// segment buffers. For each step it rebuilds the sort and the densities
+// (with their pair lists) from the saved state and runs the adjoint kernels
+// (fl_adjoint.cu). Everything is deterministic, so the rebuilt values are
+// the recorded step's, bit for bit.
 //
-// Device memory: ceil(max_steps / every) checkpoints plus `every` segment
-// slots (every > 1) of 48 B per point, and ~250 B per point of adjoint
-// buffers, identity maps and the saved final state.
+// Device memory: ceil(max_steps / every) checkpoints of 48 B per point;
+// with every = 1, 16 B per point per step of forces, else `every` segment
+// slots of 64 B per point; and ~450 B per point of adjoint buffers,
+// reverse-pair lists, identity maps and the saved final state.
 #include <stdlib.h>
 #include <string.h>
 
@@ -25,6 +27,7 @@ struct fl_tape {
     int nck;
     float4 *ck;             // nck x {pos, vel, veval} x cap
     float4 *seg;            // every x {pos, vel, veval} x cap (every > 1)
+    float4 *force;          // per step of the tape (every = 1) or of a segment: the step's SPH force
     float *time;            // per recorded step: the time it read
     uint32_t *ident[2];     // per current slot: the point's index when recording began
     int ident_cur;
@@ -32,6 +35,8 @@ struct fl_tape {
     int gcur;
     float4 *xa, *ea, *fb, *pc;
     float *rb;
+    float2 *rr;                   // per slot: density and its reciprocal
+    uint32_t *revlist, *revcnt;   // reverse pairs found by the force adjoint, for the density adjoint
     int nchunks;
     double *partial, *acc;  // per-scene parameter gradients (visc, rest density, IntStiff)
     int *sbase, *sn;
@@ -41,12 +46,13 @@ struct fl_tape {
 
 static void tape_release(fl_tape *t) {
     if (!t) return;
-    cudaFree(t->ck); cudaFree(t->seg); cudaFree(t->time);
+    cudaFree(t->ck); cudaFree(t->seg); cudaFree(t->force); cudaFree(t->time);
     for (int k = 0; k < 2; k++) {
         cudaFree(t->ident[k]);
         for (int j = 0; j < 3; j++) cudaFree(t->g[k][j]);
     }
     cudaFree(t->xa); cudaFree(t->ea); cudaFree(t->fb); cudaFree(t->pc); cudaFree(t->rb);
+    cudaFree(t->revlist); cudaFree(t->revcnt); cudaFree(t->rr);
     cudaFree(t->partial); cudaFree(t->acc); cudaFree(t->sbase); cudaFree(t->sn);
     for (int k = 0; k < F_COUNT; k++) cudaFree(t->save[k]);
     cudaFree(t->save_time);
@@ -66,25 +72,24 @@ void fl_tape_touch(fl_system *s) {
     if (s && s->tape && s->tape->steps > 0) s->tape->broken = 1;
 }
 
-// The live (pos, vel, veval) copies to / from a {pos, vel, veval} x cap block.
+// The live (pos, vel, veval) copies to / from a {pos, vel, veval} x cap
+// block, in one kernel pass.
 static int save_state(fl_system *s, const fl_tape *t, float4 *dst) {
-    const size_t bytes = 16 * (size_t)s->n;
-    if (!bytes) return FL_OK;
-    const int ids[3] = {F_POS, F_VEL, F_VEVAL};
-    for (int k = 0; k < 3; k++)
-        FL_CUDA_TRY(cudaMemcpyAsync(dst + (size_t)k * t->cap, s->f[ids[k]].cur<void>(), bytes,
-                                    cudaMemcpyDeviceToDevice, s->stream));
-    return FL_OK;
+    const float4 *src[3] = {s->f[F_POS].cur<float4>(), s->f[F_VEL].cur<float4>(), s->f[F_VEVAL].cur<float4>()};
+    float4 *out[3] = {dst, dst + t->cap, dst + 2 * (size_t)t->cap};
+    return fl_launch_copy3(s, s->n, 3, src, out);
 }
 
-static int load_state(fl_system *s, const fl_tape *t, const float4 *src) {
-    const size_t bytes = 16 * (size_t)s->n;
-    if (!bytes) return FL_OK;
-    const int ids[3] = {F_POS, F_VEL, F_VEVAL};
-    for (int k = 0; k < 3; k++)
-        FL_CUDA_TRY(cudaMemcpyAsync(s->f[ids[k]].cur<void>(), src + (size_t)k * t->cap, bytes,
-                                    cudaMemcpyDeviceToDevice, s->stream));
-    return FL_OK;
+static int load_state(fl_system *s, const fl_tape *t, const float4 *blk) {
+    const float4 *src[3] = {blk, blk + t->cap, blk + 2 * (size_t)t->cap};
+    float4 *out[3] = {s->f[F_POS].cur<float4>(), s->f[F_VEL].cur<float4>(), s->f[F_VEVAL].cur<float4>()};
+    return fl_launch_copy3(s, s->n, 3, src, out);
+}
+
+static int save_force(fl_system *s, float4 *dst) {
+    const float4 *src[1] = {s->f[F_FORCE].cur<float4>()};
+    float4 *out[1] = {dst};
+    return fl_launch_copy3(s, s->n, 1, src, out);
 }
 
 extern "C" int fl_tape_begin(fl_system *s, int max_steps, int every) {
@@ -110,6 +115,7 @@ extern "C" int fl_tape_begin(fl_system *s, int max_steps, int every) {
     do {
         if ((r = fl_dalloc((void **)&t->ck, 48 * cap * (size_t)t->nck)) != FL_OK) break;
         if (every > 1 && (r = fl_dalloc((void **)&t->seg, 48 * cap * (size_t)every)) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&t->force, 16 * cap * (size_t)(every > 1 ? every : max_steps))) != FL_OK) break;
         if ((r = fl_dalloc((void **)&t->time, 4 * (size_t)max_steps)) != FL_OK) break;
         for (int k = 0; k < 2 && r == FL_OK; k++) {
             r = fl_dalloc((void **)&t->ident[k], 4 * cap);
@@ -121,6 +127,9 @@ extern "C" int fl_tape_begin(fl_system *s, int max_steps, int every) {
         if ((r = fl_dalloc((void **)&t->fb, 16 * cap)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&t->pc, 16 * cap)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&t->rb, 4 * cap)) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&t->revcnt, 4 * cap)) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&t->rr, 8 * cap)) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&t->revlist, 4 * ((cap + 31) / 32) * 32 * (size_t)s->D.hcap)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&t->partial, 24 * (size_t)s->nscenes * t->nchunks)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&t->acc, 24 * (size_t)s->nscenes)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&t->sbase, 4 * (size_t)s->nscenes)) != FL_OK) break;
@@ -165,6 +174,9 @@ int fl_tape_pre_step(fl_system *s) {
 int fl_tape_post_step(fl_system *s) {
     fl_tape *t = s->tape;
     if (t->broken) return FL_OK;
+    // every = 1: keep the step's force (sorted order) so the reverse pass
+    // need not recompute it
+    if (t->every == 1) FL_TRY(save_force(s, t->force + (size_t)t->steps * t->cap));
     FL_TRY(fl_launch_compose(s, s->n, s->src, t->steps == 0 ? nullptr : t->ident[t->ident_cur],
                              t->ident[t->ident_cur ^ 1]));
     t->ident_cur ^= 1;
@@ -211,15 +223,15 @@ static int download_vec3(fl_system *s, const float4 *src, float *dst) {
     return FL_OK;
 }
 
-// The reverse of recorded step k from its saved state.
-static int backward_step(fl_system *s, fl_tape *t, const float4 *state, int k) {
+// The reverse of recorded step k from its saved state and force.
+static int backward_step(fl_system *s, fl_tape *t, const float4 *state, const float4 *force, int k) {
     FL_TRY(load_state(s, t, state));
     FL_TRY(fl_recompute_step(s));
     const int c = t->gcur, x = c ^ 1;
-    FL_TRY(fl_launch_adj_advance(s, t->time + k, t->g[c][0], t->g[c][1], t->g[c][2], t->xa, t->ea, t->fb,
-                                 t->g[x][1]));
-    FL_TRY(fl_launch_adj_force(s, t->fb, t->xa, t->ea, t->rb, t->pc, t->g[x][2]));
-    FL_TRY(fl_launch_adj_density(s, t->rb, t->xa, t->g[x][0]));
+    FL_TRY(fl_launch_adj_advance(s, t->time + k, force, t->g[c][0], t->g[c][1], t->g[c][2], t->xa, t->ea,
+                                 t->fb, t->g[x][1], t->rr));
+    FL_TRY(fl_launch_adj_force(s, t->rr, t->fb, t->xa, t->ea, t->rb, t->pc, t->g[x][2], t->revlist, t->revcnt));
+    FL_TRY(fl_launch_adj_density(s, t->revlist, t->revcnt, t->rb, t->xa, t->g[x][0]));
     FL_TRY(fl_launch_param_reduce(s, t->pc, t->sbase, t->sn, t->nchunks, t->partial, t->acc));
     t->gcur = x;
     return FL_OK;
@@ -233,20 +245,21 @@ static int run_reverse(fl_system *s, fl_tape *t) {
         const int t1 = (t0 + t->every < t->steps) ? t0 + t->every : t->steps;
         const float4 *ck = t->ck + (size_t)g * blk;
         if (t->every == 1) {
-            FL_TRY(backward_step(s, t, ck, t0));
+            FL_TRY(backward_step(s, t, ck, t->force + (size_t)t0 * t->cap, t0));
             continue;
         }
         // replay the segment's fused steps from its checkpoint, saving the
-        // state before each
+        // state before each step and the force it computed
         FL_TRY(load_state(s, t, ck));
         for (int k = t0; k < t1; k++) {
             FL_TRY(save_state(s, t, t->seg + (size_t)(k - t0) * blk));
-            if (k + 1 == t1) break;
             FL_CUDA_TRY(cudaMemcpyAsync(s->time_dev + s->time_slot, t->time + k, sizeof(float),
                                         cudaMemcpyDeviceToDevice, s->stream));
             FL_TRY(fl_step_fused(s));
+            FL_TRY(save_force(s, t->force + (size_t)(k - t0) * t->cap));
         }
-        for (int k = t1 - 1; k >= t0; k--) FL_TRY(backward_step(s, t, t->seg + (size_t)(k - t0) * blk, k));
+        for (int k = t1 - 1; k >= t0; k--)
+            FL_TRY(backward_step(s, t, t->seg + (size_t)(k - t0) * blk, t->force + (size_t)(k - t0) * t->cap, k));
     }
     return FL_OK;
 }
