@@ -9,6 +9,8 @@ positions on any machine (numpy float32 arithmetic is IEEE, no FMA).
 
 Workloads:
   dam_break      32,768 points, 32^3 lattice, box (-30,0,-30)..(30,60,30)
+  dam_break_scaled  the dam break at n points with box and block scaled to
+                 keep its density (65,536: the differentiated rollout)
   wave_tank      4,000,000 points filling the low-x 40% of a ~330-unit box,
                  X- wall forcing at frequency 0.2, amplitude 0.3
   batch_scenes   256 independent scenes, 2,048..65,536 points each
@@ -131,6 +133,35 @@ def dam_break(n: int = 32768, seed: int = 1, steps: int = 100) -> Scene:
     origin = (bmin[0] + 4.0, bmin[1] + 4.0, bmin[2] + 4.0)
     pos = lattice_block(n, origin, side, side, lattice_spacing(), seed)
     return _finish("dam_break_32k" if n == 32768 else f"dam_break_{n}", params, pos, steps, bmin, bmax)
+
+
+def dam_break_scaled(n: int = 65536, seed: int = 4, steps: int = 200) -> Scene:
+    """The dam break scaled to n points at the 32,768-point scene's density:
+    box and block edges grow by k = (n / 32768)^(1/3), the lattice keeps its
+    spacing (round(32 k) points per row, layers stacked to n). At 65,536
+    points: k = 1.26, box (-37.8, 0, -37.8)..(37.8, 75.6, 37.8), 40 x 40
+    points per layer, 41 layers (the last one partial)."""
+    k = (n / 32768.0) ** (1.0 / 3.0)
+    half, height = round(30.0 * k, 1), round(60.0 * k, 1)
+    bmin, bmax = (-half, 0.0, -half), (half, height, half)
+    params = make_params(bmin, bmax)
+    side = int(round(32 * k))
+    origin = (bmin[0] + 4.0 * k, bmin[1] + 4.0 * k, bmin[2] + 4.0 * k)
+    pos = lattice_block(n, origin, side, side, lattice_spacing(), seed)
+    name = "dam_break_65k" if n == 65536 else f"dam_break_scaled_{n}"
+    return _finish(name, params, pos, steps, bmin, bmax)
+
+
+def shifted_target(sc: Scene, frac: float = 0.3, seed: int = 5) -> np.ndarray:
+    """A seeded target cloud: the scene's lattice block re-jittered with
+    another seed and shifted `frac` box widths in +x (world units)."""
+    lo, hi = np.asarray(sc.params.bound_min, np.float64), np.asarray(sc.params.bound_max, np.float64)
+    s = lattice_spacing()
+    rng_jit = (uniform01(seed, 7, sc.n) - np.float32(0.5)) * np.float32(0.1) * s
+    out = sc.pos.astype(np.float64).copy()
+    out[:, 0] += frac * (hi[0] - lo[0])
+    out[:, 1] += rng_jit.astype(np.float64)
+    return out
 
 
 def wave_tank(n: int = 4_000_000, seed: int = 2, steps: int = 1000,

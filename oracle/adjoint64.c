@@ -62,28 +62,38 @@ typedef struct {
     int aclamp, vclamp;
 } AdvTape;
 
-static void walls(const P64 *q, double t, const double *X, const double *E, double *a) {
+/* Branch decisions of one point's advance: bits 0-5 the walls (Y-, Y+, X-,
+ * X+, Z-, Z+) acting, bit 6 the AccelLimit clamp, bit 7 the VelLimit clamp.
+ * mode 0 decides from the values; 1 decides and records into *mk; 2 takes
+ * the recorded decisions (the decisions frozen, as the adjoint treats them). */
+static int decide(int mode, uint8_t *mk, int bit, int cond) {
+    if (mode == 2) return (*mk >> bit) & 1;
+    if (mode == 1) *mk = (uint8_t)((*mk & ~(1u << bit)) | ((cond ? 1u : 0u) << bit));
+    return cond;
+}
+
+static void walls(const P64 *q, double t, const double *X, const double *E, double *a, uint8_t *mk, int mode) {
     double diff, adj, nx, ny, nz;
     diff = q->pr - (X[1] - (q->bmin[1] + (X[0] - q->bmin[0]) * q->slope)) * q->ss;
-    if (diff > EPSD) {
+    if (decide(mode, mk, 0, diff > EPSD)) {
         nx = -q->slope; ny = 1.0 - q->slope; nz = 0.0;
         adj = q->kb * diff - q->damp * (nx * E[0] + ny * E[1] + nz * E[2]);
         a[0] += nx * adj - E[0] * q->fric; a[1] += ny * adj - E[1] * q->fric; a[2] += nz * adj - E[2] * q->fric;
     }
     diff = q->pr - (q->bmax[1] - X[1]) * q->ss;
-    if (diff > EPSD) {
+    if (decide(mode, mk, 1, diff > EPSD)) {
         adj = q->kb * diff - q->damp * (-E[1]);
         a[0] += -E[0] * q->fric; a[1] += -adj - E[1] * q->fric; a[2] += -E[2] * q->fric;
     }
     const double wall = (sin(t * q->wfreq + X[2] / 400.0) * 0.5 + 0.5) * q->wf;
     diff = q->pr - (X[0] - (q->bmin[0] + wall)) * q->ss;
-    if (diff > EPSD) a[0] += wall * q->kb * diff - q->damp * E[0];
+    if (decide(mode, mk, 2, diff > EPSD)) a[0] += wall * q->kb * diff - q->damp * E[0];
     diff = q->pr - (q->bmax[0] - X[0]) * q->ss;
-    if (diff > EPSD) a[0] += -(q->kb * diff - q->damp * (-E[0]));
+    if (decide(mode, mk, 3, diff > EPSD)) a[0] += -(q->kb * diff - q->damp * (-E[0]));
     diff = q->pr - (X[2] - q->bmin[2]) * q->ss;
-    if (diff > EPSD) a[2] += q->kb * diff - q->damp * E[2];
+    if (decide(mode, mk, 4, diff > EPSD)) a[2] += q->kb * diff - q->damp * E[2];
     diff = q->pr - (q->bmax[2] - X[2]) * q->ss;
-    if (diff > EPSD) a[2] += -(q->kb * diff - q->damp * (-E[2]));
+    if (decide(mode, mk, 5, diff > EPSD)) a[2] += -(q->kb * diff - q->damp * (-E[2]));
 }
 
 /* The adjoint of walls(): given abar, add d(a)/dX^T abar to Xbar and
@@ -142,6 +152,8 @@ static void walls_adj(const P64 *q, double t, const double *X, const double *E, 
 typedef struct {
     double *X, *V, *E, *rho, *F;
     AdvTape *adv;
+    uint8_t *mask;   /* n branch-decision bytes of this step (mode 1/2), else null */
+    int mode;
 } Tape;
 
 static void step_forward(const P64 *q, int n, const uint32_t *perm, const uint8_t *inr, const uint32_t *poff,
@@ -190,15 +202,17 @@ static void step_forward(const P64 *q, int n, const uint32_t *perm, const uint8_
             continue;
         }
         double a[3];
+        uint8_t scratch = 0, *mk = tp->mask ? tp->mask + s : &scratch;
+        const int mode = tp->mask ? tp->mode : 0;
         for (int k = 0; k < 3; k++) a[k] = F[3 * s + k] * q->m;
-        walls(q, t, X + 3 * s, E + 3 * s, a);
+        walls(q, t, X + 3 * s, E + 3 * s, a, mk, mode);
         for (int k = 0; k < 3; k++) a[k] += q->g[k];
         for (int k = 0; k < 3; k++) at->a[k] = a[k];
         const double sa = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
-        at->aclamp = sa > q->AL * q->AL;
+        at->aclamp = decide(mode, mk, 6, sa > q->AL * q->AL);
         for (int k = 0; k < 3; k++) at->ac[k] = at->aclamp ? a[k] * q->AL / sqrt(sa) : a[k];
         const double sv = V[3 * s] * V[3 * s] + V[3 * s + 1] * V[3 * s + 1] + V[3 * s + 2] * V[3 * s + 2];
-        at->vclamp = sv > q->VL * q->VL;
+        at->vclamp = decide(mode, mk, 7, sv > q->VL * q->VL);
         for (int k = 0; k < 3; k++) at->vc[k] = at->vclamp ? V[3 * s + k] * q->VL / sqrt(sv) : V[3 * s + k];
         for (int k = 0; k < 3; k++) {
             const double vn = at->ac[k] * q->dt + at->vc[k];
@@ -323,18 +337,23 @@ static void step_backward(const P64 *q, int n, const uint32_t *perm, const uint8
 }
 
 /* T steps forward from (x, v, e) in place (doubles, n x 3). theta =
- * (visc, rest density, IntStiff) overrides the parameter block's values. */
+ * (visc, rest density, IntStiff) overrides the parameter block's values.
+ * masks (nullable, T x n bytes) with mask_mode 1 records each step's wall
+ * and clamp decisions, with mask_mode 2 replays them (see decide()). */
 void adj64_forward(const fl_params *p, const double *theta, int n, int T, const uint32_t *perm,
                    const uint8_t *inr, const uint32_t *poff, const uint32_t *pnbr, const uint64_t *pbase,
-                   const double *time, double *x, double *v, double *e) {
+                   const double *time, double *x, double *v, double *e, uint8_t *masks, int mask_mode) {
     const P64 q = p64(p, theta);
     Tape tp;
     tp.X = malloc(sizeof(double) * 3 * n); tp.V = malloc(sizeof(double) * 3 * n);
     tp.E = malloc(sizeof(double) * 3 * n); tp.rho = malloc(sizeof(double) * n);
     tp.F = malloc(sizeof(double) * 3 * n); tp.adv = malloc(sizeof(AdvTape) * n);
-    for (int t = 0; t < T; t++)
+    tp.mode = mask_mode;
+    for (int t = 0; t < T; t++) {
+        tp.mask = masks ? masks + (size_t)t * n : NULL;
         step_forward(&q, n, perm + (size_t)t * n, inr + (size_t)t * n, poff + (size_t)t * (n + 1),
                      pnbr + pbase[t], time[t], x, v, e, &tp);
+    }
     free(tp.X); free(tp.V); free(tp.E); free(tp.rho); free(tp.F); free(tp.adv);
 }
 
@@ -350,6 +369,8 @@ void adj64_backward(const fl_params *p, const double *theta, int n, int T, const
     const P64 q = p64(p, theta);
     const size_t n3 = (size_t)n * 3;
     Tape tp;
+    tp.mask = NULL;
+    tp.mode = 0;
     tp.X = malloc(sizeof(double) * n3); tp.V = malloc(sizeof(double) * n3);
     tp.E = malloc(sizeof(double) * n3); tp.rho = malloc(sizeof(double) * (n ? n : 1));
     tp.F = malloc(sizeof(double) * n3); tp.adv = malloc(sizeof(AdvTape) * (n ? n : 1));

@@ -282,7 +282,7 @@ def _adj_lib():
     if not getattr(lib, "_adj_ready", False):
         vp, i = C.c_void_p, C.c_int
         lib.orc_pairs.argtypes = [vp, i, vp, vp, vp, vp, vp, vp]
-        lib.adj64_forward.argtypes = [vp, vp, i, i] + [vp] * 9
+        lib.adj64_forward.argtypes = [vp, vp, i, i] + [vp] * 10 + [i]
         lib.adj64_backward.argtypes = [vp, vp, i, i] + [vp] * 14
         lib._adj_ready = True
     return lib
@@ -337,13 +337,18 @@ def _theta(theta):
     return None if theta is None else np.ascontiguousarray(theta, np.float64)
 
 
-def adj64_forward(params, fz: Frozen, x0, v0, e0, theta=None):
+def adj64_forward(params, fz: Frozen, x0, v0, e0, theta=None, masks=None, mask_mode: int = 0):
     """The FP64 frozen-structure forward from (x0, v0, e0): the final (x, v, e).
-    theta = (visc, rest density, IntStiff) overrides the parameter block."""
+    theta = (visc, rest density, IntStiff) overrides the parameter block.
+    masks ((T, n) uint8) with mask_mode 1 records the wall and clamp decisions
+    of every step, with mask_mode 2 reuses them (decisions frozen too)."""
     x, v, e = (np.array(a, np.float64).reshape(fz.n, 3) for a in (x0, v0, e0))
     th = _theta(theta)
+    if masks is not None:
+        assert masks.dtype == np.uint8 and masks.shape == (fz.steps, fz.n) and masks.flags.c_contiguous
     _adj_lib().adj64_forward(C.byref(params), _p(th), fz.n, fz.steps, _p(fz.perm), _p(fz.inr),
-                             _p(fz.poff), _p(fz.pnbr), _p(fz.pbase), _p(fz.time), _p(x), _p(v), _p(e))
+                             _p(fz.poff), _p(fz.pnbr), _p(fz.pbase), _p(fz.time), _p(x), _p(v), _p(e),
+                             _p(masks), int(mask_mode if masks is not None else 0))
     return x, v, e
 
 

@@ -101,3 +101,58 @@ def test_adjoint64_linearised_at_fp32_states_is_close_to_its_own(steps):
     b = O.adj64_backward(sc.params, fz, *w, x0, v0, e0, use_states=False)
     for ga, gb in zip(a, b):
         assert np.linalg.norm(ga - gb) <= 1e-3 * np.linalg.norm(gb) + 1e-12
+
+
+def _final_order(fz):
+    order = np.arange(fz.n, dtype=np.int64)
+    for k in range(fz.steps):
+        order = order[fz.perm[k]]
+    return order
+
+
+def rollout_loss64(p, fz, target, x0, v0, e0, theta, masks=None, mask_mode=0):
+    """The differentiated rollout's loss (mean squared distance of the final
+    positions to the target, over the points in range at the last step) on
+    the FP64 frozen-structure model, and its cotangent on the final state."""
+    x, _, _ = O.adj64_forward(p, fz, x0, v0, e0, theta, masks, mask_mode)
+    live = fz.inr[-1].astype(bool)
+    d = np.where(live[:, None], x - target[_final_order(fz)], 0.0)
+    m = int(live.sum())
+    return float((d ** 2).sum()) / m, 2.0 * d / m
+
+
+def test_rollout_65k_gradient_matches_central_differences():
+    """The 65,536-point scaled dam break, 8 steps: the loss gradient with
+    respect to (viscosity, rest density, IntStiff) and along a random
+    direction of the initial velocity field, adjoint against central
+    differences, both on the FP64 model. Parameters: a step of 1e-4
+    relative with the wall and limit decisions frozen as well (over 65,536
+    points some point sits within 1e-4 of a threshold, where the model has a
+    kink), and 1e-6 relative with free decisions. Velocity field: the loss
+    curves strongly along a 196,608-dimensional direction (central
+    differences converge quadratically: 2.5e-2 off at a step of 1e-4, 2.5e-4
+    at 1e-5), so the steps there are 1e-5 (frozen) and 1e-7 (free)."""
+    sc = scenes.dam_break_scaled(65536)
+    p = sc.params
+    st = O.State.new(p, sc.pos, sc.vel, sc.veval, sc.clr)
+    t = O.run(p, st, 20, 0.0, threads=4)           # a moving state, not the lattice at rest
+    fz = O.frozen_run(p, st.copy(), 8, t)
+    target = scenes.shifted_target(sc)
+    x0, v0, e0 = (np.array(a) for a in fz.states[0])
+    th0 = np.array([p.pvisc, p.prest_dens, p.pintstiff], np.float64)
+    masks = np.zeros((fz.steps, fz.n), np.uint8)
+    loss, cot = rollout_loss64(p, fz, target, x0, v0, e0, th0, masks, 1)
+    gx, gv, ge, gp = O.adj64_backward(p, fz, cot, np.zeros_like(cot), np.zeros_like(cot), x0, v0, e0,
+                                      theta=th0, use_states=False)
+    d = np.random.default_rng(8).standard_normal(v0.shape)
+    for rel, hv, mode in ((1e-4, 1e-5, 2), (1e-6, 1e-7, 0)):
+        L = lambda th, v: rollout_loss64(p, fz, target, x0, v, e0, th, masks, mode)[0]
+        for k in range(3):
+            h = rel * abs(th0[k])
+            tp = th0.copy(); tp[k] += h
+            tm = th0.copy(); tm[k] -= h
+            fd = (L(tp, v0) - L(tm, v0)) / (2 * h)
+            assert abs(fd - gp[k]) <= 1e-3 * abs(fd), ("param", k, rel, fd, gp[k])
+        fd = (L(th0, v0 + hv * d) - L(th0, v0 - hv * d)) / (2 * hv)
+        an = float((gv * d).sum())
+        assert abs(fd - an) <= 1e-3 * abs(fd), ("velocity", hv, fd, an)
