@@ -147,6 +147,7 @@ static void free_all(fl_system *s) {
     cudaFree(s->hitlist); cudaFree(s->hitcnt);
     cudaFree(s->d_scenes); cudaFree(s->point_scene); cudaFree(s->cell_scene);
     free(s->scene_point_base); free(s->scene_n); free(s->scene_cell_base); free(s->scene_ncells);
+    free(s->scene_params);
     free_grid(s);
     cudaFree(s->dev_err);
     cudaFree(s->time_dev);
@@ -280,9 +281,11 @@ extern "C" int fl_batch_create(const fl_params *params, const int *counts, int n
         s->scene_n = (int *)calloc(nscenes, sizeof(int));
         s->scene_cell_base = (int *)calloc(nscenes, sizeof(int));
         s->scene_ncells = (int *)calloc(nscenes, sizeof(int));
+        s->scene_params = (fl_params *)calloc(nscenes, sizeof(fl_params));
+        if (s->scene_params) memcpy(s->scene_params, params, sizeof(fl_params) * nscenes);
         std::vector<DevParams> tab(nscenes);
         std::vector<uint16_t> pscene((size_t)(npts > 0 ? npts : 1)), cscene((size_t)gcell);
-        if (!s->scene_point_base || !s->scene_n || !s->scene_cell_base || !s->scene_ncells) {
+        if (!s->scene_point_base || !s->scene_n || !s->scene_cell_base || !s->scene_ncells || !s->scene_params) {
             r = fl_fail(FL_ERR_NOMEM, "fl_batch_create: host allocation failed");
             break;
         }
@@ -350,6 +353,49 @@ extern "C" int fl_batch_scene_info(const fl_system *s, int scene, int *point_bas
 }
 
 extern "C" int fl_num_scenes(const fl_system *s) { return s ? s->nscenes : 0; }
+
+extern "C" int fl_batch_get_params(const fl_system *s, int scene, fl_params *p) {
+    if (!s || !p) return fl_fail(FL_ERR_ARG, "fl_batch_get_params: null argument");
+    if (scene < 0 || scene >= s->nscenes) return fl_fail(FL_ERR_ARG, "fl_batch_get_params: scene %d", scene);
+    *p = s->batched ? s->scene_params[scene] : s->P;
+    return FL_OK;
+}
+
+extern "C" int fl_batch_set_params(fl_system *s, int scene, const fl_params *p) {
+    if (!s || !p) return fl_fail(FL_ERR_ARG, "fl_batch_set_params: null argument");
+    if (scene < 0 || scene >= s->nscenes) return fl_fail(FL_ERR_ARG, "fl_batch_set_params: scene %d", scene);
+    if (!s->batched) return fl_set_params(s, p);
+    FL_TRY(check_derived(p));
+    const fl_params &o = s->scene_params[scene];
+    bool same = p->gridSrch == o.gridSrch && p->gridTotal == o.gridTotal && p->dt == o.dt;
+    for (int k = 0; k < 3; k++)
+        same = same && p->gridRes[k] == o.gridRes[k] && p->gridMin[k] == o.gridMin[k] &&
+               p->gridDelta[k] == o.gridDelta[k] && p->gridScanMax[k] == o.gridScanMax[k];
+    if (!same)
+        return fl_fail(FL_ERR_PARAMS, "fl_batch_set_params: scene %d: the new block changes the scene's grid or dt",
+                       scene);
+    DevParams d;
+    fl_make_dev_params(*p, &d);
+    d.cell_base = s->scene_cell_base[scene];
+    d.upwords = s->D.upwords;
+    d.hcap = s->D.hcap;
+    d.prune = s->D.prune;
+    FL_CUDA_TRY(cudaMemcpyAsync(s->d_scenes + scene, &d, sizeof(d), cudaMemcpyHostToDevice, s->stream));
+    FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->scene_params[scene] = *p;
+    if (scene == 0) {   // scene 0's block also serves as the launch-wide one
+        const int upwords = s->D.upwords, hcap = s->D.hcap, prune = s->D.prune;
+        s->D = d;
+        s->D.cell_base = 0;
+        s->D.upwords = upwords;
+        s->D.hcap = hcap;
+        s->D.prune = prune;
+        s->P = *p;
+        destroy_graph(s);
+    }
+    fl_tape_touch(s);
+    return FL_OK;
+}
 
 extern "C" int fl_destroy(fl_system *s) {
     if (!s) return FL_OK;

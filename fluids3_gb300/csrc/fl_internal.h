@@ -92,6 +92,7 @@ struct fl_system {
     DevParams *d_scenes;   // device table, one block per scene
     uint16_t *point_scene, *cell_scene;
     int *scene_point_base, *scene_n, *scene_cell_base, *scene_ncells;   // host copies
+    fl_params *scene_params;   // host copy of every scene's parameter block
 
     Field f[F_COUNT];      // pos/vel/veval/force: float4; press: float; clr/gcell/gndx: uint
 

@@ -97,6 +97,19 @@ extern "C" int fl_tape_begin(fl_system *s, int max_steps, int every) {
     if (max_steps < 1 || every < 1 || every > max_steps)
         return fl_fail(FL_ERR_ARG, "fl_tape_begin: max_steps %d, every %d (need 1 <= every <= max_steps)",
                        max_steps, every);
+    if (s->tape && s->tape->max_steps == max_steps && s->tape->every == every &&
+        s->tape->cap == (s->max_points > 0 ? s->max_points : 1)) {
+        // same shape: start over in the storage already held
+        fl_tape *t = s->tape;
+        FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+        t->steps = 0;
+        t->n = 0;
+        t->broken = 0;
+        t->ident_cur = 0;
+        t->gcur = 0;
+        t->recording = 1;
+        return FL_OK;
+    }
     fl_tape_free(s);
     fl_tape *t = new fl_tape();
     memset(t, 0, sizeof(*t));

@@ -19,14 +19,16 @@ def position_loss(system: FluidSystem, target: np.ndarray, order: np.ndarray | N
     """Mean squared distance (world units^2) of the final positions to
     `target` (per point, indexed as when recording began), over the points
     that were inside the scan range at the start of the last step (the others
-    are parked at -1000 and carry no derivative). Returns (loss, dL/dpos in
+    are parked at -1000 and carry no derivative) and whose target is finite
+    (NaN marks a point without one). Returns (loss, dL/dpos in
     the current slot order as float32, number of points counted); for a
     batched system the mean is taken per scene and the losses summed."""
     if order is None:
         order = system.TapeOrder()
     x = system.GetBuffer(FPOS).astype(np.float64)
-    live = system.GetBuffer(FGCELL) != GRID_UNDEF
-    d = np.where(live[:, None], x - np.asarray(target, np.float64)[order], 0.0)
+    y = np.asarray(target, np.float64)[order]
+    live = (system.GetBuffer(FGCELL) != GRID_UNDEF) & np.isfinite(y).all(axis=1) & np.isfinite(x).all(axis=1)
+    d = np.where(live[:, None], np.where(live[:, None], x, 0.0) - np.where(np.isfinite(y), y, 0.0), 0.0)
     grad = np.zeros_like(d)
     loss = 0.0
     counted = 0
@@ -42,10 +44,12 @@ def position_loss(system: FluidSystem, target: np.ndarray, order: np.ndarray | N
     return loss, grad.astype(np.float32), counted
 
 
-def differentiated_rollout(system: FluidSystem, steps: int, target: np.ndarray, every: int = 1) -> dict:
+def differentiated_rollout(system: FluidSystem, steps: int, target: np.ndarray, every: int = 1,
+                           keep_tape: bool = False) -> dict:
     """Record `steps` steps from the system's current state (checkpoints every
     `every` steps), then back-propagate position_loss(target). The system is
-    left at the final state with the tape closed."""
+    left at the final state; the tape is closed unless keep_tape (then the
+    next rollout of the same shape reuses its storage)."""
     system.TapeBegin(steps, every)
     try:
         system.RunSteps(steps)
@@ -53,7 +57,8 @@ def differentiated_rollout(system: FluidSystem, steps: int, target: np.ndarray, 
         loss, dpos, counted = position_loss(system, target, order)
         gpos, gvel, gveval, gparams = system.Backward(dpos)
     finally:
-        system.TapeEnd()
+        if not keep_tape:
+            system.TapeEnd()
     return {"loss": loss, "points": counted, "grad_pos": gpos, "grad_vel": gvel, "grad_veval": gveval,
             "grad_params": gparams, "order": order, "dloss_dpos": dpos}
 

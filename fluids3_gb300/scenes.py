@@ -13,6 +13,8 @@ Workloads:
                  keep its density (65,536: the differentiated rollout)
   wave_tank      4,000,000 points filling the low-x 40% of a ~330-unit box,
                  X- wall forcing at frequency 0.2, amplitude 0.3
+  fit_scenes     64 scenes of 8,192..32,768 points with a hidden viscosity
+                 each (the batched parameter fit)
   batch_scenes   256 independent scenes, 2,048..65,536 points each
                  (log-uniform), each a block filling 20..60% of its own box,
                  with its own viscosity (0.1..0.5) and rest density (500..700)
@@ -217,6 +219,21 @@ def batch_scenes(nscenes: int = 256, seed: int = 3, nmin: int = 2048, nmax: int 
         visc = float(np.float32(0.1 + 0.4 * u[2][k]))
         rest = float(np.float32(500.0 + 200.0 * u[3][k]))
         out.append(block_scene(n, fill, seed * 1000 + k, f"scene_{k}", steps, pvisc=visc, prest_dens=rest))
+    return out
+
+
+def fit_scenes(nscenes: int = 64, seed: int = 6, nmin: int = 8192, nmax: int = 32768,
+               steps: int = 100) -> list[Scene]:
+    """Scenes for the batched parameter fit: point counts log-uniform in
+    [nmin, nmax], fill fraction U[0.2, 0.6], and a hidden viscosity
+    U[0.1, 0.5] (in params.pvisc); every other parameter is the dam-break set."""
+    u = [_draws(seed, k, nscenes) for k in range(3)]
+    out = []
+    for k in range(nscenes):
+        n = int(round(np.exp(np.log(nmin) + u[0][k] * (np.log(nmax) - np.log(nmin)))))
+        fill = 0.2 + 0.4 * u[1][k]
+        visc = float(np.float32(0.1 + 0.4 * u[2][k]))
+        out.append(block_scene(n, fill, seed * 1000 + k, f"fit_{k}", steps, pvisc=visc))
     return out
 
 

@@ -103,6 +103,15 @@ class FluidSystem:
         call("fl_batch_scene_info", self._h, int(scene), *[C.byref(x) for x in v])
         return dict(point_base=v[0].value, n=v[1].value, cell_base=v[2].value, ncells=v[3].value)
 
+    def SceneParams(self, scene: int) -> FlParams:
+        p = FlParams()
+        call("fl_batch_get_params", self._h, int(scene), C.byref(p))
+        return p
+
+    def SetSceneParams(self, scene: int, params: FlParams) -> None:
+        """Replace one scene's physical parameters (same grid and dt)."""
+        call("fl_batch_set_params", self._h, int(scene), C.byref(params))
+
     # -- lifetime -------------------------------------------------------------
     def close(self) -> None:
         if self._h:

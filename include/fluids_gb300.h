@@ -170,6 +170,14 @@ int fl_num_scenes(const fl_system *s);
  * reference-layout grid. A single-scene system is scene 0. */
 int fl_batch_scene_info(const fl_system *s, int scene, int *point_base, int *n, int *cell_base,
                         int *ncells);
+/* One scene's parameter block. fl_batch_set_params replaces the physical
+ * parameters of scene `scene` (e.g. its viscosity or IntStiff during a
+ * parameter fit) without rebuilding the batch: the new block (derived) must
+ * keep the scene's grid -- gridRes, gridMin, gridDelta, gridSrch -- and the
+ * batch's dt, else FL_ERR_PARAMS. Like fl_set_params it invalidates an
+ * open tape. A single-scene system takes scene 0 through fl_set_params. */
+int fl_batch_get_params(const fl_system *s, int scene, fl_params *p);
+int fl_batch_set_params(fl_system *s, int scene, const fl_params *p);
 
 /* ---- data movement (fluid.h host layout: float3 packed 12 B, uint 4 B) --- */
 
@@ -271,7 +279,9 @@ int fl_get_phase_times(fl_system *s, double ms[8], int *steps);
  * sort, which pairs interact, which walls and limits act) is piecewise
  * constant and carries no derivative.
  *
- * fl_tape_begin opens a tape for up to max_steps steps: every Run step
+ * fl_tape_begin opens a tape for up to max_steps steps (a tape already
+ * open with the same max_steps and every starts over in its storage,
+ * without reallocating; another shape is freed first): every Run step
  * from then on saves the state before it every `every` steps (48 B per
  * point each; every > 1 trades memory for a replay of each segment during
  * fl_backward) and its time. Changing the state outside Run while recording

@@ -124,3 +124,44 @@ def test_batch_rejects_mixed_dt_and_wrong_count():
     with F.FluidSystem.batch([sc.params for sc in scs], [sc.n for sc in scs]) as b:
         with pytest.raises(F.FluidsError):
             b.SetParticles(scs[0].pos)
+
+
+def test_batch_set_params_equals_a_scene_created_with_them():
+    """fl_batch_set_params: a scene whose viscosity and IntStiff are replaced
+    steps exactly like a system created with them; a block that changes the
+    scene's grid is rejected."""
+    from fluids3_gb300.fit import set_scene_physics
+    scs = scenes.batch_scenes(nscenes=3, nmin=1500, nmax=3000, seed=31)
+    cat = scenes.concat(scs)
+    with F.FluidSystem.batch([sc.params for sc in scs], [sc.n for sc in scs]) as b:
+        b.SetParticles(cat["pos"], cat["vel"], cat["veval"], clr=cat["clr"])
+        for k in (0, 2):
+            set_scene_physics(b, k, 0.123, 1.7)
+        b.RunSteps(6)
+        got = b.GetBuffer(F.FPOS)
+        bad = scenes.make_params((0.0, 0.0, 0.0), (10.0, 10.0, 10.0))
+        with pytest.raises(F.FluidsError) as e:
+            b.SetSceneParams(1, bad)
+        assert e.value.code == -3
+    base = 0
+    for k, sc in enumerate(scs):
+        p = sc.params.copy()
+        if k != 1:
+            p.pvisc, p.pintstiff = 0.123, 1.7
+        p = F.derive_params(p)
+        with F.FluidSystem(p, sc.n) as s:
+            s.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
+            s.RunSteps(6)
+            assert_bit_equal(got[base:base + sc.n], s.GetBuffer(F.FPOS), f"scene {k}")
+        base += sc.n
+
+
+def test_batched_fit_recovers_viscosity_on_a_small_batch():
+    """A small version of the batched parameter fit: 4 scenes, 40 steps,
+    checkpoints every 10. The loss falls and the viscosity error shrinks."""
+    from fluids3_gb300.fit import batched_fit
+    scs = scenes.fit_scenes(nscenes=4, nmin=2000, nmax=4000, seed=32)
+    res = batched_fit(scs, steps=40, every=10, iters=25, lr=0.05)
+    start_err = np.abs(0.3 - res.hidden_visc) / res.hidden_visc
+    assert res.losses[-1] < 0.5 * res.losses[0], res.losses
+    assert np.median(res.visc_rel_err) < 0.5 * np.median(start_err), (res.visc, res.hidden_visc)
