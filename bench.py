@@ -24,6 +24,13 @@ density, force + advance (six kernels).
   cpu_baseline  the reference's CPU path (the reference kernels built for the
           host where available, else the oracle port) on a bounded sample
 
+  batched  256 scenes stepped as one batched system vs one at a time
+  adjoint  adjoint/forward time per step: the differentiated 65,536-point
+          rollout (checkpointed and every-step tapes, their device memory)
+          and the 4M wave tank
+  fit     the 64-scene batched parameter fit: viscosity recovery error,
+          device memory of a 100-step tape with and without checkpointing
+
 --impl reference prints the reference arm instead (CPU, all host threads).
 Multi-GPU (torchrun): every rank steps its own replica (no exchange), the
 slowest rank's time sets the aggregate.
@@ -31,6 +38,7 @@ slowest rank's time sets the aggregate.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -74,6 +82,11 @@ def parse():
     ap.add_argument("--batch-scenes", type=int, default=256,
                     help="scenes in the batched-vs-one-at-a-time comparison (0 skips it)")
     ap.add_argument("--batch-steps", type=int, default=20)
+    ap.add_argument("--adjoint-steps", type=int, default=200,
+                    help="steps of the differentiated 65,536-point rollout (0 skips the adjoint section)")
+    ap.add_argument("--adjoint-every", type=int, default=20, help="checkpoint interval of that rollout")
+    ap.add_argument("--fit-iters", type=int, default=40,
+                    help="iterations of the 64-scene batched parameter fit (0 skips it)")
     return ap.parse_args()
 
 
@@ -303,6 +316,157 @@ def batched_comparison(args):
                         "visc U[0.1,0.5], rest density U[500,700], dam-break parameters otherwise"}
 
 
+def _device_free():
+    try:
+        import torch
+        return int(torch.cuda.mem_get_info()[0])
+    except Exception:
+        return None
+
+
+def _time_backward(s, dpos):
+    """Wall time of one fl_backward with the cotangent and the gradients in
+    device memory (fl_backward returns after its stream is done)."""
+    import torch
+    from fluids3_gb300 import _lib
+    d = torch.from_numpy(np.ascontiguousarray(dpos, np.float32)).cuda()
+    outs = [torch.empty_like(d) for _ in range(3)]
+    gp = np.zeros((s.NumScenes(), 3), np.float64)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _lib.check("fl_backward", _lib.lib().fl_backward(s.handle, d.data_ptr(), None, None, outs[0].data_ptr(),
+                                                   outs[1].data_ptr(), outs[2].data_ptr(),
+                                                   gp.ctypes.data_as(ctypes.c_void_p)))
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    return (t1 - t0) * 1e3, gp, outs
+
+
+def adjoint_measurements(args):
+    """Adjoint cost against the forward (adjoint/forward time per step).
+
+    rollout_65k: the differentiated rollout -- the 65,536-point scaled dam
+    break for --adjoint-steps steps, loss = mean squared distance of the
+    final positions to the seeded target cloud (the initial block shifted
+    0.3 box widths in +x), gradients for viscosity, rest density, IntStiff
+    and the initial velocities; with checkpoints every --adjoint-every steps
+    and with every step kept (device memory of both tapes).
+    wave_tank_4m: the bench workload after the warm-up, 10 recorded steps,
+    every = 1 and 5.
+    forward = graph-replayed steps without a tape; taped = the recorded
+    steps; backward = fl_backward with device buffers, per recorded step."""
+    import fluids3_gb300 as F
+    from fluids3_gb300 import scenes
+    from fluids3_gb300.rollout import position_loss
+
+    out = {}
+    sc = scenes.dam_break_scaled(65536)
+    target = scenes.shifted_target(sc)
+    T = args.adjoint_steps
+    free_before = _device_free()
+    s = F.FluidSystem(sc.params, sc.n)
+    s.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
+    s.SaveCheckpoint(0)
+    free_sys = _device_free()
+    s.RunSteps(2)                                  # graph capture
+    s.RestoreCheckpoint(0)
+    ms_fwd = s.TimeSteps(T, graph=True) / T
+    runs = {}
+    for every in (args.adjoint_every, 1):
+        s.RestoreCheckpoint(0)
+        f0 = _device_free()
+        s.TapeBegin(T, every)
+        f1 = _device_free()
+        s.Sync()
+        t0 = time.perf_counter()
+        s.RunSteps(T)
+        s.Sync()
+        t1 = time.perf_counter()
+        loss, dpos, counted = position_loss(s, target)
+        ms_b, gp, outs = _time_backward(s, dpos)
+        gvel = outs[1].cpu().numpy()
+        s.TapeEnd()
+        runs[every] = {"every": every, "tape_bytes": (f0 - f1) if f0 is not None else None,
+                       "taped_forward_ms_per_step": (t1 - t0) * 1e3 / T,
+                       "backward_ms_per_step": ms_b / T, "ratio": ms_b / T / ms_fwd,
+                       "loss": loss, "points_in_loss": counted,
+                       "grad_params": dict(zip(("pvisc", "prest_dens", "pintstiff"), gp[0].tolist())),
+                       "grad_vel_rms": float(np.sqrt((gvel.astype(np.float64) ** 2).mean()))}
+    s.close()
+    out["rollout_65k"] = {
+        "workload": f"{sc.name}: 65,536-point dam break, box scaled x1.26 (same density as the 32,768-point "
+                    f"scene), {T} steps; loss vs the initial block shifted 0.3 box widths in +x",
+        "steps": T, "forward_ms_per_step": ms_fwd,
+        "system_bytes": (free_before - free_sys) if free_before is not None else None,
+        "checkpointed": runs[args.adjoint_every], "every_step": runs[1],
+        "adjoint_forward_ratio": runs[args.adjoint_every]["ratio"]}
+
+    scene = scenes.wave_tank(n=args.n)
+    s = F.FluidSystem(scene.params, scene.n)
+    s.SetParticles(scene.pos, scene.vel, scene.veval, clr=scene.clr)
+    s.RunSteps(max(args.warmup, 3))
+    s.SaveCheckpoint(0)
+    T4 = 10
+    ms_fwd = s.TimeSteps(T4, graph=True) / T4
+    rows = []
+    w = np.random.default_rng(1).standard_normal((scene.n, 3)).astype(np.float32)
+    for every in (1, 5):
+        s.RestoreCheckpoint(0)
+        s.TapeBegin(T4, every)
+        s.Sync()
+        t0 = time.perf_counter()
+        s.RunSteps(T4)
+        s.Sync()
+        t1 = time.perf_counter()
+        _time_backward(s, w)                       # first call: staging buffers
+        ms_b, _, _ = _time_backward(s, w)
+        s.TapeEnd()
+        rows.append({"every": every, "taped_forward_ms_per_step": (t1 - t0) * 1e3 / T4,
+                     "backward_ms_per_step": ms_b / T4, "ratio": ms_b / T4 / ms_fwd})
+    s.close()
+    out["wave_tank_4m"] = {"steps": T4, "forward_ms_per_step": ms_fwd, "runs": rows}
+    return out
+
+
+def fit_measurement(args):
+    """The batched parameter fit: 64 scenes of 8,192..32,768 points
+    (log-uniform), each with a hidden viscosity U[0.1, 0.5] generating its
+    100-step target trajectory; per-scene viscosity and IntStiff fitted from
+    0.3 / 1.0 by Adam on adjoint gradients, each iteration ten 10-step
+    windows along the target trajectory (checkpoints every 10 steps). Device
+    memory of one 100-step tape of the whole batch with and without
+    checkpointing."""
+    import fluids3_gb300 as F
+    from fluids3_gb300 import scenes
+    from fluids3_gb300.fit import batched_fit
+
+    scs = scenes.fit_scenes()
+    total = sum(sc.n for sc in scs)
+    cat = scenes.concat(scs)
+    mem = {}
+    with F.FluidSystem.batch([sc.params for sc in scs], [sc.n for sc in scs]) as b:
+        b.SetParticles(cat["pos"], cat["vel"], cat["veval"], clr=cat["clr"])
+        for every in (10, 1):
+            f0 = _device_free()
+            b.TapeBegin(100, every)
+            f1 = _device_free()
+            b.TapeEnd()
+            mem[every] = (f0 - f1) if f0 is not None else None
+    t0 = time.perf_counter()
+    res = batched_fit(scs, steps=100, window=10, every=10, iters=args.fit_iters, lr=0.05)
+    el = time.perf_counter() - t0
+    err = res.visc_rel_err
+    start_err = np.abs(0.3 - res.hidden_visc) / res.hidden_visc
+    return {"scenes": len(scs), "points": total, "steps": 100, "window": 10, "every": 10,
+            "iterations": args.fit_iters, "seconds": el,
+            "loss_first": res.losses[0], "loss_last": res.losses[-1],
+            "visc_rel_err": {"median": float(np.median(err)), "p90": float(np.percentile(err, 90)),
+                             "max": float(err.max()), "start_median": float(np.median(start_err))},
+            "intstiff": {"hidden": 1.0, "median": float(np.median(res.stiff)),
+                         "min": float(res.stiff.min()), "max": float(res.stiff.max())},
+            "tape_bytes_100_steps": {"every_10": mem[10], "every_1": mem[1]}}
+
+
 def config_of(scene, args):
     p = scene.params
     return {"workload": f"{scene.name}: {scene.n:,}-point SPH wave tank (dam break with X- wall forcing, "
@@ -421,6 +585,8 @@ def our_arm(args, rank, world, local_rank):
         return
 
     batched = batched_comparison(args) if args.batch_scenes > 0 else None
+    adjoint = adjoint_measurements(args) if args.adjoint_steps > 0 else None
+    fit = fit_measurement(args) if args.fit_iters > 0 else None
     value = world * scene.n * args.steps / (ms / 1e3) / 1e6
     dominant = max((k for k in phases if k != "scan"), key=lambda k: phases[k])
     dur_ms = phases[dominant]
@@ -454,6 +620,8 @@ def our_arm(args, rank, world, local_rank):
         "e2e": {"value": world * n * e2e_steps / e2e_s / 1e6, "unit": METRIC, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": e2e_steps},
         "batched": batched,
+        "adjoint": adjoint,
+        "fit": fit,
         "clocks": clocks.summary(t0, t1),
         "gpu_launches": KERNELS_PER_STEP * args.steps,
         "device_status": status,
