@@ -195,6 +195,15 @@ class FluidSystem:
                  FGRIDOFF: "gridoff"}
         return {v: self.GetBuffer(k) for k, v in names.items()}
 
+    def SavePoints(self, path, with_veval: bool = True) -> None:
+        """SavePoints (cpp:1511-1545): the points to a .pts file; with_veval
+        adds the evaluated velocity for an exact resume."""
+        call("fl_save_points", self._h, str(path).encode(), 1 if with_veval else 0)
+
+    def LoadPoints(self, path) -> None:
+        """RunPlayback (cpp:1787-1841): the points of a .pts file."""
+        call("fl_load_points", self._h, str(path).encode())
+
     # -- phases (fluid_system.h:249-256) --------------------------------------
     def InsertParticlesCUDA(self, readback: bool = False):
         n, c = self.NumPoints(), self.getGridTotal()

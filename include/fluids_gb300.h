@@ -67,6 +67,7 @@ extern "C" {
 #define FL_ERR_DEVICE    -5   /* a kernel raised its device error word           */
 #define FL_ERR_STATE     -6   /* phase called before the phase it depends on     */
 #define FL_ERR_NOMEM     -7   /* device allocation failed                        */
+#define FL_ERR_IO        -8   /* a point file could not be read or written       */
 
 /* Device error word bits (fl_device_status). */
 #define FL_DEV_SPIN_TIMEOUT  0x1u  /* a look-back wait hit its iteration limit */
@@ -202,6 +203,23 @@ int fl_host_free(void *p);
 int fl_export_device(fl_system *s, int buf_id, void *dev, size_t bytes);
 int fl_import_device(fl_system *s, int n, const void *dev_pos, const void *dev_vel,
                      const void *dev_veval);
+
+/* ---- point files ---------------------------------------------------------
+ * The .pts format of SavePoints / RunPlayback (cpp:1511-1545, 1787-1841):
+ * int N, int nfields, then per field {int type (0 char, 2 float), int
+ * channels, N x channels values}: position float x3, velocity float x3,
+ * colour char x4 (RGBA8), and -- written here when asked -- a fourth field,
+ * evaluated velocity float x3, so a run resumes bit for bit (readers that
+ * stop after three fields, like the reference's, are unaffected). Host byte
+ * order. fl_pts_read with all arrays NULL only fills *n and *nfields; a
+ * missing fourth field reads as zeros. Malformed files give FL_ERR_IO. */
+int fl_pts_write(const char *path, int n, const float *pos, const float *vel, const uint32_t *clr,
+                 const float *veval);
+int fl_pts_read(const char *path, int *n, int *nfields, float *pos, float *vel, uint32_t *clr, float *veval);
+/* SavePoints: the system's points to `path` (veval as well when with_veval).
+ * RunPlayback: the file's points into the system (fl_set_particles). */
+int fl_save_points(fl_system *s, const char *path, int with_veval);
+int fl_load_points(fl_system *s, const char *path);
 
 /* ---- phases (fluid_system.h:249-256) ------------------------------------- */
 
