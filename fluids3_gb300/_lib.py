@@ -66,6 +66,8 @@ SIGNATURES = [
     ("fl_pts_read", C.c_int, [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), vp, vp, vp, vp]),
     ("fl_save_points", C.c_int, [vp, C.c_char_p, C.c_int]),
     ("fl_load_points", C.c_int, [vp, C.c_char_p]),
+    ("fl_sample_volume", C.c_int, [vp, vp, C.POINTER(C.c_int), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                    C.c_float, C.c_int]),
     ("fl_tape_begin", C.c_int, [vp, C.c_int, C.c_int]),
     ("fl_tape_steps", C.c_int, [vp]),
     ("fl_tape_order", C.c_int, [vp, vp]),

@@ -233,6 +233,8 @@ int fl_launch_unpack3(fl_system *s, const float *src, float4 *dst, int n);
 int fl_launch_grid_identity(fl_system *s, uint32_t *dst, int n, const uint32_t *gcell);
 int fl_launch_gcell_ref(fl_system *s, uint32_t *dst);
 int fl_launch_integrity(fl_system *s, unsigned long long *bad_dev);
+int fl_launch_sample_volume(fl_system *s, const int res[3], const float bmin[3], const float bmax[3],
+                            float scalar, float gausskern, float h2, float *out);
 size_t fl_scan_tile();
 size_t fl_upbits_bytes(const fl_system *s);
 size_t fl_scan_scratch_bytes(int ntiles);

@@ -1,4 +1,5 @@
-// Point files and particle emission: the data either side of the step.
+// Point files, volume sampling and particle emission: the data either side
+// of the step.
 //
 // .pts files follow SavePoints / RunPlayback (fluids4.0/fluid_system.cpp:
 // 1511-1545, 1787-1841): int N, int nfields, then per field
@@ -7,6 +8,7 @@
 // (char x4). This writer may add a fourth field, the evaluated velocity
 // (float x3), so a run resumes exactly; a reader that stops after three
 // fields (the reference's) reads such a file unchanged. Host byte order.
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -119,4 +121,41 @@ extern "C" int fl_load_points(fl_system *s, const char *path) {
     if (r == FL_OK) r = fl_set_particles(s, n, pos, vel, ve, nullptr, nullptr, clr);
     free(pos); free(vel); free(ve); free(clr);
     return r;
+}
+
+// SampleParticlesCUDA (cpp:2497-2507) with SaveBricks' preparation
+// (cpp:1597-1612): optionally insert + prefix sum + counting sort first,
+// then one launch over the voxel lattice. gausskern and h2 as the reference
+// derives them (UpdateParamsCUDA cpp:2302; fluid_kernels.cu:268, where
+// 2.0 * r2 / 8.0 is evaluated in double).
+extern "C" int fl_sample_volume(fl_system *s, float *out, const int res[3], const float bmin[3],
+                                const float bmax[3], float scalar, int sort_first) {
+    if (!s || !out || !res || !bmin || !bmax) return fl_fail(FL_ERR_ARG, "fl_sample_volume: null argument");
+    if (s->batched) return fl_fail(FL_ERR_STATE, "fl_sample_volume: a batched system samples no single volume");
+    if (res[0] < 1 || res[1] < 1 || res[2] < 1 || (long long)res[0] * res[1] * res[2] > (1LL << 31))
+        return fl_fail(FL_ERR_ARG, "fl_sample_volume: resolution %d x %d x %d", res[0], res[1], res[2]);
+    if (sort_first) {
+        FL_TRY(fl_insert_particles(s, nullptr, nullptr, nullptr));
+        FL_TRY(fl_prefix_sum_cells(s, nullptr, 1));
+        FL_TRY(fl_counting_sort_full(s, nullptr));
+    } else if (!s->have_grid || s->offsets_inclusive) {
+        return fl_fail(FL_ERR_STATE, "fl_sample_volume: no sorted grid (sort_first = 1, or the phase calls first)");
+    }
+    const float sr = s->P.psmoothradius;
+    const float gausskern = 1.0f / powf(3.141592f * 2.0f * sr * sr, 3.0f / 2.0f);
+    const float h2 = (float)(2.0 * (double)s->P.r2 / 8.0);
+    const size_t bytes = sizeof(float) * (size_t)res[0] * res[1] * res[2];
+    cudaPointerAttributes attr;
+    const bool on_device = cudaPointerGetAttributes(&attr, out) == cudaSuccess && attr.type == cudaMemoryTypeDevice;
+    cudaGetLastError();
+    if (on_device) {
+        FL_TRY(fl_launch_sample_volume(s, res, bmin, bmax, scalar, gausskern, h2, out));
+        FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+        return FL_OK;
+    }
+    FL_TRY(fl_ensure_stage(s, bytes));
+    FL_TRY(fl_launch_sample_volume(s, res, bmin, bmax, scalar, gausskern, h2, (float *)s->stage));
+    FL_CUDA_TRY(cudaMemcpyAsync(out, s->stage, bytes, cudaMemcpyDefault, s->stream));
+    FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return FL_OK;
 }

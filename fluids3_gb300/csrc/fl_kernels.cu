@@ -670,6 +670,48 @@ __global__ void k_grid_identity(int n, const uint32_t *__restrict__ gcell, uint3
     dst[i] = gcell ? ((gcell[i] != kUndef) ? (uint32_t)i : kUndef) : kUndef;
 }
 
+// sampleParticles (fluids4.0/fluid_kernels.cu:263-308): a Gaussian-weighted
+// particle count at every voxel of a res.x x res.y x res.z lattice over
+// [bmin, bmax), read from the sorted grid. Voxel (x, y, z) sits at
+// bmin + (x / res.x, y / res.y, z / res.z) * (bmax - bmin) and writes
+// out[(z * res.y + y) * res.x + x] (the reference's final store; its
+// out-of-range store uses another order, an upstream slip not kept here);
+// voxels outside the scan range read 0.
+__global__ void __launch_bounds__(512)
+k_sample_volume(const __grid_constant__ DevParams P, int3 res, float3 bmin, float3 bmax, float scalar,
+                float gausskern, float h2, const float4 *__restrict__ pos, const uint32_t *__restrict__ off,
+                const uint32_t *__restrict__ cnt, float *__restrict__ out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z * blockDim.z + threadIdx.z;
+    if (x >= res.x || y >= res.y || z >= res.z) return;
+    const float px = bmin.x + ((float)x / (float)res.x) * (bmax.x - bmin.x);
+    const float py = bmin.y + ((float)y / (float)res.y) * (bmax.y - bmin.y);
+    const float pz = bmin.z + ((float)z / (float)res.z) * (bmax.z - bmin.z);
+    const size_t idx = ((size_t)z * res.y + y) * res.x + x;
+    const uint32_t cell = cell_of(P, make_float4(px, py, pz, 0.0f));
+    if (cell == (uint32_t)P.ncells) {
+        out[idx] = 0.0f;
+        return;
+    }
+    const int base = (int)cell - P.nadj;
+    float v = 0.0f;
+    for (int c = 0; c < P.gridAdjCnt; c++) {
+        const int cl = base + P.adj[c];
+        const uint32_t j0 = off[cl], j1 = j0 + cnt[cl];
+        for (uint32_t j = j0; j < j1; j++) {
+            const float4 q = pos[j];
+            const float dx = px - q.x, dy = py - q.y, dz = pz - q.z;
+            float dsq = dx * dx + dy * dy + dz * dz;
+            if (dsq < P.rd2 && dsq > 0.0f) {
+                dsq = sqrtf(dsq * P.d2);
+                v += gausskern * expf(-(dsq * dsq) / h2);
+            }
+        }
+    }
+    out[idx] = v * scalar;
+}
+
 // IntegrityCheck (fluids4.0/fluid_system.cpp:2426-2453): every sorted slot of
 // cell g must carry gcell == g and gndx == its rank; tail slots must be UNDEF.
 template <bool BATCH>
@@ -877,6 +919,18 @@ int fl_launch_grid_identity(fl_system *s, uint32_t *dst, int n, const uint32_t *
     if (n == 0) return FL_OK;
     k_grid_identity<<<blocks_for(n, kThreads), kThreads, 0, s->stream>>>(n, gcell, dst);
     FL_LAUNCH_CHECK("grid_identity");
+    return FL_OK;
+}
+
+int fl_launch_sample_volume(fl_system *s, const int res[3], const float bmin[3], const float bmax[3],
+                            float scalar, float gausskern, float h2, float *out) {
+    const dim3 block(8, 8, 8);
+    const dim3 grid((unsigned)((res[0] + 7) / 8), (unsigned)((res[1] + 7) / 8), (unsigned)((res[2] + 7) / 8));
+    k_sample_volume<<<grid, block, 0, s->stream>>>(s->D, make_int3(res[0], res[1], res[2]),
+                                                    make_float3(bmin[0], bmin[1], bmin[2]),
+                                                    make_float3(bmax[0], bmax[1], bmax[2]), scalar, gausskern, h2,
+                                                    s->f[F_POS].cur<float4>(), s->off, s->cnt, out);
+    FL_LAUNCH_CHECK("sample_volume");
     return FL_OK;
 }
 

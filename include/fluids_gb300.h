@@ -221,6 +221,19 @@ int fl_pts_read(const char *path, int *n, int *nfields, float *pos, float *vel, 
 int fl_save_points(fl_system *s, const char *path, int with_veval);
 int fl_load_points(fl_system *s, const char *path);
 
+/* SampleParticlesCUDA (cpp:2497-2507; kernel fluid_kernels.cu:263-308), the
+ * volume sampling behind SaveBricks (cpp:1597-1752): at every voxel of a
+ * res[0] x res[1] x res[2] lattice over [bmin, bmax) (voxel i at bmin + i /
+ * res * (bmax - bmin)), scalar x the sum over the particles of its search
+ * block within the smoothing radius of gausskern * exp(-r^2 / h2) (r in
+ * simulation units, h2 = r2 / 4). Written to out[(z * res[1] + y) * res[0]
+ * + x] (host or device memory); voxels outside the scan range are 0. With
+ * sort_first the points are first binned and sorted (InsertParticles,
+ * PrefixSumCells, CountingSortFull, as SaveBricks does), else the grid of
+ * the last sort is used. Single-scene systems. */
+int fl_sample_volume(fl_system *s, float *out, const int res[3], const float bmin[3], const float bmax[3],
+                     float scalar, int sort_first);
+
 /* ---- phases (fluid_system.h:249-256) ------------------------------------- */
 
 /* InsertParticlesCUDA (cpp:2334-2350; kernel fluid_kernels.cu:22-53).
