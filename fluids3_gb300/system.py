@@ -204,6 +204,21 @@ class FluidSystem:
         """RunPlayback (cpp:1787-1841): the points of a .pts file."""
         call("fl_load_points", self._h, str(path).encode())
 
+    def SampleParticles(self, res, bmin, bmax, scalar: float = 1.0 / 100.0, sort_first: bool = True,
+                        out=None):
+        """SampleParticlesCUDA (cpp:2497-2507): Gaussian-weighted particle
+        density on a res = (x, y, z) voxel lattice over [bmin, bmax); returns
+        (or fills `out`, host array or device pointer) shape (z, y, x)."""
+        r = (C.c_int * 3)(*[int(v) for v in res])
+        lo = (C.c_float * 3)(*[float(v) for v in bmin])
+        hi = (C.c_float * 3)(*[float(v) for v in bmax])
+        if out is None or isinstance(out, np.ndarray):
+            arr = out if out is not None else np.empty((int(res[2]), int(res[1]), int(res[0])), np.float32)
+            call("fl_sample_volume", self._h, _ptr(arr), r, lo, hi, C.c_float(scalar), 1 if sort_first else 0)
+            return arr
+        call("fl_sample_volume", self._h, out, r, lo, hi, C.c_float(scalar), 1 if sort_first else 0)
+        return None
+
     # -- phases (fluid_system.h:249-256) --------------------------------------
     def InsertParticlesCUDA(self, readback: bool = False):
         n, c = self.NumPoints(), self.getGridTotal()

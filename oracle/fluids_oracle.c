@@ -139,6 +139,42 @@ void orc_pairs(const fl_params *p, int n, const float *pos, const uint32_t *gcel
     poff[n] = k;
 }
 
+/* sampleParticles (fluids4.0/fluid_kernels.cu:263-308) over a sorted state
+ * (FGRID = identity): voxel (x, y, z) at bmin + i / res * (bmax - bmin),
+ * out[(z * res[1] + y) * res[0] + x] = scalar * sum gausskern * exp(-r^2 / h2)
+ * over the search block's particles within the smoothing radius; 0 where
+ * the voxel lies outside the scan range. FP32 in the reference's order
+ * (libm expf here, CUDA's expf on the device: the sums agree to ~1e-6). */
+void orc_sample_volume(const fl_params *p, const float *pos, const uint32_t *off, const uint32_t *cnt,
+                       const int *res, const float *bmin, const float *bmax, float scalar, float gausskern,
+                       float h2, float *out) {
+    const int nadj = (1 * p->gridRes[2] + 1) * p->gridRes[0] + 1;
+    for (int z = 0; z < res[2]; z++)
+        for (int y = 0; y < res[1]; y++)
+            for (int x = 0; x < res[0]; x++) {
+                float q[3];
+                const int ix[3] = {x, y, z};
+                for (int k = 0; k < 3; k++) q[k] = bmin[k] + ((float)ix[k] / (float)res[k]) * (bmax[k] - bmin[k]);
+                const size_t idx = ((size_t)z * res[1] + y) * res[0] + x;
+                const uint32_t c = cell_of(p, q);
+                if (c == (uint32_t)p->gridTotal) { out[idx] = 0.0f; continue; }
+                const int base = (int)c - nadj;
+                float v = 0.0f;
+                for (int a = 0; a < p->gridAdjCnt; a++) {
+                    const int cell = base + p->gridAdj[a];
+                    for (uint32_t j = off[cell]; j < off[cell] + cnt[cell]; j++) {
+                        const float dx = q[0] - pos[3 * j], dy = q[1] - pos[3 * j + 1], dz = q[2] - pos[3 * j + 2];
+                        float dsq = dx * dx + dy * dy + dz * dz;
+                        if (dsq < p->rd2 && dsq > 0.0f) {
+                            dsq = sqrtf(dsq * p->d2);
+                            v += gausskern * expf(-(dsq * dsq) / h2);
+                        }
+                    }
+                }
+                out[idx] = v * scalar;
+            }
+}
+
 /* computeForce (fluids4.0/fluid_kernels.cu:180-217); the float3 operators
  * of cutil_math.h expand component-wise, and '/ s' is '* (1.0f / s)'. */
 void orc_force(const fl_params *p, int n, const float *pos, const float *veval,

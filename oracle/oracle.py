@@ -372,3 +372,31 @@ def adj64_backward(params, fz: Frozen, xb, vb, eb, x0=None, v0=None, e0=None, th
                               _p(fz.pnbr), _p(fz.pbase), _p(fz.time), _p(st), _p(x0), _p(v0), _p(e0),
                               _p(xb), _p(vb), _p(eb), _p(g))
     return xb, vb, eb, g
+
+
+def sample_volume(params, pos, off, cnt, res, bmin, bmax, scalar):
+    """sampleParticles on a sorted state (pos in slot order, off/cnt per
+    cell); returns a (res_z, res_y, res_x) float32 array."""
+    lib = orc()
+    if not getattr(lib, "_sample_ready", False):
+        vp = C.c_void_p
+        lib.orc_sample_volume.argtypes = [vp] * 8 + [C.c_float, C.c_float, C.c_float, vp]
+        lib._sample_ready = True
+    sr = np.float32(params.psmoothradius)
+    gk = np.float32(1.0) / np.float32(_libm_powf(np.float32(3.141592) * np.float32(2.0) * sr * sr, 1.5))
+    h2 = np.float32(2.0 * float(np.float32(params.r2)) / 8.0)
+    r = np.array(res, np.int32)
+    out = np.zeros((res[2], res[1], res[0]), np.float32)
+    pos = np.ascontiguousarray(pos, np.float32)
+    off = np.ascontiguousarray(off, np.uint32)
+    cnt = np.ascontiguousarray(cnt, np.uint32)
+    lib.orc_sample_volume(C.byref(params), _p(pos), _p(off), _p(cnt), _p(r), _p(np.array(bmin, np.float32)),
+                          _p(np.array(bmax, np.float32)), C.c_float(scalar), C.c_float(gk), C.c_float(h2), _p(out))
+    return out
+
+
+def _libm_powf(x, y):
+    libm = C.CDLL("libm.so.6")
+    libm.powf.restype = C.c_float
+    libm.powf.argtypes = [C.c_float, C.c_float]
+    return np.float32(libm.powf(C.c_float(x), C.c_float(y)))
