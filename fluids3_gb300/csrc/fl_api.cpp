@@ -18,7 +18,7 @@
 #include "fl_internal.h"
 
 // Pairs the density pass records per point for the force pass (HBM: 4 B
-// per entry, 192 B per point of capacity).
+// per entry, 512 B per point of capacity).
 static const int kPairListCap = 128;
 
 // ---------------------------------------------------------------------------
@@ -555,6 +555,43 @@ extern "C" int fl_set_particles(fl_system *s, int n, const float *pos, const flo
     }
     // the caller may reuse its host arrays on return
     FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    fl_reset_progress(s);
+    return FL_OK;
+}
+
+// AddParticle (fluids4.0/fluid_system.cpp:274-290) k times with the given
+// values: the points go after the live ones, force and density start at 0.
+extern "C" int fl_add_particles(fl_system *s, int k, const float *pos, const float *vel, const float *veval,
+                                const uint32_t *clr) {
+    if (!s || (k > 0 && !pos)) return fl_fail(FL_ERR_ARG, "fl_add_particles: null system or pos");
+    if (k < 0) return fl_fail(FL_ERR_ARG, "fl_add_particles: k < 0");
+    if (s->batched) return fl_fail(FL_ERR_STATE, "fl_add_particles: a batched system has fixed scene sizes");
+    if ((long long)s->n + k > s->max_points)
+        return fl_fail(FL_ERR_CAPACITY, "fl_add_particles: %d + %d points exceed capacity %d", s->n, k, s->max_points);
+    if (k == 0) return FL_OK;
+    destroy_graph(s);
+    const int base = s->n;
+    const size_t v3 = 12 * (size_t)k;
+    FL_TRY(fl_ensure_stage(s, 3 * v3));
+    const float *src3[3] = {pos, vel, veval};
+    const int fid[3] = {F_POS, F_VEL, F_VEVAL};
+    for (int q = 0; q < 3; q++) {
+        float4 *dst = s->f[fid[q]].cur<float4>() + base;
+        if (!src3[q]) {
+            FL_CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(float4) * (size_t)k, s->stream));
+            continue;
+        }
+        float *slice = (float *)((char *)s->stage + q * v3);
+        FL_CUDA_TRY(cudaMemcpyAsync(slice, src3[q], v3, cudaMemcpyHostToDevice, s->stream));
+        FL_TRY(fl_launch_unpack3(s, slice, dst, k));
+    }
+    FL_CUDA_TRY(cudaMemsetAsync(s->f[F_FORCE].cur<float4>() + base, 0, sizeof(float4) * (size_t)k, s->stream));
+    FL_CUDA_TRY(cudaMemsetAsync(s->f[F_PRESS].cur<float>() + base, 0, 4 * (size_t)k, s->stream));
+    uint32_t *cdst = s->f[F_CLR].cur<uint32_t>() + base;
+    if (clr) FL_CUDA_TRY(cudaMemcpyAsync(cdst, clr, 4 * (size_t)k, cudaMemcpyHostToDevice, s->stream));
+    else FL_CUDA_TRY(cudaMemsetAsync(cdst, 0, 4 * (size_t)k, s->stream));
+    FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->n = base + k;
     fl_reset_progress(s);
     return FL_OK;
 }

@@ -195,6 +195,15 @@ class FluidSystem:
                  FGRIDOFF: "gridoff"}
         return {v: self.GetBuffer(k) for k, v in names.items()}
 
+    def AddParticles(self, pos, vel=None, veval=None, clr=None) -> None:
+        """AddParticle (cpp:274-290) for every row of pos (N,3): appended
+        after the live points."""
+        pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+        k = pos.shape[0]
+        f3 = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float32).reshape(k, 3)
+        c = None if clr is None else np.ascontiguousarray(clr, dtype=np.uint32).reshape(k)
+        call("fl_add_particles", self._h, k, *[_ptr(a) for a in (pos, f3(vel), f3(veval), c)])
+
     def SavePoints(self, path, with_veval: bool = True) -> None:
         """SavePoints (cpp:1511-1545): the points to a .pts file; with_veval
         adds the evaluated velocity for an exact resume."""

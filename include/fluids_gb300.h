@@ -188,6 +188,14 @@ int fl_set_particles(fl_system *s, int n, const float *pos, const float *vel,
                      const float *veval, const float *force, const float *press,
                      const uint32_t *clr);
 
+/* AddParticle (cpp:274-290), k at a time, for emitters (AddEmit, cpp:336-361):
+ * k points from host arrays appended after the live ones (vel, veval and
+ * clr may be NULL: zero); force and density start at zero. FL_ERR_CAPACITY
+ * beyond max_points; single-scene systems only. Like fl_set_particles it
+ * invalidates an open tape. */
+int fl_add_particles(fl_system *s, int k, const float *pos, const float *vel, const float *veval,
+                     const uint32_t *clr);
+
 /* Copy buffer `buf_id` (FL_F* id) into host memory in fluid.h layout.
  * `bytes` must be at least the buffer size (N or C elements). */
 int fl_get_buffer(fl_system *s, int buf_id, void *host_dst, size_t bytes);

@@ -438,3 +438,36 @@ def test_points_file_resume_is_exact(tmp_path):
         b.LoadPoints(path)
         assert_bit_equal(b.GetBuffer(F.FPOS), a.GetBuffer(F.FPOS), "3-field pos")
         assert not b.GetBuffer(F.FVEVAL).any()
+
+
+def test_emitter_appends_points_and_steps_like_the_oracle():
+    """EmitParticles / AddEmit through fl_add_particles: every third frame
+    64 points join a 2,000-point dam break (capacity 2,400); each step after
+    an emission equals the oracle's step on the same points, bit for bit."""
+    from fluids3_gb300.emit import Emitter
+    sc = scenes.dam_break(n=2000)
+    p = sc.params
+    em = Emitter(pos=(-20.0, 40.0, -5.0), every=3, count=64, azimuth=0.0, tilt=90.0, speed=1.5,
+                 spread=(15.0, 10.0), spacing=1.475, seed=9)
+    st = O.State.new(p, sc.pos, sc.vel, sc.veval, sc.clr)
+    t = 0.0
+    with F.FluidSystem(p, 2400) as s:
+        s.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
+        mirror = Emitter(**{k: getattr(em, k) for k in ("pos", "every", "count", "azimuth", "tilt", "speed",
+                                                         "spread", "spacing", "seed")})
+        for frame in range(1, 10):
+            added = em.step(s)
+            mirror.frame += 1
+            if frame % 3 == 0:
+                pos, vel, clr = mirror.points(np.float32(t))
+                st = O.State.new(p, np.concatenate([st.pos, pos]), np.concatenate([st.vel, vel]),
+                                 np.concatenate([st.veval, vel]), np.concatenate([st.clr, clr]))
+                assert added == 64
+            t = O.step(p, st, t)
+            assert s.NumPoints() == st.n
+            assert_bit_equal(s.GetBuffer(F.FPOS), st.pos, f"frame {frame} pos")
+            assert_bit_equal(s.GetBuffer(F.FCLR), st.clr, f"frame {frame} clr")
+        assert s.NumPoints() == 2192
+        with pytest.raises(F.FluidsError) as e:
+            s.AddParticles(np.zeros((300, 3), np.float32))
+        assert e.value.code == -4
