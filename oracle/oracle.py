@@ -250,6 +250,18 @@ class RefKernels:
         self.rebind()
         self.lib.ref_advance(C.c_float(time), C.c_float(dt), C.c_float(ss), self.n, threads)
 
+    def sample(self, res, bmin, bmax, scalar):
+        """sampleParticles over the current sorted state; (z, y, x) array."""
+        self.rebind()
+        if not getattr(self.lib, "_sample_ready", False):
+            self.lib.ref_sample_particles.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                                                      C.c_void_p, C.c_int, C.c_float]
+            self.lib._sample_ready = True
+        out = np.zeros((res[2], res[1], res[0]), np.float32)
+        self.lib.ref_sample_particles(_p(out), res[0], res[1], res[2], _p(np.array(bmin, np.float32)),
+                                      _p(np.array(bmax, np.float32)), self.n, C.c_float(scalar))
+        return out
+
     def run(self, steps, time, threads=1) -> float:
         self.rebind()
         t = C.c_float(time)
@@ -380,7 +392,7 @@ def sample_volume(params, pos, off, cnt, res, bmin, bmax, scalar):
     lib = orc()
     if not getattr(lib, "_sample_ready", False):
         vp = C.c_void_p
-        lib.orc_sample_volume.argtypes = [vp] * 8 + [C.c_float, C.c_float, C.c_float, vp]
+        lib.orc_sample_volume.argtypes = [vp] * 7 + [C.c_float, C.c_float, C.c_float, vp]
         lib._sample_ready = True
     sr = np.float32(params.psmoothradius)
     gk = np.float32(1.0) / np.float32(_libm_powf(np.float32(3.141592) * np.float32(2.0) * sr * sr, 1.5))

@@ -128,6 +128,27 @@ void ref_advance(float time, float dt, float ss, int n, int threads) {
     for (int i = 0; i < n; i++) { set_thread(i); advanceParticles(time, dt, ss, n); }
 }
 
+/* sampleParticles (fluid_kernels.cu:263-308) once per voxel, blockIdx = the
+ * voxel (blockDim 1). gausskern as UpdateParamsCUDA derives it (cpp:2302).
+ * The kernel stores an out-of-range voxel at another index than an
+ * in-range one; callers keep the box inside the scan range. */
+void ref_sample_particles(float *brick, int rx, int ry, int rz, const float *bmin, const float *bmax, int n,
+                          float scalar) {
+    const float sr = fparam.psmoothradius;
+    fparam.gausskern = 1.0f / pow(3.141592f * 2.0f * sr * sr, 3.0f / 2.0f);
+    const uint3 res = make_uint3((unsigned)rx, (unsigned)ry, (unsigned)rz);
+    const float3 lo = make_float3(bmin[0], bmin[1], bmin[2]);
+    const float3 hi = make_float3(bmax[0], bmax[1], bmax[2]);
+    blockDim = make_uint3(1, 1, 1);
+    threadIdx = make_uint3(0, 0, 0);
+    for (int z = 0; z < rz; z++)
+        for (int y = 0; y < ry; y++)
+            for (int x = 0; x < rx; x++) {
+                blockIdx = make_uint3((unsigned)x, (unsigned)y, (unsigned)z);
+                sampleParticles(brick, res, lo, hi, n, scalar);
+            }
+}
+
 /* `steps` RUN_GPU_FULL steps starting at *time; *time advances by dt each step. */
 void ref_run(int n, int steps, float *time, float dt, int threads) {
     for (int s = 0; s < steps; s++) {

@@ -195,3 +195,24 @@ def test_checker_catches_a_planted_mistake(golden_dir):
     if not np.array_equal(gndx, g["sort_gndx"]):
         with pytest.raises(AssertionError):
             assert_bit_equal(gndx, g["sort_gndx"], "planted gndx swap")
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference tree not present at build time")
+def test_sample_volume_restatement_matches_reference_source():
+    """orc_sample_volume against the reference's sampleParticles kernel body
+    built for the host, on a sorted 2,000-point dam break, over boxes inside
+    the scan range (the reference stores out-of-range voxels at another
+    index than in-range ones)."""
+    sc = scenes.dam_break(n=2000)
+    p = sc.params
+    R = O.RefKernels(p, sc.pos, sc.vel, sc.veval, sc.clr)
+    R.insert(); R.prefix_sum(1); R.counting_sort()
+    lo = np.array(p.gridMin[:], np.float32) + np.float32(1.2) / np.array(p.gridDelta[:], np.float32)
+    hi = np.array(p.gridMax[:], np.float32) - np.float32(2.5) / np.array(p.gridDelta[:], np.float32)
+    cnt = np.append(R.buf["gridcnt"], 0).astype(np.uint32)
+    off = np.append(R.buf["gridoff"], 0).astype(np.uint32)
+    for res in ((9, 7, 5), (16, 16, 16)):
+        want = R.sample(res, lo, hi, 0.01)
+        got = O.sample_volume(p, R.buf["pos"], off, cnt, res, lo, hi, 0.01)
+        assert want.max() > 0
+        assert_bit_equal(got, want, f"sample {res}")
