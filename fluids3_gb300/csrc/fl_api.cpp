@@ -517,6 +517,19 @@ extern "C" int fl_host_free(void *p) {
     return FL_OK;
 }
 
+// Page-locked host memory (fl_host_alloc, cudaHostAlloc) is mapped into the
+// device's address space: kernels read and write it directly over the
+// host link, so a transfer needs no staging copy. Returns the device-side
+// address of such memory, or null for pageable memory.
+static void *mapped_device_ptr(const void *host) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return (a.type == cudaMemoryTypeHost) ? a.devicePointer : nullptr;
+}
+
 extern "C" int fl_set_particles(fl_system *s, int n, const float *pos, const float *vel,
                                 const float *veval, const float *force, const float *press,
                                 const uint32_t *clr) {
@@ -539,6 +552,10 @@ extern "C" int fl_set_particles(fl_system *s, int n, const float *pos, const flo
             float4 *dst = s->f[fid[k]].cur<float4>();
             if (!src3[k]) {
                 FL_CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(float4) * (size_t)n, s->stream));
+                continue;
+            }
+            if (const void *mapped = mapped_device_ptr(src3[k])) {
+                FL_TRY(fl_launch_unpack3(s, (const float *)mapped, dst, n));   // read over the host link
                 continue;
             }
             float *slice = (float *)((char *)s->stage + k * v3);
@@ -653,6 +670,13 @@ extern "C" int fl_get_buffer(fl_system *s, int id, void *host, size_t bytes) {
     FL_TRY(buffer_bytes(s, id, &need));
     if (bytes < need) return fl_fail(FL_ERR_ARG, "fl_get_buffer: %zu bytes < %zu needed", bytes, need);
     if (need == 0) return FL_OK;
+    if (id == FL_FPOS || id == FL_FVEL || id == FL_FVEVAL || id == FL_FFORCE) {
+        if (void *mapped = mapped_device_ptr(host)) {   // page-locked: pack straight into it
+            FL_TRY(export_to_device(s, id, mapped));
+            FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+            return FL_OK;
+        }
+    }
     FL_TRY(fl_ensure_stage(s, need));
     FL_TRY(export_to_device(s, id, s->stage));
     FL_CUDA_TRY(cudaMemcpyAsync(host, s->stage, need, cudaMemcpyDeviceToHost, s->stream));
