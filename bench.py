@@ -94,6 +94,23 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def allmax(dist, x: float) -> float:
+    """The largest x over all ranks (the slowest rank's time sets the job's)."""
+    if not dist:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world: int, points_per_rank: int, steps: int, ms_slowest: float) -> float:
+    """Whole-job Mparticle-steps/s: every rank steps its own replica of
+    points_per_rank points; the slowest rank's time is the job's."""
+    return world * points_per_rank * steps / (ms_slowest / 1e3) / 1e6
+
+
 # ---------------------------------------------------------------------------
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons, sampled every 100 ms."""
@@ -531,13 +548,6 @@ def our_arm(args, rank, world, local_rank):
         if dist:
             dist.barrier()
 
-    def allmax(x: float) -> float:
-        if not dist:
-            return x
-        import torch
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
 
     scene = scenes.wave_tank(n=args.n)
     p = scene.params
@@ -562,7 +572,7 @@ def our_arm(args, rank, world, local_rank):
     barrier()
     time.sleep(0.25)
     clocks.stop()
-    ms = allmax(ms)
+    ms = allmax(dist, ms)
     status = s.DeviceStatus()
 
     # -- per-kernel times: the same K steps again from the saved state, eager,
@@ -604,7 +614,7 @@ def our_arm(args, rank, world, local_rank):
         F._lib.check("fl_get_buffer", lib.fl_get_buffer(s.handle, F.FPOS, vp(pin_out.array), d2h))
     te1 = time.perf_counter()
     barrier()
-    e2e_s = allmax(te1 - te0)
+    e2e_s = allmax(dist, te1 - te0)
     for a in (pin_pos, pin_vel, pin_vev, pin_clr, pin_out):
         a.free()
     s.close()
@@ -615,7 +625,7 @@ def our_arm(args, rank, world, local_rank):
     batched = batched_comparison(args) if args.batch_scenes > 0 else None
     adjoint = adjoint_measurements(args) if args.adjoint_steps > 0 else None
     fit = fit_measurement(args) if args.fit_iters > 0 else None
-    value = world * scene.n * args.steps / (ms / 1e3) / 1e6
+    value = job_value(world, scene.n, args.steps, ms)
     dominant = max((k for k in phases if k != "scan"), key=lambda k: phases[k])
     dur_ms = phases[dominant]
     algo = ALGO_BYTES[dominant] * n_in
