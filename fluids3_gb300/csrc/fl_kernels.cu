@@ -423,8 +423,9 @@ __device__ __forceinline__ void drain_hits(const DevParams &P, ForcePoint &fp, u
 
 // The force on point i (all 32 lanes of the warp must call this). With
 // LIST the pairs come from the density pass's list (every lane draining its
-// own list in step); a warp with a point whose pairs overflowed the list
-// walks its candidates again instead.
+// own list in step); a point whose pairs overflowed the list walks its
+// candidates again. Without LIST (no density pass since the last sort) the
+// warp walks and drains per-lane hit lists in shared memory.
 template <bool PRUNE, bool LIST>
 __device__ __forceinline__ float3 force_of(const DevParams &P, int i, bool active, uint32_t gc,
                                            const float4 *__restrict__ pos,
@@ -435,8 +436,6 @@ __device__ __forceinline__ float3 force_of(const DevParams &P, int i, bool activ
                                            const uint32_t *__restrict__ upbits,
                                            const uint32_t *__restrict__ hitlist,
                                            const uint32_t *__restrict__ hitcnt) {
-    __shared__ uint32_t s_hits[kHitCap * kForceThreads];
-    uint32_t *hits = s_hits + threadIdx.x;
     ForcePoint fp;
     fp.f = make_float3(0.0f, 0.0f, 0.0f);
     uint32_t my_code = 0;
@@ -449,15 +448,38 @@ __device__ __forceinline__ float3 force_of(const DevParams &P, int i, bool activ
         my_code = __float_as_uint(fp.p.w);
         base = (int)gc - P.nadj;
     }
-    if (LIST) {
+    if constexpr (LIST) {
+        // No shared memory here, so the whole unified L1 caches the
+        // neighbour reads. A lane whose list overflowed (rare with 128
+        // entries) walks its candidates and adds each pair as found, in the
+        // same order.
         const uint32_t nh = active ? hitcnt[i] : 0u;
-        if (!__any_sync(0xffffffffu, nh > (uint32_t)P.hcap)) {
+        const bool over = nh > (uint32_t)P.hcap;
+        if (!__any_sync(0xffffffffu, over)) {
             const uint32_t most = __reduce_max_sync(0xffffffffu, nh);
             for (uint32_t t = 0; t < most; t++)
                 if (t < nh) add_pair_force(P, fp, hitlist[list_at(P, i, t)], pos, veval, press);
             return fp.f;
         }
+        if (!over) {
+            for (uint32_t t = 0; t < nh; t++) add_pair_force(P, fp, hitlist[list_at(P, i, t)], pos, veval, press);
+            return fp.f;
+        }
+        for (int c = 0; c < P.gridAdjCnt; c++) {
+            CandIter it;
+            cand_begin<PRUNE>(it, P, c, base + P.adj[c], my_code, true, off, cnt, upbits);
+            uint32_t j;
+            while (cand_next<PRUNE>(it, P, upbits, j)) {
+                const float4 q = pos[j];
+                const float dx = fp.p.x - q.x, dy = fp.p.y - q.y, dz = fp.p.z - q.z;
+                const float dsq = dx * dx + dy * dy + dz * dz;
+                if (dsq < P.rd2 && dsq > 0.0f) add_pair_force(P, fp, j, pos, veval, press);
+            }
+        }
+        return fp.f;
     }
+    __shared__ uint32_t s_hits[kHitCap * kForceThreads];
+    uint32_t *hits = s_hits + threadIdx.x;
     uint32_t nhits = 0;
     for (int c = 0; c < P.gridAdjCnt; c++) {
         CandIter it;
