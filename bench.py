@@ -85,6 +85,7 @@ def parse():
     ap.add_argument("--adjoint-steps", type=int, default=200,
                     help="steps of the differentiated 65,536-point rollout (0 skips the adjoint section)")
     ap.add_argument("--adjoint-every", type=int, default=20, help="checkpoint interval of that rollout")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the compiled block shapes")
     ap.add_argument("--fit-iters", type=int, default=40,
                     help="iterations of the 64-scene batched parameter fit (0 skips it)")
     return ap.parse_args()
@@ -299,6 +300,7 @@ def batched_comparison(args):
     b = F.FluidSystem.batch([sc.params for sc in scs], [sc.n for sc in scs])
     b.SetParticles(cat["pos"], cat["vel"], cat["veval"], clr=cat["clr"])
     b.RunSteps(max(args.warmup, 3))
+    tuned = b.Autotune(3) if not args.no_autotune else None
     b.SaveCheckpoint(0)
     ms_b = b.TimeSteps(k, graph=True, restart_every=seg, restart_slot=0)
     b.Sync()
@@ -329,6 +331,7 @@ def batched_comparison(args):
     return {"scenes": len(scs), "points": total, "steps": k, "value": vb, "unit": METRIC,
             "one_at_a_time_value": vs, "speedup": vb / vs, "ms_per_step": ms_b / k,
             "one_at_a_time_ms_per_step": ms_seq / k, "scenes_bit_identical": same,
+            "autotuned_block_shapes": tuned, "one_at_a_time_block_shapes": "compiled defaults",
             "workload": "scenes log-uniform 2,048..65,536 points, fill U[0.2,0.6] of own box, "
                         "visc U[0.1,0.5], rest density U[500,700], dam-break parameters otherwise"}
 
@@ -558,6 +561,7 @@ def our_arm(args, rank, world, local_rank):
     # per-kernel region below replays exactly the timed steps
     s.RunSteps(max(args.warmup, 3))
     s.Sync()
+    tuned = s.Autotune(3) if not args.no_autotune else None
     s.SaveCheckpoint(0)
 
     # -- timed region: exactly K steps, graph replay ---------------------------
@@ -657,6 +661,7 @@ def our_arm(args, rank, world, local_rank):
         "cpu_baseline": cpu,
         "e2e": {"value": world * n * e2e_steps / e2e_s / 1e6, "unit": METRIC, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+        "autotuned_block_shapes": tuned,
         "batched": batched,
         "adjoint": adjoint,
         "fit": fit,

@@ -152,7 +152,7 @@ static void free_all(fl_system *s) {
     cudaFree(s->dev_err);
     cudaFree(s->time_dev);
     cudaFree(s->stage);
-    for (int c = 0; c < FL_MAX_CHECKPOINTS; c++) {
+    for (int c = 0; c <= FL_MAX_CHECKPOINTS; c++) {
         for (int k = 0; k < F_COUNT; k++) cudaFree(s->ckpt[c][k]);
         cudaFree(s->ckpt_time[c]);
     }
@@ -954,10 +954,17 @@ extern "C" int fl_run_steps(fl_system *s, int nsteps) {
     return FL_OK;
 }
 
+static int save_slot(fl_system *s, int slot);
+static int restore_slot(fl_system *s, int slot);
+
 extern "C" int fl_checkpoint_save(fl_system *s, int slot) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_checkpoint_save: null system");
     if (slot < 0 || slot >= FL_MAX_CHECKPOINTS)
         return fl_fail(FL_ERR_ARG, "fl_checkpoint_save: slot %d outside [0, %d)", slot, FL_MAX_CHECKPOINTS);
+    return save_slot(s, slot);
+}
+
+static int save_slot(fl_system *s, int slot) {
     const size_t np = (size_t)(s->max_points > 0 ? s->max_points : 1);
     if (!s->ckpt_time[slot]) {
         for (int k = 0; k < F_COUNT; k++) FL_TRY(fl_dalloc(&s->ckpt[slot][k], s->f[k].esz * np));
@@ -979,6 +986,10 @@ extern "C" int fl_checkpoint_restore(fl_system *s, int slot) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_checkpoint_restore: null system");
     if (slot < 0 || slot >= FL_MAX_CHECKPOINTS || !s->ckpt_time[slot])
         return fl_fail(FL_ERR_ARG, "fl_checkpoint_restore: slot %d holds no checkpoint", slot);
+    return restore_slot(s, slot);
+}
+
+static int restore_slot(fl_system *s, int slot) {
     s->n = s->ckpt_n[slot];
     for (int k = 0; k < F_COUNT; k++)
         if (s->n > 0)
@@ -990,6 +1001,54 @@ extern "C" int fl_checkpoint_restore(fl_system *s, int slot) {
     s->time_host_valid = s->ckpt_host_valid[slot];
     fl_reset_progress(s);
     return FL_OK;
+}
+
+// Block-shape autotuner: for each tunable pass in turn (density, force,
+// sort) every candidate block size is timed over `steps` eager steps from
+// the same saved state, the others held at their best so far; the state is
+// restored at the end. Block sizes change no result: each point's work is
+// one thread's (or one warp's, the sort's cell) whatever the block.
+extern "C" int fl_autotune(fl_system *s, int steps, int *chosen) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_autotune: null system");
+    if (steps < 1) return fl_fail(FL_ERR_ARG, "fl_autotune: steps < 1");
+    if (fl_tape_recording(s)) return fl_fail(FL_ERR_STATE, "fl_autotune: a tape is recording (fl_tape_end first)");
+    if (s->n == 0) return FL_OK;
+    const int slot = FL_MAX_CHECKPOINTS;   // the tuner's own checkpoint slot
+    FL_TRY(save_slot(s, slot));
+    int *knob[3] = {&s->blk_density, &s->blk_force, &s->blk_sort};
+    const int cand[3][3] = {{64, 128, 256}, {32, 64, 128}, {64, 128, 256}};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    FL_CUDA_TRY(cudaEventCreate(&e0));
+    cudaError_t ce = cudaEventCreate(&e1);
+    if (ce != cudaSuccess) { cudaEventDestroy(e0); return fl_fail(FL_ERR_CUDA, "fl_autotune: event"); }
+    int r = FL_OK;
+    for (int k = 0; k < 3 && r == FL_OK; k++) {
+        int best = 0;
+        float best_ms = 0.0f;
+        for (int c = 0; c < 3 && r == FL_OK; c++) {
+            *knob[k] = cand[k][c];
+            destroy_graph(s);
+            if ((r = restore_slot(s, slot)) != FL_OK) break;
+            if ((r = fl_run(s)) != FL_OK) break;            // warm: first launch of this shape
+            if ((r = restore_slot(s, slot)) != FL_OK) break;
+            cudaEventRecord(e0, s->stream);
+            for (int t = 0; t < steps && r == FL_OK; t++) r = fl_run(s);
+            cudaEventRecord(e1, s->stream);
+            if (cudaEventSynchronize(e1) != cudaSuccess) { r = fl_fail(FL_ERR_CUDA, "fl_autotune: timing"); break; }
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (best == 0 || ms < best_ms) { best = cand[k][c]; best_ms = ms; }
+        }
+        *knob[k] = best;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    destroy_graph(s);
+    if (r == FL_OK) r = restore_slot(s, slot);
+    if (r == FL_OK && chosen) {
+        chosen[0] = s->blk_density; chosen[1] = s->blk_force; chosen[2] = s->blk_sort;
+    }
+    return r;
 }
 
 extern "C" int fl_device_status(fl_system *s, uint32_t *flags) {

@@ -142,17 +142,22 @@ struct fl_system {
     int have_insert, have_offsets, have_grid;
     int offsets_inclusive;
 
+    // threads per block of the sort, density and force passes (0: the
+    // compiled default); set by fl_autotune, results do not depend on them
+    int blk_sort, blk_density, blk_force;
+
     // graph replay for fl_run_steps
     cudaGraphExec_t graph_exec;
     int graph_steps;
     int graph_live[F_COUNT];
 
     // checkpoints: per slot, one copy of every field's live buffer + time
-    void *ckpt[FL_MAX_CHECKPOINTS][F_COUNT];
-    float *ckpt_time[FL_MAX_CHECKPOINTS];
-    int ckpt_n[FL_MAX_CHECKPOINTS];
-    float ckpt_host_time[FL_MAX_CHECKPOINTS];
-    int ckpt_host_valid[FL_MAX_CHECKPOINTS];
+    // one more slot than the caller's: the autotuner's own
+    void *ckpt[FL_MAX_CHECKPOINTS + 1][F_COUNT];
+    float *ckpt_time[FL_MAX_CHECKPOINTS + 1];
+    int ckpt_n[FL_MAX_CHECKPOINTS + 1];
+    float ckpt_host_time[FL_MAX_CHECKPOINTS + 1];
+    int ckpt_host_valid[FL_MAX_CHECKPOINTS + 1];
 
     // adjoint tape (fl_tape.cpp), null until fl_tape_begin
     struct fl_tape *tape;

@@ -256,7 +256,7 @@ __device__ __forceinline__ CellCtx cell_ctx(const DevParams &P0, const SceneTab 
 template <int MODE, bool BATCH>
 __global__ void __launch_bounds__(kThreads)
 k_sort_cells(const __grid_constant__ SortArgs a) {
-    const int c = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (c >= a.gcells) return;
     const uint32_t m = a.cnt[c];
     if (m == 0) return;
@@ -787,12 +787,12 @@ int fl_launch_sort_cells(fl_system *s, int mode) {
     a.T = fl_scene_tab(s);
     a.prune = (mode >= 1) ? s->D.prune : 0;
     a.upbits = s->upbits;
-    const int warps_per_block = kThreads / 32;
-    const int grid = blocks_for((long long)s->gcells, warps_per_block);
+    const int bs = s->blk_sort ? s->blk_sort : kThreads;
+    const int grid = blocks_for((long long)s->gcells, bs / 32);
     if (mode == 0) {
         a.gndx_pre = s->f[F_GNDX].cur<uint32_t>();
         auto kern = s->batched ? k_sort_cells<0, true> : k_sort_cells<0, false>;
-        kern<<<grid, kThreads, 0, s->stream>>>(a);
+        kern<<<grid, bs, 0, s->stream>>>(a);
     } else {
         a.pos_in = s->f[F_POS].cur<float4>(); a.pos_out = s->f[F_POS].nxt<float4>();
         a.vel_in = s->f[F_VEL].cur<float4>(); a.vel_out = s->f[F_VEL].nxt<float4>();
@@ -804,7 +804,7 @@ int fl_launch_sort_cells(fl_system *s, int mode) {
             FL_CUDA_TRY(cudaMemsetAsync(s->upbits, 0, (mode == 2 ? 2 : 1) * fl_upbits_bytes(s), s->stream));
         auto kern = (mode == 2) ? (s->batched ? k_sort_cells<2, true> : k_sort_cells<2, false>)
                                 : (s->batched ? k_sort_cells<1, true> : k_sort_cells<1, false>);
-        kern<<<grid, kThreads, 0, s->stream>>>(a);
+        kern<<<grid, bs, 0, s->stream>>>(a);
         s->codes_valid = s->D.prune;
     }
     FL_LAUNCH_CHECK("sort_cells");
@@ -852,7 +852,8 @@ static auto density_kernel(bool prune) {
 int fl_launch_density(fl_system *s) {
     if (s->n == 0) return FL_OK;
     auto kern = s->batched ? density_kernel<true>(use_prune(s)) : density_kernel<false>(use_prune(s));
-    kern<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(
+    const int bs = s->blk_density ? s->blk_density : kThreads;
+    kern<<<blocks_for(s->n, bs), bs, 0, s->stream>>>(
         s->D, fl_scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt,
         s->upbits, s->f[F_PRESS].cur<float>(), s->hitlist, s->hitcnt);
     FL_LAUNCH_CHECK("density");
@@ -874,7 +875,8 @@ int fl_launch_force(fl_system *s) {
     const bool pr = use_prune(s);
     auto kern = s->lists_valid ? (s->batched ? force_kernel<true, true>(pr) : force_kernel<true, false>(pr))
                                : (s->batched ? force_kernel<false, true>(pr) : force_kernel<false, false>(pr));
-    kern<<<blocks_for(s->n, kForceThreads), kForceThreads, 0, s->stream>>>(
+    const int bs = s->blk_force ? s->blk_force : kForceThreads;
+    kern<<<blocks_for(s->n, bs), bs, 0, s->stream>>>(
         s->D, fl_scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->f[F_VEVAL].cur<float4>(),
         s->f[F_PRESS].cur<float>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt, s->upbits,
         s->hitlist, s->hitcnt, s->f[F_FORCE].cur<float4>());
@@ -887,7 +889,8 @@ int fl_launch_force_advance(fl_system *s, float dt) {
     auto kern = s->lists_valid
                     ? (s->batched ? force_advance_kernel<true, true>(pr) : force_advance_kernel<true, false>(pr))
                     : (s->batched ? force_advance_kernel<false, true>(pr) : force_advance_kernel<false, false>(pr));
-    kern<<<blocks_for(s->n > 0 ? s->n : 1, kForceThreads), kForceThreads, 0, s->stream>>>(
+    const int bs = s->blk_force ? s->blk_force : kForceThreads;
+    kern<<<blocks_for(s->n > 0 ? s->n : 1, bs), bs, 0, s->stream>>>(
         s->D, fl_scene_tab(s), s->n, s->time_dev, s->time_slot, dt, s->f[F_POS].cur<float4>(),
         s->f[F_VEVAL].cur<float4>(), s->f[F_PRESS].cur<float>(), s->f[F_GCELL].cur<uint32_t>(), s->off,
         s->cnt, s->upbits, s->hitlist, s->hitcnt,

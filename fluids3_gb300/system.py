@@ -333,6 +333,12 @@ class FluidSystem:
     def TapeEnd(self) -> None:
         call("fl_tape_end", self._h)
 
+    def Autotune(self, steps: int = 3) -> dict:
+        """Pick the fastest block shapes for this system's work (state kept)."""
+        out = (C.c_int * 3)()
+        call("fl_autotune", self._h, int(steps), out)
+        return {"density": out[0], "force": out[1], "sort": out[2]}
+
     # -- timing ---------------------------------------------------------------
     def SetTiming(self, enable: bool) -> None:
         call("fl_set_timing", self._h, 1 if enable else 0)

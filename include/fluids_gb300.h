@@ -284,6 +284,13 @@ int fl_run_steps(fl_system *s, int nsteps);
 int fl_checkpoint_save(fl_system *s, int slot);
 int fl_checkpoint_restore(fl_system *s, int slot);
 
+/* Block-shape autotuner (no counterpart in the reference): times each of
+ * the density, force and sort passes at three block sizes over `steps`
+ * steps from the current state (restored afterwards) and keeps the fastest;
+ * chosen (nullable) gets the threads per block of density, force, sort.
+ * Results are identical for every block size. Invalidates an open tape. */
+int fl_autotune(fl_system *s, int steps, int *chosen);
+
 /* Wait for the system stream; returns FL_ERR_DEVICE if a kernel raised the
  * device error word since the last fl_sync (bits in *dev_flags if non-NULL). */
 int fl_sync(fl_system *s);

@@ -165,3 +165,18 @@ def test_batched_fit_recovers_viscosity_on_a_small_batch():
     start_err = np.abs(0.3 - res.hidden_visc) / res.hidden_visc
     assert res.losses[-1] < 0.5 * res.losses[0], res.losses
     assert np.median(res.visc_rel_err) < 0.5 * np.median(start_err), (res.visc, res.hidden_visc)
+
+
+def test_batched_autotune_changes_no_result():
+    scs = scenes.batch_scenes(nscenes=6, nmin=1500, nmax=6000, seed=41)
+    cat = scenes.concat(scs)
+    outs = []
+    for tune in (False, True):
+        with F.FluidSystem.batch([sc.params for sc in scs], [sc.n for sc in scs]) as b:
+            b.SetParticles(cat["pos"], cat["vel"], cat["veval"], clr=cat["clr"])
+            b.RunSteps(3)
+            if tune:
+                b.Autotune(2)
+            b.RunSteps(5)
+            outs.append(b.GetBuffer(F.FPOS))
+    assert_bit_equal(outs[1], outs[0], "autotuned batch")

@@ -471,3 +471,23 @@ def test_emitter_appends_points_and_steps_like_the_oracle():
         with pytest.raises(F.FluidsError) as e:
             s.AddParticles(np.zeros((300, 3), np.float32))
         assert e.value.code == -4
+
+
+def test_autotune_changes_no_result():
+    """fl_autotune picks block shapes by timing; the steps after it equal the
+    steps with the compiled shapes bit for bit, and the state it started
+    from is left in place."""
+    sc = scenes.wave_tank(n=100_000)
+    with F.FluidSystem(sc.params, sc.n) as a, F.FluidSystem(sc.params, sc.n) as b:
+        for s in (a, b):
+            s.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
+            s.RunSteps(5)
+        before = a.GetBuffer(F.FPOS)
+        chosen = a.Autotune(2)
+        assert chosen["density"] in (64, 128, 256) and chosen["force"] in (32, 64, 128)
+        assert chosen["sort"] in (64, 128, 256)
+        assert_bit_equal(a.GetBuffer(F.FPOS), before, "state kept")
+        a.RunSteps(6)
+        b.RunSteps(6)
+        for k in (F.FPOS, F.FVEL, F.FVEVAL, F.FPRESS):
+            assert_bit_equal(a.GetBuffer(k), b.GetBuffer(k), f"buffer {k}")
