@@ -302,6 +302,8 @@ def batched_comparison(args):
     b.RunSteps(max(args.warmup, 3))
     tuned = b.Autotune(3) if not args.no_autotune else None
     b.SaveCheckpoint(0)
+    b.RunSteps(2)                       # capture the graph for the tuned shapes
+    b.RestoreCheckpoint(0)
     ms_b = b.TimeSteps(k, graph=True, restart_every=seg, restart_slot=0)
     b.Sync()
     st_b = {f: b.GetBuffer(getattr(F, "F" + f.upper())) for f in ("pos", "vel", "veval", "gcell")}
@@ -563,6 +565,8 @@ def our_arm(args, rank, world, local_rank):
     s.Sync()
     tuned = s.Autotune(3) if not args.no_autotune else None
     s.SaveCheckpoint(0)
+    s.RunSteps(2)                       # capture the graph for the tuned shapes
+    s.RestoreCheckpoint(0)
 
     # -- timed region: exactly K steps, graph replay ---------------------------
     clocks = ClockSampler(local_rank).start()
