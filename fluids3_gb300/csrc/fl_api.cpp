@@ -1051,6 +1051,38 @@ extern "C" int fl_autotune(fl_system *s, int steps, int *chosen) {
     return r;
 }
 
+extern "C" int fl_conservation(fl_system *s, double *out) {
+    if (!s || !out) return fl_fail(FL_ERR_ARG, "fl_conservation: null argument");
+    const int ns = s->nscenes;
+    int most = s->n;
+    std::vector<int> base(ns), cnt(ns);
+    for (int k = 0; k < ns; k++) {
+        base[k] = s->batched ? s->scene_point_base[k] : 0;
+        cnt[k] = s->batched ? s->scene_n[k] : s->n;
+        if (s->batched && k == 0) most = 0;
+        if (s->batched && cnt[k] > most) most = cnt[k];
+    }
+    const int nchunks = fl_conservation_chunks(most);
+    const size_t vals = (size_t)ns * nchunks * FL_CONSERVATION_VALUES;
+    const size_t bytes = sizeof(double) * vals + 2 * sizeof(int) * (size_t)ns + 64;
+    FL_TRY(fl_ensure_stage(s, bytes));
+    double *partial = (double *)s->stage;
+    int *dbase = (int *)(partial + vals), *dcnt = dbase + ns;
+    FL_CUDA_TRY(cudaMemcpyAsync(dbase, base.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s->stream));
+    FL_CUDA_TRY(cudaMemcpyAsync(dcnt, cnt.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s->stream));
+    FL_TRY(fl_launch_conservation(s, dbase, dcnt, nchunks, partial));
+    std::vector<double> h(vals);
+    FL_CUDA_TRY(cudaMemcpyAsync(h.data(), partial, sizeof(double) * vals, cudaMemcpyDeviceToHost, s->stream));
+    FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    for (int k = 0; k < ns; k++)
+        for (int v = 0; v < FL_CONSERVATION_VALUES; v++) {
+            double t = 0.0;
+            for (int c = 0; c < nchunks; c++) t += h[((size_t)k * nchunks + c) * FL_CONSERVATION_VALUES + v];
+            out[(size_t)k * FL_CONSERVATION_VALUES + v] = t;
+        }
+    return FL_OK;
+}
+
 extern "C" int fl_device_status(fl_system *s, uint32_t *flags) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_device_status: null system");
     uint32_t v = 0;

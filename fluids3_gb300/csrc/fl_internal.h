@@ -238,6 +238,8 @@ int fl_launch_unpack3(fl_system *s, const float *src, float4 *dst, int n);
 int fl_launch_grid_identity(fl_system *s, uint32_t *dst, int n, const uint32_t *gcell);
 int fl_launch_gcell_ref(fl_system *s, uint32_t *dst);
 int fl_launch_integrity(fl_system *s, unsigned long long *bad_dev);
+int fl_conservation_chunks(int max_scene_points);
+int fl_launch_conservation(fl_system *s, const int *sbase, const int *sn, int nchunks, double *partial);
 int fl_launch_sample_volume(fl_system *s, const int res[3], const float bmin[3], const float bmax[3],
                             float scalar, float gausskern, float h2, float *out);
 size_t fl_scan_tile();

@@ -734,6 +734,55 @@ k_sample_volume(const __grid_constant__ DevParams P, int3 res, float3 bmin, floa
     out[idx] = v * scalar;
 }
 
+// Global conservation sums in FP64, per scene: block (chunk, scene) adds up
+// kConsChunk points of its scene into kConsVals partial sums (the only FP64
+// work of the library). Points parked outside the domain (-1000, -1000,
+// -1000) are left out. Values: count, mass, momentum (3), kinetic energy,
+// gravitational potential energy, and the first moment of position (3,
+// world units; divided by the count on the host for the centre of mass).
+constexpr int kConsVals = 10;
+constexpr int kConsChunk = 8192;
+constexpr int kConsThreads = 256;
+
+__global__ void __launch_bounds__(kConsThreads)
+k_conservation(const __grid_constant__ DevParams P0, const SceneTab T, const int *__restrict__ sbase,
+               const int *__restrict__ sn, int nchunks, const float4 *__restrict__ pos,
+               const float4 *__restrict__ vel, double *__restrict__ partial) {
+    const int chunk = blockIdx.x, scene = blockIdx.y;
+    const DevParams &P = T.params ? T.params[scene] : P0;
+    const int b = sbase[scene], m = sn[scene];
+    const double mass = P.pmass, ss = P.sim_scale;
+    double acc[kConsVals];
+#pragma unroll
+    for (int k = 0; k < kConsVals; k++) acc[k] = 0.0;
+    const int lo = chunk * kConsChunk;
+    for (int k = lo + (int)threadIdx.x; k < lo + kConsChunk && k < m; k += kConsThreads) {
+        const float4 x = pos[b + k];
+        if (x.x == -1000.0f && x.y == -1000.0f && x.z == -1000.0f) continue;
+        const float4 v = vel[b + k];
+        acc[0] += 1.0;
+        acc[1] += mass;
+        acc[2] += mass * v.x; acc[3] += mass * v.y; acc[4] += mass * v.z;
+        acc[5] += 0.5 * mass * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
+        acc[6] -= mass * ss * ((double)P.gravity.x * x.x + (double)P.gravity.y * x.y + (double)P.gravity.z * x.z);
+        acc[7] += x.x; acc[8] += x.y; acc[9] += x.z;
+    }
+    __shared__ double sm[kConsVals][kConsThreads / 32];
+    const int w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < kConsVals; k++) {
+        double t = acc[k];
+        for (int d = 16; d > 0; d >>= 1) t += __shfl_down_sync(0xffffffffu, t, d);
+        if ((threadIdx.x & 31u) == 0) sm[k][w] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x < kConsVals) {
+        double t = 0.0;
+        for (int q = 0; q < kConsThreads / 32; q++) t += sm[threadIdx.x][q];
+        partial[((size_t)scene * nchunks + chunk) * kConsVals + threadIdx.x] = t;
+    }
+}
+
 // IntegrityCheck (fluids4.0/fluid_system.cpp:2426-2453): every sorted slot of
 // cell g must carry gcell == g and gndx == its rank; tail slots must be UNDEF.
 template <bool BATCH>
@@ -956,6 +1005,19 @@ int fl_launch_sample_volume(fl_system *s, const int res[3], const float bmin[3],
                                                     make_float3(bmax[0], bmax[1], bmax[2]), scalar, gausskern, h2,
                                                     s->f[F_POS].cur<float4>(), s->off, s->cnt, out);
     FL_LAUNCH_CHECK("sample_volume");
+    return FL_OK;
+}
+
+int fl_conservation_chunks(int max_scene_points) {
+    return max_scene_points <= 0 ? 1 : (max_scene_points + kConsChunk - 1) / kConsChunk;
+}
+
+int fl_launch_conservation(fl_system *s, const int *sbase, const int *sn, int nchunks, double *partial) {
+    dim3 grid((unsigned)nchunks, (unsigned)s->nscenes);
+    k_conservation<<<grid, kConsThreads, 0, s->stream>>>(s->D, fl_scene_tab(s), sbase, sn, nchunks,
+                                                         s->f[F_POS].cur<float4>(), s->f[F_VEL].cur<float4>(),
+                                                         partial);
+    FL_LAUNCH_CHECK("conservation");
     return FL_OK;
 }
 

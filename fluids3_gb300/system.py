@@ -333,6 +333,15 @@ class FluidSystem:
     def TapeEnd(self) -> None:
         call("fl_tape_end", self._h)
 
+    CONSERVATION = ("count", "mass", "px", "py", "pz", "kinetic", "potential", "sx", "sy", "sz")
+
+    def Conservation(self) -> np.ndarray:
+        """(nscenes, 10) FP64 sums: count, mass, momentum, kinetic and
+        potential energy, sum of positions (fl_conservation)."""
+        out = np.zeros((self.NumScenes(), 10), np.float64)
+        call("fl_conservation", self._h, _ptr(out))
+        return out
+
     def Autotune(self, steps: int = 3) -> dict:
         """Pick the fastest block shapes for this system's work (state kept)."""
         out = (C.c_int * 3)()

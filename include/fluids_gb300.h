@@ -284,6 +284,16 @@ int fl_run_steps(fl_system *s, int nsteps);
 int fl_checkpoint_save(fl_system *s, int slot);
 int fl_checkpoint_restore(fl_system *s, int slot);
 
+/* Global conservation sums per scene, in FP64 on the device (rollouts are
+ * chaotic, so they are judged by these drifts rather than by trajectories):
+ * out[10 * scene + k] = count of points not parked outside the domain,
+ * mass, momentum x/y/z (pmass * vel), kinetic energy (1/2 pmass |vel|^2),
+ * gravitational potential energy (-pmass gravity . pos * sim_scale), and
+ * the sum of positions x/y/z (world units; / count = centre of mass). No
+ * counterpart in the reference. */
+#define FL_CONSERVATION_VALUES 10
+int fl_conservation(fl_system *s, double *out);
+
 /* Block-shape autotuner (no counterpart in the reference): times each of
  * the density, force and sort passes at three block sizes over `steps`
  * steps from the current state (restored afterwards) and keeps the fastest;

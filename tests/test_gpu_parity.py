@@ -491,3 +491,45 @@ def test_autotune_changes_no_result():
         b.RunSteps(6)
         for k in (F.FPOS, F.FVEL, F.FVEVAL, F.FPRESS):
             assert_bit_equal(a.GetBuffer(k), b.GetBuffer(k), f"buffer {k}")
+
+
+def _conservation64(p, pos, vel):
+    keep = ~((pos == -1000.0).all(axis=1))
+    x = pos[keep].astype(np.float64)
+    v = vel[keep].astype(np.float64)
+    m = float(np.float32(p.pmass))
+    g = np.array(p.gravity[:], np.float32).astype(np.float64)
+    ss = float(np.float32(p.sim_scale))
+    return np.array([keep.sum(), m * keep.sum(), *(m * v.sum(0)), 0.5 * m * (v * v).sum(),
+                     -m * ss * (x @ g).sum(), *x.sum(0)])
+
+
+def test_conservation_sums_match_fp64_of_the_oracle_state():
+    """fl_conservation (FP64 on the device) against numpy FP64 sums over the
+    oracle's bit-identical states along a 40-step dam break; also per scene
+    of a batch, equal to each scene alone."""
+    sc = scenes.dam_break(n=5000)
+    p = sc.params
+    st = O.State.new(p, sc.pos, sc.vel, sc.veval, sc.clr)
+    t = 0.0
+    with F.FluidSystem(p, sc.n) as s:
+        s.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
+        for seg in range(4):
+            s.RunSteps(10)
+            t = O.run(p, st, 10, t)
+            got = s.Conservation()[0]
+            want = _conservation64(p, st.pos, st.vel)
+            assert np.allclose(got, want, rtol=1e-12, atol=1e-12 * np.abs(want).max()), (seg, got, want)
+        assert got[0] == sc.n and got[5] > 0
+    scs = scenes.batch_scenes(nscenes=3, nmin=1500, nmax=3000, seed=51)
+    cat = scenes.concat(scs)
+    with F.FluidSystem.batch([sc.params for sc in scs], [sc.n for sc in scs]) as b:
+        b.SetParticles(cat["pos"], cat["vel"], cat["veval"], clr=cat["clr"])
+        b.RunSteps(7)
+        per = b.Conservation()
+    for k, sc in enumerate(scs):
+        with F.FluidSystem(sc.params, sc.n) as s:
+            s.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
+            s.RunSteps(7)
+            alone = s.Conservation()[0]
+        assert np.allclose(per[k], alone, rtol=1e-12, atol=1e-12 * np.abs(alone).max()), k
