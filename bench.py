@@ -596,6 +596,22 @@ def our_arm(args, rank, world, local_rank):
     s.SetTiming(False)
     n_in = int(s.GetBuffer(F.FGRIDCNT).sum(dtype=np.int64))
 
+    # -- conservation drift over one segment (FP64 sums on the device)
+    s.RestoreCheckpoint(0)
+    c0 = s.Conservation()[0]
+    seg_steps = args.segment if args.segment > 0 else args.steps
+    s.RunSteps(seg_steps)
+    c1 = s.Conservation()[0]
+    e0, e1 = c0[5] + c0[6], c1[5] + c1[6]
+    conservation = {"steps": seg_steps, "points": [int(c0[0]), int(c1[0])],
+                    "mass_rel_drift": float(c1[1] / c0[1] - 1.0),
+                    "energy_start_J": float(e0), "energy_end_J": float(e1),
+                    "energy_rel_change": float((e1 - e0) / abs(e0)),
+                    "kinetic_end_J": float(c1[5]), "momentum_end": [float(v) for v in c1[2:5]],
+                    "centre_of_mass_shift": [float(a / c1[0] - b / c0[0]) for a, b in zip(c1[7:10], c0[7:10])],
+                    "note": "kinetic + gravitational potential energy; walls, viscosity and the limits "
+                            "dissipate it, the moving X- wall feeds it"}
+
     # -- e2e: host buffers through the C ABI ------------------------------------
     e2e_steps = args.e2e_steps or min(args.steps, 20)
     n = scene.n
@@ -666,6 +682,7 @@ def our_arm(args, rank, world, local_rank):
         "e2e": {"value": world * n * e2e_steps / e2e_s / 1e6, "unit": METRIC, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": e2e_steps},
         "autotuned_block_shapes": tuned,
+        "conservation": conservation,
         "batched": batched,
         "adjoint": adjoint,
         "fit": fit,
