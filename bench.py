@@ -662,6 +662,9 @@ def our_arm(args, rank, world, local_rank):
                 "algorithmic_bytes_per_launch": algo, "mean_launch_ms": dur_ms,
                 "bound_observed": rec.get("bound_observed"),
                 "issue_active_pct_ncu": rec.get("issue_active_pct"),
+                "issue_roofline_frac_ncu": rec.get("issue_roofline_frac"),
+                "issue_roofline_note": "warp instructions / (time x 152 SMs x 4 schedulers x SM clock), "
+                                       "from the committed ncu capture: the roof this kernel meets",
                 "profile": "profiles/ncu_wave_tank_4m.md"}
     step_bytes = sum(ALGO_BYTES[k] for k in ALGO_BYTES) * n_in + 12 * (p.gridTotal + 1)
     cpu = None
