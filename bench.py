@@ -381,7 +381,8 @@ def adjoint_measurements(args):
     and the initial velocities; with checkpoints every --adjoint-every steps
     and with every step kept (device memory of both tapes).
     wave_tank_4m: the bench workload after the warm-up, 10 recorded steps,
-    every = 1 and 5.
+    every = 1 and 5 (5 also with the segment replays keeping their pair
+    lists, FL_TAPE_KEEP_LISTS).
     forward = graph-replayed steps without a tape; taped = the recorded
     steps; backward = fl_backward with device buffers, per recorded step."""
     import fluids3_gb300 as F
@@ -460,9 +461,9 @@ def adjoint_measurements(args):
     ms_fwd = s.TimeSteps(T4, graph=True) / T4
     rows = []
     w = np.random.default_rng(1).standard_normal((scene.n, 3)).astype(np.float32)
-    for every in (1, 5):
+    for every, keep in ((1, False), (5, False), (5, True)):
         s.RestoreCheckpoint(0)
-        s.TapeBegin(T4, every)
+        s.TapeBegin(T4, every, keep)
         s.Sync()
         t0 = time.perf_counter()
         s.RunSteps(T4)
@@ -471,7 +472,7 @@ def adjoint_measurements(args):
         _time_backward(s, w)                       # first call: staging buffers
         ms_b, _, _ = _time_backward(s, w)
         s.TapeEnd()
-        rows.append({"every": every, "taped_forward_ms_per_step": (t1 - t0) * 1e3 / T4,
+        rows.append({"every": every, "keep_lists": keep, "taped_forward_ms_per_step": (t1 - t0) * 1e3 / T4,
                      "backward_ms_per_step": ms_b / T4, "ratio": ms_b / T4 / ms_fwd})
     s.close()
     out["wave_tank_4m"] = {"steps": T4, "forward_ms_per_step": ms_fwd, "runs": rows}

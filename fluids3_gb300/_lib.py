@@ -72,6 +72,7 @@ SIGNATURES = [
     ("fl_sample_volume", C.c_int, [vp, vp, C.POINTER(C.c_int), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                     C.c_float, C.c_int]),
     ("fl_tape_begin", C.c_int, [vp, C.c_int, C.c_int]),
+    ("fl_tape_begin_ex", C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
     ("fl_tape_steps", C.c_int, [vp]),
     ("fl_tape_order", C.c_int, [vp, vp]),
     ("fl_backward", C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp]),

@@ -851,13 +851,19 @@ static int run_step(fl_system *s, TimingState *t) {
 
 int fl_step_fused(fl_system *s) { return run_step(s, nullptr); }
 
-int fl_recompute_step(fl_system *s) {
+int fl_rebuild_grid(fl_system *s) {
     FL_TRY(clear_grid(s));
     FL_TRY(fl_launch_insert(s, nullptr));
     FL_TRY(fl_launch_scan(s, s->gcells, 0));
     FL_TRY(fl_launch_scatter_index(s));
     FL_TRY(fl_launch_sort_cells(s, 2));
     flip(s, F_POS); flip(s, F_VEL); flip(s, F_VEVAL); flip(s, F_CLR); flip(s, F_GCELL); flip(s, F_GNDX);
+    s->lists_valid = 0;
+    return FL_OK;
+}
+
+int fl_recompute_step(fl_system *s) {
+    FL_TRY(fl_rebuild_grid(s));
     FL_TRY(fl_launch_density(s));
     return FL_OK;
 }

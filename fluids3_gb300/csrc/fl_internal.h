@@ -194,6 +194,8 @@ int fl_step_fused(fl_system *s);
 // (gathering pos/vel/veval/clr, publishing both band-flag sets) and density
 // (with pair lists) into the live copies.
 int fl_recompute_step(fl_system *s);
+// The same without the density pass: insert, scan, sort (mode 2) only.
+int fl_rebuild_grid(fl_system *s);
 
 // ---- adjoint tape (fl_tape.cpp) --------------------------------------------
 int fl_tape_recording(const fl_system *s);

@@ -42,6 +42,13 @@ struct fl_tape {
     int *sbase, *sn;
     void *save[F_COUNT];    // the live state when fl_backward starts, restored at its end
     float *save_time;
+    // FL_TAPE_KEEP_LISTS (every > 1): per segment slot, the replayed step's
+    // pair lists, pair counts and densities, so its reverse step skips the
+    // density pass
+    int keep_lists;
+    size_t list_words;
+    uint32_t *seg_list, *seg_cnt;
+    float *seg_rho;
 };
 
 static void tape_release(fl_tape *t) {
@@ -56,6 +63,7 @@ static void tape_release(fl_tape *t) {
     cudaFree(t->partial); cudaFree(t->acc); cudaFree(t->sbase); cudaFree(t->sn);
     for (int k = 0; k < F_COUNT; k++) cudaFree(t->save[k]);
     cudaFree(t->save_time);
+    cudaFree(t->seg_list); cudaFree(t->seg_cnt); cudaFree(t->seg_rho);
     delete t;
 }
 
@@ -93,11 +101,17 @@ static int save_force(fl_system *s, float4 *dst) {
 }
 
 extern "C" int fl_tape_begin(fl_system *s, int max_steps, int every) {
+    return fl_tape_begin_ex(s, max_steps, every, 0);
+}
+
+extern "C" int fl_tape_begin_ex(fl_system *s, int max_steps, int every, int flags) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_tape_begin: null system");
+    if (flags & ~FL_TAPE_KEEP_LISTS) return fl_fail(FL_ERR_ARG, "fl_tape_begin_ex: unknown flags 0x%x", flags);
+    const int keep = (flags & FL_TAPE_KEEP_LISTS) && every > 1;
     if (max_steps < 1 || every < 1 || every > max_steps)
         return fl_fail(FL_ERR_ARG, "fl_tape_begin: max_steps %d, every %d (need 1 <= every <= max_steps)",
                        max_steps, every);
-    if (s->tape && s->tape->max_steps == max_steps && s->tape->every == every &&
+    if (s->tape && s->tape->max_steps == max_steps && s->tape->every == every && s->tape->keep_lists == keep &&
         s->tape->cap == (s->max_points > 0 ? s->max_points : 1)) {
         // same shape: start over in the storage already held
         fl_tape *t = s->tape;
@@ -149,7 +163,14 @@ extern "C" int fl_tape_begin(fl_system *s, int max_steps, int every) {
         if ((r = fl_dalloc((void **)&t->sn, 4 * (size_t)s->nscenes)) != FL_OK) break;
         for (int k = 0; k < F_COUNT && r == FL_OK; k++) r = fl_dalloc(&t->save[k], s->f[k].esz * cap);
         if (r != FL_OK) break;
-        r = fl_dalloc((void **)&t->save_time, 256);
+        if ((r = fl_dalloc((void **)&t->save_time, 256)) != FL_OK) break;
+        if (keep) {
+            t->keep_lists = 1;
+            t->list_words = ((cap + 31) / 32) * 32 * (size_t)s->D.hcap;
+            if ((r = fl_dalloc((void **)&t->seg_list, 4 * t->list_words * (size_t)every)) != FL_OK) break;
+            if ((r = fl_dalloc((void **)&t->seg_cnt, 4 * cap * (size_t)every)) != FL_OK) break;
+            r = fl_dalloc((void **)&t->seg_rho, 4 * cap * (size_t)every);
+        }
     } while (0);
     if (r != FL_OK) {
         tape_release(t);
@@ -236,16 +257,37 @@ static int download_vec3(fl_system *s, const float4 *src, float *dst) {
     return FL_OK;
 }
 
-// The reverse of recorded step k from its saved state and force.
-static int backward_step(fl_system *s, fl_tape *t, const float4 *state, const float4 *force, int k) {
+// The reverse of recorded step k from its saved state and force; with
+// `slot` >= 0 the step's pair lists, counts and densities come from that
+// segment slot instead of a density pass.
+static int backward_step(fl_system *s, fl_tape *t, const float4 *state, const float4 *force, int k,
+                         int slot = -1) {
     FL_TRY(load_state(s, t, state));
-    FL_TRY(fl_recompute_step(s));
+    uint32_t *own_list = s->hitlist, *own_cnt = s->hitcnt;
+    if (slot >= 0) {
+        FL_TRY(fl_rebuild_grid(s));
+        if (s->n)
+            FL_CUDA_TRY(cudaMemcpyAsync(s->f[F_PRESS].cur<void>(), t->seg_rho + (size_t)slot * t->cap,
+                                        4 * (size_t)s->n, cudaMemcpyDeviceToDevice, s->stream));
+        s->hitlist = t->seg_list + (size_t)slot * t->list_words;
+        s->hitcnt = t->seg_cnt + (size_t)slot * t->cap;
+        s->lists_valid = 1;
+    } else {
+        FL_TRY(fl_recompute_step(s));
+    }
     const int c = t->gcur, x = c ^ 1;
-    FL_TRY(fl_launch_adj_advance(s, t->time + k, force, t->g[c][0], t->g[c][1], t->g[c][2], t->xa, t->ea,
-                                 t->fb, t->g[x][1], t->rr));
-    FL_TRY(fl_launch_adj_force(s, t->rr, t->fb, t->xa, t->ea, t->rb, t->pc, t->g[x][2], t->revlist, t->revcnt));
-    FL_TRY(fl_launch_adj_density(s, t->revlist, t->revcnt, t->rb, t->xa, t->g[x][0]));
-    FL_TRY(fl_launch_param_reduce(s, t->pc, t->sbase, t->sn, t->nchunks, t->partial, t->acc));
+    const int r = [&]() {
+        FL_TRY(fl_launch_adj_advance(s, t->time + k, force, t->g[c][0], t->g[c][1], t->g[c][2], t->xa, t->ea,
+                                     t->fb, t->g[x][1], t->rr));
+        FL_TRY(fl_launch_adj_force(s, t->rr, t->fb, t->xa, t->ea, t->rb, t->pc, t->g[x][2], t->revlist,
+                                   t->revcnt));
+        FL_TRY(fl_launch_adj_density(s, t->revlist, t->revcnt, t->rb, t->xa, t->g[x][0]));
+        FL_TRY(fl_launch_param_reduce(s, t->pc, t->sbase, t->sn, t->nchunks, t->partial, t->acc));
+        return FL_OK;
+    }();
+    s->hitlist = own_list;
+    s->hitcnt = own_cnt;
+    if (r != FL_OK) return r;
     t->gcur = x;
     return FL_OK;
 }
@@ -268,11 +310,23 @@ static int run_reverse(fl_system *s, fl_tape *t) {
             FL_TRY(save_state(s, t, t->seg + (size_t)(k - t0) * blk));
             FL_CUDA_TRY(cudaMemcpyAsync(s->time_dev + s->time_slot, t->time + k, sizeof(float),
                                         cudaMemcpyDeviceToDevice, s->stream));
-            FL_TRY(fl_step_fused(s));
+            uint32_t *own_list = s->hitlist, *own_cnt = s->hitcnt;
+            if (t->keep_lists) {   // the step's density pass writes its lists into the slot
+                s->hitlist = t->seg_list + (size_t)(k - t0) * t->list_words;
+                s->hitcnt = t->seg_cnt + (size_t)(k - t0) * t->cap;
+            }
+            const int r = fl_step_fused(s);
+            s->hitlist = own_list;
+            s->hitcnt = own_cnt;
+            FL_TRY(r);
             FL_TRY(save_force(s, t->force + (size_t)(k - t0) * t->cap));
+            if (t->keep_lists && s->n)
+                FL_CUDA_TRY(cudaMemcpyAsync(t->seg_rho + (size_t)(k - t0) * t->cap, s->f[F_PRESS].cur<void>(),
+                                            4 * (size_t)s->n, cudaMemcpyDeviceToDevice, s->stream));
         }
         for (int k = t1 - 1; k >= t0; k--)
-            FL_TRY(backward_step(s, t, t->seg + (size_t)(k - t0) * blk, t->force + (size_t)(k - t0) * t->cap, k));
+            FL_TRY(backward_step(s, t, t->seg + (size_t)(k - t0) * blk, t->force + (size_t)(k - t0) * t->cap, k,
+                                 t->keep_lists ? k - t0 : -1));
     }
     return FL_OK;
 }

@@ -294,10 +294,11 @@ class FluidSystem:
         return int(bad.value)
 
     # -- adjoint (no counterpart in the reference) ----------------------------
-    def TapeBegin(self, max_steps: int, every: int = 1) -> None:
+    def TapeBegin(self, max_steps: int, every: int = 1, keep_lists: bool = False) -> None:
         """Record the Run steps that follow (up to ``max_steps``; a checkpoint of
-        the state every ``every`` steps) for Backward."""
-        call("fl_tape_begin", self._h, int(max_steps), int(every))
+        the state every ``every`` steps) for Backward. keep_lists: segment
+        replays keep their pair lists (more memory, faster reverse steps)."""
+        call("fl_tape_begin_ex", self._h, int(max_steps), int(every), 1 if keep_lists else 0)
 
     def TapeSteps(self) -> int:
         return int(lib().fl_tape_steps(self._h))

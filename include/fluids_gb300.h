@@ -357,6 +357,12 @@ int fl_get_phase_times(fl_system *s, double ms[8], int *steps);
  * fl_tape_order gives, per current slot, the point's index when recording
  * began (n uint32, host or device). fl_tape_steps: steps recorded. */
 int fl_tape_begin(fl_system *s, int max_steps, int every);
+/* fl_tape_begin with flags. FL_TAPE_KEEP_LISTS (every > 1): a segment
+ * replay keeps each replayed step's pair lists, pair counts and densities
+ * (~520 B per point per step of the segment: 512 B of pair list), so its
+ * reverse step skips the density pass -- memory for time. */
+#define FL_TAPE_KEEP_LISTS 1
+int fl_tape_begin_ex(fl_system *s, int max_steps, int every, int flags);
 int fl_tape_steps(const fl_system *s);
 int fl_tape_order(fl_system *s, uint32_t *order);
 int fl_backward(fl_system *s, const float *dpos, const float *dvel, const float *dveval,

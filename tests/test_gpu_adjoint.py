@@ -27,14 +27,14 @@ PARAM_TOL = 1e-3
 FL_ERR_ARG, FL_ERR_CAPACITY, FL_ERR_STATE = -1, -4, -6   # include/fluids_gb300.h
 
 
-def _gpu_record(sc, st, time, steps, every, params=None):
+def _gpu_record(sc, st, time, steps, every, params=None, keep_lists=False):
     """Run `steps` taped GPU steps from oracle state `st`; returns the system
     (still open) and the per-step (pos, vel, veval) read back before each step."""
     p = params or sc.params
     s = F.FluidSystem(p, st.n)
     s.SetParticles(st.pos, st.vel, st.veval, clr=st.clr)
     s.time = time
-    s.TapeBegin(steps, every)
+    s.TapeBegin(steps, every, keep_lists)
     states = []
     for _ in range(steps):
         states.append((s.GetBuffer(F.FPOS), s.GetBuffer(F.FVEL), s.GetBuffer(F.FVEVAL)))
@@ -143,13 +143,13 @@ def test_checkpoint_segments_and_repeat_are_bit_identical():
     st, t = stirred_state(sc, 15, seed=19)
     w = np.random.default_rng(20).standard_normal((3, st.n, 3)).astype(np.float32)
     results = []
-    for every in (1, 3, 7):
-        s, _ = _gpu_record(sc, st, t, 7, every)
+    for every, keep in ((1, False), (3, False), (7, False), (3, True), (7, True)):
+        s, _ = _gpu_record(sc, st, t, 7, every, keep_lists=keep)
         with s:
             a = s.Backward(*w)
             b = s.Backward(*w)
             for x, y in zip(a, b):
-                assert_bit_equal(x, y, f"repeat, every={every}")
+                assert_bit_equal(x, y, f"repeat, every={every}, keep_lists={keep}")
             results.append(a)
     for r in results[1:]:
         for x, y in zip(results[0], r):
