@@ -381,8 +381,8 @@ def adjoint_measurements(args):
     and the initial velocities; with checkpoints every --adjoint-every steps
     and with every step kept (device memory of both tapes).
     wave_tank_4m: the bench workload after the warm-up, 10 recorded steps,
-    every = 1 and 5 (5 also with the segment replays keeping their pair
-    lists, FL_TAPE_KEEP_LISTS).
+    every = 1 and 5, each also with the recorded / replayed steps keeping
+    their pair lists (FL_TAPE_KEEP_LISTS).
     forward = graph-replayed steps without a tape; taped = the recorded
     steps; backward = fl_backward with device buffers, per recorded step."""
     import fluids3_gb300 as F
@@ -461,7 +461,7 @@ def adjoint_measurements(args):
     ms_fwd = s.TimeSteps(T4, graph=True) / T4
     rows = []
     w = np.random.default_rng(1).standard_normal((scene.n, 3)).astype(np.float32)
-    for every, keep in ((1, False), (5, False), (5, True)):
+    for every, keep in ((1, False), (1, True), (5, False), (5, True)):
         s.RestoreCheckpoint(0)
         s.TapeBegin(T4, every, keep)
         s.Sync()

@@ -49,6 +49,7 @@ struct fl_tape {
     size_t list_words;
     uint32_t *seg_list, *seg_cnt;
     float *seg_rho;
+    uint32_t *own_list, *own_cnt;   // the system's own lists while a recorded step writes into a slot
 };
 
 static void tape_release(fl_tape *t) {
@@ -70,6 +71,10 @@ static void tape_release(fl_tape *t) {
 void fl_tape_free(fl_system *s) {
     if (!s || !s->tape) return;
     cudaStreamSynchronize(s->stream);
+    if (s->tape->own_list) {   // a recorded step stopped while writing into a slot
+        s->hitlist = s->tape->own_list;
+        s->hitcnt = s->tape->own_cnt;
+    }
     tape_release(s->tape);
     s->tape = nullptr;
 }
@@ -107,7 +112,7 @@ extern "C" int fl_tape_begin(fl_system *s, int max_steps, int every) {
 extern "C" int fl_tape_begin_ex(fl_system *s, int max_steps, int every, int flags) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_tape_begin: null system");
     if (flags & ~FL_TAPE_KEEP_LISTS) return fl_fail(FL_ERR_ARG, "fl_tape_begin_ex: unknown flags 0x%x", flags);
-    const int keep = (flags & FL_TAPE_KEEP_LISTS) && every > 1;
+    const int keep = (flags & FL_TAPE_KEEP_LISTS) ? 1 : 0;
     if (max_steps < 1 || every < 1 || every > max_steps)
         return fl_fail(FL_ERR_ARG, "fl_tape_begin: max_steps %d, every %d (need 1 <= every <= max_steps)",
                        max_steps, every);
@@ -164,12 +169,13 @@ extern "C" int fl_tape_begin_ex(fl_system *s, int max_steps, int every, int flag
         for (int k = 0; k < F_COUNT && r == FL_OK; k++) r = fl_dalloc(&t->save[k], s->f[k].esz * cap);
         if (r != FL_OK) break;
         if ((r = fl_dalloc((void **)&t->save_time, 256)) != FL_OK) break;
-        if (keep) {
+        if (keep) {   // slots: every step of a segment (every > 1) or of the whole tape (every = 1)
             t->keep_lists = 1;
+            const size_t slots = (size_t)(every > 1 ? every : max_steps);
             t->list_words = ((cap + 31) / 32) * 32 * (size_t)s->D.hcap;
-            if ((r = fl_dalloc((void **)&t->seg_list, 4 * t->list_words * (size_t)every)) != FL_OK) break;
-            if ((r = fl_dalloc((void **)&t->seg_cnt, 4 * cap * (size_t)every)) != FL_OK) break;
-            r = fl_dalloc((void **)&t->seg_rho, 4 * cap * (size_t)every);
+            if ((r = fl_dalloc((void **)&t->seg_list, 4 * t->list_words * slots)) != FL_OK) break;
+            if ((r = fl_dalloc((void **)&t->seg_cnt, 4 * cap * slots)) != FL_OK) break;
+            r = fl_dalloc((void **)&t->seg_rho, 4 * cap * slots);
         }
     } while (0);
     if (r != FL_OK) {
@@ -202,11 +208,25 @@ int fl_tape_pre_step(fl_system *s) {
     if (k % t->every == 0) FL_TRY(save_state(s, t, t->ck + (size_t)(k / t->every) * 3 * t->cap));
     FL_CUDA_TRY(cudaMemcpyAsync(t->time + k, s->time_dev + s->time_slot, sizeof(float),
                                 cudaMemcpyDeviceToDevice, s->stream));
+    if (t->keep_lists && t->every == 1) {   // this step's density pass writes into slot k
+        t->own_list = s->hitlist;
+        t->own_cnt = s->hitcnt;
+        s->hitlist = t->seg_list + (size_t)k * t->list_words;
+        s->hitcnt = t->seg_cnt + (size_t)k * t->cap;
+    }
     return FL_OK;
 }
 
 int fl_tape_post_step(fl_system *s) {
     fl_tape *t = s->tape;
+    if (t->own_list) {
+        s->hitlist = t->own_list;
+        s->hitcnt = t->own_cnt;
+        t->own_list = t->own_cnt = nullptr;
+        if (!t->broken && s->n)
+            FL_CUDA_TRY(cudaMemcpyAsync(t->seg_rho + (size_t)t->steps * t->cap, s->f[F_PRESS].cur<void>(),
+                                        4 * (size_t)s->n, cudaMemcpyDeviceToDevice, s->stream));
+    }
     if (t->broken) return FL_OK;
     // every = 1: keep the step's force (sorted order) so the reverse pass
     // need not recompute it
@@ -300,7 +320,7 @@ static int run_reverse(fl_system *s, fl_tape *t) {
         const int t1 = (t0 + t->every < t->steps) ? t0 + t->every : t->steps;
         const float4 *ck = t->ck + (size_t)g * blk;
         if (t->every == 1) {
-            FL_TRY(backward_step(s, t, ck, t->force + (size_t)t0 * t->cap, t0));
+            FL_TRY(backward_step(s, t, ck, t->force + (size_t)t0 * t->cap, t0, t->keep_lists ? t0 : -1));
             continue;
         }
         // replay the segment's fused steps from its checkpoint, saving the

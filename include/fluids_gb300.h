@@ -357,10 +357,11 @@ int fl_get_phase_times(fl_system *s, double ms[8], int *steps);
  * fl_tape_order gives, per current slot, the point's index when recording
  * began (n uint32, host or device). fl_tape_steps: steps recorded. */
 int fl_tape_begin(fl_system *s, int max_steps, int every);
-/* fl_tape_begin with flags. FL_TAPE_KEEP_LISTS (every > 1): a segment
- * replay keeps each replayed step's pair lists, pair counts and densities
- * (~520 B per point per step of the segment: 512 B of pair list), so its
- * reverse step skips the density pass -- memory for time. */
+/* fl_tape_begin with flags. FL_TAPE_KEEP_LISTS: each step's pair lists,
+ * pair counts and densities are kept (~520 B per point per step: 512 B of
+ * pair list) -- for every step of the tape when every = 1, for the steps of
+ * the segment being replayed when every > 1 -- so its reverse step skips
+ * the density pass: memory for time, same gradients. */
 #define FL_TAPE_KEEP_LISTS 1
 int fl_tape_begin_ex(fl_system *s, int max_steps, int every, int flags);
 int fl_tape_steps(const fl_system *s);

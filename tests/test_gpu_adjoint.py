@@ -143,7 +143,7 @@ def test_checkpoint_segments_and_repeat_are_bit_identical():
     st, t = stirred_state(sc, 15, seed=19)
     w = np.random.default_rng(20).standard_normal((3, st.n, 3)).astype(np.float32)
     results = []
-    for every, keep in ((1, False), (3, False), (7, False), (3, True), (7, True)):
+    for every, keep in ((1, False), (3, False), (7, False), (1, True), (3, True), (7, True)):
         s, _ = _gpu_record(sc, st, t, 7, every, keep_lists=keep)
         with s:
             a = s.Backward(*w)
