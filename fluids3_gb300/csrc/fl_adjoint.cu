@@ -401,7 +401,8 @@ __device__ __forceinline__ bool rev_next(RevIter &it, const DevParams &P, const 
     return true;
 }
 
-// Reverse of computeForce for point s (all 32 lanes of a warp call it).
+// Reverse of computeForce for point s (all threads of the block call it,
+// with grouping_smem(blockDim, kBandKeys) bytes of dynamic shared memory).
 // First each lane walks its reverse block (the points whose search block
 // holds s, outside s's own cell) and records the reverse pairs it finds in
 // revlist; then the warp evaluates, in step, every lane's own pairs (the
@@ -422,7 +423,10 @@ k_adj_force(const __grid_constant__ DevParams P0, const SceneTab T, int n,
             const float4 *__restrict__ fb, float4 *__restrict__ xa, const float4 *__restrict__ ea,
             float *__restrict__ rb, float4 *__restrict__ pc, float4 *__restrict__ e_out,
             uint32_t *__restrict__ revlist, uint32_t *__restrict__ revcnt) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    // pruned: the lanes of a warp take points with the same upper-band bits,
+    // which decide the cells of the reverse block a point visits
+    extern __shared__ uint32_t s_dyn[];
+    const int s = PRUNE ? band_grouped_slot(n, pos, gcell, 0, s_dyn) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const DevParams &P = scene_params(P0, T, s < n ? s : 0);
     const uint32_t gc = (s < n) ? gcell[s] : kUndef;
     const bool active = gc != kUndef;
@@ -709,7 +713,7 @@ int fl_launch_adj_force(fl_system *s, const float2 *rr, const float4 *fb, float4
         return fl_fail(FL_ERR_CAPACITY, "adjoint: %d points (at most %u)", s->max_points, kSlotMask);
     const bool pr = adj_prune(s);
     auto kern = pr ? k_adj_force<true> : k_adj_force<false>;
-    kern<<<blocks_for(s->n, kAdjThreads), kAdjThreads, 0, s->stream>>>(
+    kern<<<blocks_for(s->n, kAdjThreads), kAdjThreads, grouping_smem(kAdjThreads, kBandKeys), s->stream>>>(
         s->D, fl_scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->f[F_VEVAL].cur<float4>(),
         rr, s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt, s->upbits, s->hitlist,
         s->hitcnt, s->src, fb, xa, ea, rb, pc, e_out, revlist, revcnt);

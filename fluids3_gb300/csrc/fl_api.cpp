@@ -1022,7 +1022,7 @@ extern "C" int fl_autotune(fl_system *s, int steps, int *chosen) {
     const int slot = FL_MAX_CHECKPOINTS;   // the tuner's own checkpoint slot
     FL_TRY(save_slot(s, slot));
     int *knob[3] = {&s->blk_density, &s->blk_force, &s->blk_sort};
-    const int cand[3][3] = {{64, 128, 256}, {32, 64, 128}, {64, 128, 256}};
+    const int cand[3][4] = {{128, 256, 512, 1024}, {32, 64, 128, 0}, {64, 128, 256, 0}};
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     FL_CUDA_TRY(cudaEventCreate(&e0));
     cudaError_t ce = cudaEventCreate(&e1);
@@ -1031,7 +1031,7 @@ extern "C" int fl_autotune(fl_system *s, int steps, int *chosen) {
     for (int k = 0; k < 3 && r == FL_OK; k++) {
         int best = 0;
         float best_ms = 0.0f;
-        for (int c = 0; c < 3 && r == FL_OK; c++) {
+        for (int c = 0; c < 4 && cand[k][c] && r == FL_OK; c++) {
             *knob[k] = cand[k][c];
             destroy_graph(s);
             if ((r = restore_slot(s, slot)) != FL_OK) break;

@@ -149,6 +149,80 @@ __device__ __forceinline__ bool cand_next(CandIter &it, const DevParams &P,
     return true;
 }
 
+// ---------------------------------------------------------------------------
+// Block-local thread orders. Each point's result is one thread's work in the
+// reference's order, so which thread of a block takes which of the block's
+// points changes no result; grouping points whose loops have the same shape
+// into the same warps shortens the loops that run as long as their slowest
+// lane. group_by_key() returns the slot this thread takes: the block's slots
+// ordered by their threads' keys (< NKEYS), ascending slot within a key. All
+// threads of the block call it; s_dyn holds grouping_smem(blockDim, NKEYS)
+// bytes of scratch, which the caller may reuse once it has returned.
+__host__ __device__ inline size_t grouping_smem(int threads, uint32_t nkeys) {
+    return (size_t)nkeys * (threads / 32) * sizeof(uint32_t) + (size_t)threads * sizeof(uint16_t);
+}
+
+template <uint32_t NKEYS>
+__device__ __forceinline__ int group_by_key(uint32_t key, uint32_t *s_dyn) {
+    const unsigned lane = threadIdx.x & 31u, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t *s_cnt = s_dyn;                                               // (key, warp), key-major
+    uint16_t *s_slot = reinterpret_cast<uint16_t *>(s_dyn + NKEYS * nw);
+    const unsigned below = (1u << lane) - 1u;
+    uint32_t rank = 0;
+    __syncthreads();   // earlier users of the scratch are done
+    if constexpr (NKEYS <= 16) {
+#pragma unroll
+        for (uint32_t k = 0; k < NKEYS; k++) {
+            const unsigned b = __ballot_sync(0xffffffffu, key == k);
+            if (lane == 0) s_cnt[k * nw + w] = __popc(b);
+            if (key == k) rank = __popc(b & below);
+        }
+    } else {
+        for (uint32_t e = threadIdx.x; e < NKEYS * nw; e += blockDim.x) s_cnt[e] = 0;
+        __syncthreads();
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        rank = __popc(peers & below);
+        if (rank == 0) s_cnt[key * nw + w] = __popc(peers);
+    }
+    __syncthreads();
+    if (w == 0) {   // exclusive scan of the (key, warp) counts
+        const uint32_t total = NKEYS * nw;
+        uint32_t run = 0;
+        for (uint32_t c0 = 0; c0 < total; c0 += 32) {
+            const uint32_t e = c0 + lane;
+            const uint32_t v = (e < total) ? s_cnt[e] : 0u;
+            uint32_t x = v;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+                if (lane >= (unsigned)d) x += y;
+            }
+            if (e < total) s_cnt[e] = run + x - v;
+            run += __shfl_sync(0xffffffffu, x, 31);
+        }
+    }
+    __syncthreads();
+    s_slot[s_cnt[key * nw + w] + rank] = (uint16_t)threadIdx.x;
+    __syncthreads();
+    return (int)(blockIdx.x * blockDim.x) + s_slot[threadIdx.x];
+}
+
+// Points of one cell with the same band bits visit the same candidates of
+// the pruned walks (lower-band bits, shift 3: the entries of the search
+// block; upper-band bits, shift 0: the cells of the reverse block), so the
+// walks group a block's points by those bits, then cells out of range, then
+// slots past n. Needs grouping_smem(blockDim, kBandKeys) bytes of s_dyn.
+constexpr uint32_t kBandKeys = 10;
+
+__device__ __forceinline__ int band_grouped_slot(int n, const float4 *__restrict__ pos,
+                                                 const uint32_t *__restrict__ gcell, int shift,
+                                                 uint32_t *s_dyn) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t key = kBandKeys - 1;
+    if (i < n) key = (gcell[i] == kUndef) ? kBandKeys - 2 : ((__float_as_uint(pos[i].w) >> shift) & 7u);
+    return group_by_key<kBandKeys>(key, s_dyn);
+}
+
 // Pair list written by the density pass: for point i (global thread i,
 // warp w = i / 32, lane l = i % 32) entry t lives at
 // ((w * hcap + t) * 32 + l), so a warp reading entry t of all its lanes

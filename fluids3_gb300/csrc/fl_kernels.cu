@@ -322,67 +322,22 @@ k_gather_all(int n, const uint32_t *__restrict__ src,
     gndx_o[s] = gndx[i];
 }
 
-// Thread order of the pruned walk. A point's lower-band bits (code bits
-// 3-5) decide which entries of its search block it visits, and points of
-// one cell with the same bits visit the same candidates, so the threads of
-// a block take the block's points grouped by those bits (then cells out of
-// range, then slots past n), ascending slot within a group. The lanes of a
-// warp then walk the same entries instead of each entry running as long as
-// the slowest lane's. Each thread still computes one point's sum, so the
-// results do not depend on the order. Returns the slot this thread takes;
-// all threads of the block must call it.
-constexpr uint32_t kClassKeys = 10;
-
-__device__ __forceinline__ int class_grouped_slot(int n, const float4 *__restrict__ pos,
-                                                  const uint32_t *__restrict__ gcell) {
-    __shared__ uint32_t s_cnt[kClassKeys * (kThreads / 32)];
-    __shared__ uint8_t s_slot[kThreads];
-    const unsigned lane = lane_id(), w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int base = blockIdx.x * blockDim.x;
-    const int i = base + threadIdx.x;
-    uint32_t key = kClassKeys - 1;
-    if (i < n) key = (gcell[i] == kUndef) ? kClassKeys - 2 : ((__float_as_uint(pos[i].w) >> 3) & 7u);
-    uint32_t rank = 0;
-#pragma unroll
-    for (uint32_t k = 0; k < kClassKeys; k++) {
-        const unsigned b = __ballot_sync(0xffffffffu, key == k);
-        if (lane == 0) s_cnt[k * nw + w] = __popc(b);
-        if (key == k) rank = __popc(b & ((1u << lane) - 1u));
-    }
-    __syncthreads();
-    if (w == 0) {   // exclusive scan of the (key, warp) counts, key-major
-        const uint32_t total = kClassKeys * nw;
-        uint32_t run = 0;
-        for (uint32_t c0 = 0; c0 < total; c0 += 32) {
-            const uint32_t e = c0 + lane;
-            const uint32_t v = (e < total) ? s_cnt[e] : 0u;
-            uint32_t x = v;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
-                if (lane >= (unsigned)d) x += y;
-            }
-            if (e < total) s_cnt[e] = run + x - v;
-            run += __shfl_sync(0xffffffffu, x, 31);
-        }
-    }
-    __syncthreads();
-    s_slot[s_cnt[key * nw + w] + rank] = (uint8_t)threadIdx.x;
-    __syncthreads();
-    return base + s_slot[threadIdx.x];
-}
+constexpr int kDensityMaxThreads = 1024;
 
 // computePressure (fluids4.0/fluid_kernels.cu:112-149). FGRID is the
 // identity after a full sort (cu:83), so neighbour slots are read directly.
 // With LIST the slots of the pairs that pass 0 < d^2 < rd2 are recorded, in
 // visiting order, for the force pass (same positions, same test).
 template <bool PRUNE, bool LIST, bool BATCH>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kDensityMaxThreads, 2)
 k_density(const __grid_constant__ DevParams P0, const SceneTab T, int n, const float4 *__restrict__ pos,
           const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ off,
           const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
           float *__restrict__ press, uint32_t *__restrict__ hitlist, uint32_t *__restrict__ hitcnt) {
-    const int i = PRUNE ? class_grouped_slot(n, pos, gcell) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    // pruned: the lanes of a warp take points with the same lower-band bits,
+    // which decide the entries of the search block a point visits
+    extern __shared__ uint32_t s_dyn[];
+    const int i = PRUNE ? band_grouped_slot(n, pos, gcell, 3, s_dyn) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (i >= n) return;
     const DevParams &P = BATCH ? T.params[T.point_scene[i]] : P0;
     const uint32_t gc = gcell[i];
@@ -952,7 +907,7 @@ int fl_launch_density(fl_system *s) {
     if (s->n == 0) return FL_OK;
     auto kern = s->batched ? density_kernel<true>(use_prune(s)) : density_kernel<false>(use_prune(s));
     const int bs = s->blk_density ? s->blk_density : kThreads;
-    kern<<<blocks_for(s->n, bs), bs, 0, s->stream>>>(
+    kern<<<blocks_for(s->n, bs), bs, grouping_smem(bs, kBandKeys), s->stream>>>(
         s->D, fl_scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt,
         s->upbits, s->f[F_PRESS].cur<float>(), s->hitlist, s->hitcnt);
     FL_LAUNCH_CHECK("density");

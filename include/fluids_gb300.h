@@ -294,11 +294,12 @@ int fl_checkpoint_restore(fl_system *s, int slot);
 #define FL_CONSERVATION_VALUES 10
 int fl_conservation(fl_system *s, double *out);
 
-/* Block-shape autotuner (no counterpart in the reference): times each of
- * the density, force and sort passes at three block sizes over `steps`
- * steps from the current state (restored afterwards) and keeps the fastest;
- * chosen (nullable) gets the threads per block of density, force, sort.
- * Results are identical for every block size. Invalidates an open tape. */
+/* Block-shape autotuner (no counterpart in the reference): times the
+ * density pass at 128..1024 threads per block and the force and sort passes
+ * at three block sizes each, over `steps` steps from the current state
+ * (restored afterwards), and keeps the fastest; chosen (nullable) gets the
+ * threads per block of density, force, sort. Results are identical for
+ * every block size. FL_ERR_STATE while a tape is recording. */
 int fl_autotune(fl_system *s, int steps, int *chosen);
 
 /* Wait for the system stream; returns FL_ERR_DEVICE if a kernel raised the
