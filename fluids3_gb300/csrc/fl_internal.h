@@ -224,8 +224,9 @@ int fl_launch_insert(fl_system *s, uint32_t *gcell_pre_or_null);
 int fl_launch_scan(fl_system *s, int count, int clear_status);
 int fl_launch_scatter_index(fl_system *s);
 // mode 0: rank only (sorted src + canonical gndx into f[F_GNDX].cur, pre-sort order)
-// mode 1: fused rank + gather of pos/vel/veval/clr/gcell/gndx into the nxt copies
-// mode 2: mode 1 that also publishes the lower-band slot flags (upbits rows 3-5)
+// mode 1: sorted src, then a gather of pos/vel/veval/clr/gcell/gndx into the
+//         nxt copies with band codes and the upper-band slot flags (rows 0-2)
+// mode 2: mode 1 that also writes the lower-band slot flags (upbits rows 3-5)
 int fl_launch_sort_cells(fl_system *s, int mode);
 // gather every field cur -> nxt through src (phase-API counting sort)
 int fl_launch_gather_all(fl_system *s);

@@ -102,70 +102,18 @@ __device__ __forceinline__ void warp_bitonic(uint32_t (&v)[K]) {
     }
 }
 
+// Mode 0 (phase API) also records each point's rank within its cell by
+// pre-sort index (gndx_pre); mode 1 (fused step) only orders src, and
+// k_gather_sorted then moves the points.
 struct SortArgs {
     const uint32_t *off, *cnt;
     uint32_t *src, *scratch;
     uint32_t *gndx_pre;                // mode 0: canonical gndx by pre-sort index
-    // mode 1 gather
-    const float4 *pos_in, *vel_in, *veval_in;
-    const uint32_t *clr_in;
-    float4 *pos_out, *vel_out, *veval_out;
-    uint32_t *clr_out, *gcell_out, *gndx_out;
-    uint32_t *upbits;                  // mode 1 with pruning: per-slot upper-band flags
     int gcells;                        // internal cell entries (all scenes, bins included)
-    int prune;
-    SceneTab T;
-    DevParams P;                       // single-scene parameters
 };
-
-// The cell a sorting warp owns: its scene's parameters, its entry index
-// (global), its index within the scene's grid, and whether it is the
-// scene's out-of-range bin.
-struct CellCtx {
-    const DevParams *P;
-    int c, local;
-    bool overflow;
-};
-
-// Writes slot o+k of cell c from pre-sort point i; returns the band code
-// (mode 1 with pruning) so the caller can build the cell's masks.
-template <int MODE>
-__device__ __forceinline__ uint32_t emit_slot(const SortArgs &a, const CellCtx &cx, uint32_t o, uint32_t k,
-                                              uint32_t i) {
-    if (MODE == 0) {
-        a.gndx_pre[i] = k;
-        return 0u;
-    } else {
-        const uint32_t s = o + k;
-        float4 p = a.pos_in[i];
-        const uint32_t code = a.prune ? band_code(*cx.P, cx.local, p) : 0u;
-        p.w = __uint_as_float(code);
-        a.pos_out[s] = p;
-        a.vel_out[s] = a.vel_in[i];
-        a.veval_out[s] = a.veval_in[i];
-        a.clr_out[s] = a.clr_in[i];
-        a.gcell_out[s] = cx.overflow ? kUndef : (uint32_t)cx.c;
-        a.gndx_out[s] = k;
-        return code;
-    }
-}
-
-// Emit slots o .. o+m-1 of cell c from the sorted src (all lanes call).
-template <int MODE>
-__device__ __forceinline__ void emit_range(const SortArgs &a, const CellCtx &cx, uint32_t o, uint32_t m) {
-    const unsigned lane = lane_id();
-    for (uint32_t kb = 0; kb < m; kb += 32) {
-        const uint32_t k = kb + lane;
-        const bool valid = k < m;
-        uint32_t code = 0;
-        if (valid) code = emit_slot<MODE>(a, cx, o, k, a.src[o + k]);
-        if (MODE >= 1 && a.prune) publish_upbits(*cx.P, a.upbits, o + kb, code, valid);
-        if (MODE == 2 && a.prune) publish_upbits(*cx.P, a.upbits + 3 * (size_t)cx.P->upwords, o + kb, code >> 3, valid);
-    }
-}
 
 template <int MODE, int K>
-__device__ __forceinline__ void sort_segment(const SortArgs &a, const CellCtx &cx, uint32_t o, uint32_t m) {
+__device__ __forceinline__ void sort_segment(const SortArgs &a, uint32_t o, uint32_t m) {
     const unsigned lane = lane_id();
     uint32_t v[K];
 #pragma unroll
@@ -174,22 +122,13 @@ __device__ __forceinline__ void sort_segment(const SortArgs &a, const CellCtx &c
         v[r] = (e < m) ? a.src[o + e] : 0xffffffffu;
     }
     warp_bitonic<K>(v);
-    if constexpr (K == 1) {
-        uint32_t code = 0;
-        if (lane < m) {
-            a.src[o + lane] = v[0];   // canonical src in both modes (the adjoint reads it)
-            code = emit_slot<MODE>(a, cx, o, lane, v[0]);
-        }
-        if (MODE >= 1 && a.prune) publish_upbits(*cx.P, a.upbits, o, code, lane < m);
-        if (MODE == 2 && a.prune) publish_upbits(*cx.P, a.upbits + 3 * (size_t)cx.P->upwords, o, code >> 3, lane < m);
-    } else {
 #pragma unroll
-        for (int r = 0; r < K; r++) {
-            const uint32_t e = lane * K + r;
-            if (e < m) a.src[o + e] = v[r];
+    for (int r = 0; r < K; r++) {
+        const uint32_t e = lane * K + r;
+        if (e < m) {
+            a.src[o + e] = v[r];
+            if (MODE == 0) a.gndx_pre[v[r]] = e;
         }
-        __syncwarp();
-        emit_range<MODE>(a, cx, o, m);
     }
 }
 
@@ -207,7 +146,7 @@ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t *a, uint32_t 
 }
 
 template <int MODE>
-__device__ void sort_segment_dense(const SortArgs &a, const CellCtx &cx, uint32_t o, uint32_t m) {
+__device__ void sort_segment_dense(const SortArgs &a, uint32_t o, uint32_t m) {
     const unsigned lane = lane_id();
     constexpr uint32_t kChunk = 128;
     for (uint32_t cb = 0; cb < m; cb += kChunk) {
@@ -238,10 +177,35 @@ __device__ void sort_segment_dense(const SortArgs &a, const CellCtx &cx, uint32_
         a.scratch[o + rank] = key;
     }
     __syncwarp();
-    for (uint32_t k = lane; k < m; k += 32) a.src[o + k] = a.scratch[o + k];
-    __syncwarp();
-    emit_range<MODE>(a, cx, o, m);
+    for (uint32_t k = lane; k < m; k += 32) {
+        const uint32_t key = a.scratch[o + k];
+        a.src[o + k] = key;
+        if (MODE == 0) a.gndx_pre[key] = k;
+    }
 }
+
+template <int MODE>
+__global__ void __launch_bounds__(kThreads)
+k_sort_cells(const __grid_constant__ SortArgs a) {
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (c >= a.gcells) return;
+    const uint32_t m = a.cnt[c];
+    if (m == 0) return;
+    const uint32_t o = a.off[c];
+    if (m <= 32) sort_segment<MODE, 1>(a, o, m);
+    else if (m <= 64) sort_segment<MODE, 2>(a, o, m);
+    else if (m <= 128) sort_segment<MODE, 4>(a, o, m);
+    else sort_segment_dense<MODE>(a, o, m);
+}
+
+// The cell a warp owns: its scene's parameters, its entry index (global),
+// its index within the scene's grid, and whether it is the scene's
+// out-of-range bin.
+struct CellCtx {
+    const DevParams *P;
+    int c, local;
+    bool overflow;
+};
 
 template <bool BATCH>
 __device__ __forceinline__ CellCtx cell_ctx(const DevParams &P0, const SceneTab &T, int c) {
@@ -253,19 +217,52 @@ __device__ __forceinline__ CellCtx cell_ctx(const DevParams &P0, const SceneTab 
     return cx;
 }
 
-template <int MODE, bool BATCH>
+// The move of the fused sort, one thread per sorted slot s: the point
+// src[s] (canonical order, set by k_sort_cells in mode 1) goes to slot s
+// with its band code in pos.w, its cell in gcell and its rank within the
+// cell in gndx (countingSortFull, fluids4.0/fluid_kernels.cu:56-87, with
+// the canonical within-cell order). The 32 slots of a warp are one word of
+// each slot-flag row, so the warp stores the words whole: rows 0-2 the
+// upper-band flags (ROWS >= 1), rows 3-5 the lower-band flags (ROWS == 2).
+template <bool BATCH, int ROWS>
 __global__ void __launch_bounds__(kThreads)
-k_sort_cells(const __grid_constant__ SortArgs a) {
-    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (c >= a.gcells) return;
-    const uint32_t m = a.cnt[c];
-    if (m == 0) return;
-    const uint32_t o = a.off[c];
-    const CellCtx cx = cell_ctx<BATCH>(a.P, a.T, c);
-    if (m <= 32) sort_segment<MODE, 1>(a, cx, o, m);
-    else if (m <= 64) sort_segment<MODE, 2>(a, cx, o, m);
-    else if (m <= 128) sort_segment<MODE, 4>(a, cx, o, m);
-    else sort_segment_dense<MODE>(a, cx, o, m);
+k_gather_sorted(const __grid_constant__ DevParams P0, const SceneTab T, int n, const uint32_t *__restrict__ src,
+                const uint32_t *__restrict__ cell_pre, const uint32_t *__restrict__ off,
+                const float4 *__restrict__ pos_in, const float4 *__restrict__ vel_in,
+                const float4 *__restrict__ veval_in, const uint32_t *__restrict__ clr_in,
+                float4 *__restrict__ pos_out, float4 *__restrict__ vel_out, float4 *__restrict__ veval_out,
+                uint32_t *__restrict__ clr_out, uint32_t *__restrict__ gcell_out,
+                uint32_t *__restrict__ gndx_out, uint32_t *__restrict__ upbits) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (blockIdx.x * blockDim.x + (threadIdx.x & ~31u) >= (unsigned)n) return;   // whole warp past n
+    const bool valid = s < n;
+    uint32_t code = 0, upwords = 0;
+    if (valid) {
+        const uint32_t i = src[s];
+        const uint32_t c = cell_pre[i];
+        const DevParams &P = BATCH ? T.params[T.cell_scene[c]] : P0;
+        const int local = (int)c - P.cell_base;
+        float4 p = pos_in[i];
+        if (ROWS >= 1) code = band_code(P, local, p);
+        p.w = __uint_as_float(code);
+        pos_out[s] = p;
+        vel_out[s] = vel_in[i];
+        veval_out[s] = veval_in[i];
+        clr_out[s] = clr_in[i];
+        gcell_out[s] = (local == P.ncells) ? kUndef : c;
+        gndx_out[s] = (uint32_t)s - off[c];
+        upwords = (uint32_t)P.upwords;
+    }
+    if constexpr (ROWS >= 1) {
+        const size_t word = (size_t)(s >> 5);
+        const unsigned lane = lane_id();
+        upwords = __shfl_sync(0xffffffffu, upwords, 0);   // lane 0 holds a point (s0 < n)
+#pragma unroll
+        for (int row = 0; row < 3 * ROWS; row++) {
+            const unsigned b = __ballot_sync(0xffffffffu, valid && ((code >> row) & 1u));
+            if (lane == 0) upbits[(size_t)row * upwords + word] = b;
+        }
+    }
 }
 
 // Band codes and upper-band slot flags for an already sorted grid
@@ -837,31 +834,30 @@ int fl_launch_sort_cells(fl_system *s, int mode) {
     SortArgs a = {};
     a.off = s->off; a.cnt = s->cnt; a.src = s->src; a.scratch = s->rank_tmp;
     a.gcells = s->gcells;
-    a.P = s->D;
-    a.T = fl_scene_tab(s);
-    a.prune = (mode >= 1) ? s->D.prune : 0;
-    a.upbits = s->upbits;
     const int bs = s->blk_sort ? s->blk_sort : kThreads;
     const int grid = blocks_for((long long)s->gcells, bs / 32);
     if (mode == 0) {
         a.gndx_pre = s->f[F_GNDX].cur<uint32_t>();
-        auto kern = s->batched ? k_sort_cells<0, true> : k_sort_cells<0, false>;
-        kern<<<grid, bs, 0, s->stream>>>(a);
-    } else {
-        a.pos_in = s->f[F_POS].cur<float4>(); a.pos_out = s->f[F_POS].nxt<float4>();
-        a.vel_in = s->f[F_VEL].cur<float4>(); a.vel_out = s->f[F_VEL].nxt<float4>();
-        a.veval_in = s->f[F_VEVAL].cur<float4>(); a.veval_out = s->f[F_VEVAL].nxt<float4>();
-        a.clr_in = s->f[F_CLR].cur<uint32_t>(); a.clr_out = s->f[F_CLR].nxt<uint32_t>();
-        a.gcell_out = s->f[F_GCELL].nxt<uint32_t>();
-        a.gndx_out = s->f[F_GNDX].nxt<uint32_t>();
-        if (a.prune)
-            FL_CUDA_TRY(cudaMemsetAsync(s->upbits, 0, (mode == 2 ? 2 : 1) * fl_upbits_bytes(s), s->stream));
-        auto kern = (mode == 2) ? (s->batched ? k_sort_cells<2, true> : k_sort_cells<2, false>)
-                                : (s->batched ? k_sort_cells<1, true> : k_sort_cells<1, false>);
-        kern<<<grid, bs, 0, s->stream>>>(a);
-        s->codes_valid = s->D.prune;
+        k_sort_cells<0><<<grid, bs, 0, s->stream>>>(a);
+        FL_LAUNCH_CHECK("sort_cells");
+        return FL_OK;
     }
+    k_sort_cells<1><<<grid, bs, 0, s->stream>>>(a);
     FL_LAUNCH_CHECK("sort_cells");
+    if (s->n > 0) {
+        const int rows = s->D.prune ? mode : 0;
+        auto gather = s->batched ? (rows == 2 ? k_gather_sorted<true, 2>
+                                              : rows == 1 ? k_gather_sorted<true, 1> : k_gather_sorted<true, 0>)
+                                 : (rows == 2 ? k_gather_sorted<false, 2>
+                                              : rows == 1 ? k_gather_sorted<false, 1> : k_gather_sorted<false, 0>);
+        gather<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(
+            s->D, fl_scene_tab(s), s->n, s->src, s->cell_pre, s->off, s->f[F_POS].cur<float4>(),
+            s->f[F_VEL].cur<float4>(), s->f[F_VEVAL].cur<float4>(), s->f[F_CLR].cur<uint32_t>(),
+            s->f[F_POS].nxt<float4>(), s->f[F_VEL].nxt<float4>(), s->f[F_VEVAL].nxt<float4>(),
+            s->f[F_CLR].nxt<uint32_t>(), s->f[F_GCELL].nxt<uint32_t>(), s->f[F_GNDX].nxt<uint32_t>(), s->upbits);
+        FL_LAUNCH_CHECK("gather_sorted");
+    }
+    s->codes_valid = s->D.prune;
     return FL_OK;
 }
 
