@@ -63,8 +63,8 @@ k_scatter_index(int n, const uint32_t *__restrict__ cell_pre, const uint32_t *__
 }
 
 // ---------------------------------------------------------------------------
-// Canonical within-cell order. Each warp owns one cell segment of src and
-// sorts its point indices ascending, so slot off[c]+k holds the k-th lowest
+// Canonical within-cell order. A warp sorts the point indices of one cell
+// segment of src at a time, ascending, so slot off[c]+k holds the k-th lowest
 // index in cell c -- the order a serial insert (gndx = cnt[cell]++) yields.
 // Segments up to 128 points are sorted in registers by a warp bitonic
 // network (K keys per lane, element e = lane*K + r); larger ones take a
@@ -184,18 +184,67 @@ __device__ void sort_segment_dense(const SortArgs &a, uint32_t o, uint32_t m) {
     }
 }
 
+// Each warp owns kSortCells consecutive cell entries: one read of their
+// counts and offsets, then the cells that need ordering (a single point is
+// in order already, but mode 0 still records its rank). Cells of up to 64
+// points go through one pipeline, the next cell's keys loading while the
+// current one sorts; larger cells are sorted on their own afterwards.
+constexpr int kSortCells = 4;
+
 template <int MODE>
 __global__ void __launch_bounds__(kThreads)
 k_sort_cells(const __grid_constant__ SortArgs a) {
-    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (c >= a.gcells) return;
-    const uint32_t m = a.cnt[c];
-    if (m == 0) return;
-    const uint32_t o = a.off[c];
-    if (m <= 32) sort_segment<MODE, 1>(a, o, m);
-    else if (m <= 64) sort_segment<MODE, 2>(a, o, m);
-    else if (m <= 128) sort_segment<MODE, 4>(a, o, m);
-    else sort_segment_dense<MODE>(a, o, m);
+    const int c0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * kSortCells;
+    if (c0 >= a.gcells) return;
+    const unsigned lane = lane_id();
+    const int c = c0 + (int)lane;
+    const bool owned = lane < (unsigned)kSortCells && c < a.gcells;
+    const uint32_t my_m = owned ? a.cnt[c] : 0u;
+    const uint32_t my_o = owned ? a.off[c] : 0u;
+    const unsigned todo_all = __ballot_sync(0xffffffffu, my_m > (MODE == 0 ? 0u : 1u));
+    const unsigned large = __ballot_sync(0xffffffffu, my_m > 64u);
+    unsigned todo = todo_all & ~large;
+
+    uint32_t m = 0, o = 0, w0 = 0xffffffffu, w1 = 0xffffffffu;
+    auto fetch = [&]() {   // next small cell's size, offset and keys (element e = 2 lane + r)
+        if (!todo) { m = 0; return; }
+        const int k = __ffs(todo) - 1;
+        todo &= todo - 1u;
+        m = __shfl_sync(0xffffffffu, my_m, k);
+        o = __shfl_sync(0xffffffffu, my_o, k);
+        const uint32_t e = 2 * lane;
+        w0 = (e < m) ? a.src[o + e] : 0xffffffffu;
+        w1 = (e + 1 < m) ? a.src[o + e + 1] : 0xffffffffu;
+    };
+    fetch();
+    while (m) {
+        uint32_t v[2] = {w0, w1};
+        const uint32_t cm = m, co = o;
+        fetch();
+        // the insert hands out a cell's slots in ascending runs (one per
+        // insert warp), so a segment is often in order already
+        const uint32_t next = __shfl_down_sync(0xffffffffu, v[0], 1);
+        const bool in_order = __all_sync(0xffffffffu, v[0] <= v[1] && (lane == 31 || v[1] <= next));
+        if (in_order && MODE != 0) continue;
+        if (!in_order) warp_bitonic<2>(v);
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            const uint32_t e = 2 * lane + r;
+            if (e < cm) {
+                a.src[co + e] = v[r];
+                if (MODE == 0) a.gndx_pre[v[r]] = e;
+            }
+        }
+    }
+    unsigned rest = todo_all & large;
+    while (rest) {
+        const int k = __ffs(rest) - 1;
+        rest &= rest - 1u;
+        const uint32_t lm = __shfl_sync(0xffffffffu, my_m, k);
+        const uint32_t lo = __shfl_sync(0xffffffffu, my_o, k);
+        if (lm <= 128) sort_segment<MODE, 4>(a, lo, lm);
+        else sort_segment_dense<MODE>(a, lo, lm);
+    }
 }
 
 // The cell a warp owns: its scene's parameters, its entry index (global),
@@ -835,7 +884,7 @@ int fl_launch_sort_cells(fl_system *s, int mode) {
     a.off = s->off; a.cnt = s->cnt; a.src = s->src; a.scratch = s->rank_tmp;
     a.gcells = s->gcells;
     const int bs = s->blk_sort ? s->blk_sort : kThreads;
-    const int grid = blocks_for((long long)s->gcells, bs / 32);
+    const int grid = blocks_for((long long)s->gcells, (bs / 32) * kSortCells);
     if (mode == 0) {
         a.gndx_pre = s->f[F_GNDX].cur<uint32_t>();
         k_sort_cells<0><<<grid, bs, 0, s->stream>>>(a);
