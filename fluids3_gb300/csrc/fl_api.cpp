@@ -144,7 +144,7 @@ static void free_all(fl_system *s) {
     for (int k = 0; k < F_COUNT; k++)
         for (int c = 0; c < 2; c++) cudaFree(s->f[k].p[c]);
     cudaFree(s->cell_pre); cudaFree(s->rank_tmp); cudaFree(s->src); cudaFree(s->upbits);
-    cudaFree(s->hitlist); cudaFree(s->hitcnt);
+    cudaFree(s->hitlist); cudaFree(s->hitcnt); cudaFree(s->pairdata);
     cudaFree(s->d_scenes); cudaFree(s->point_scene); cudaFree(s->cell_scene);
     free(s->scene_point_base); free(s->scene_n); free(s->scene_cell_base); free(s->scene_ncells);
     free(s->scene_params);
@@ -206,6 +206,7 @@ extern "C" int fl_create(const fl_params *p, int max_points, fl_system **out) {
         s->D.hcap = kPairListCap;
         if ((r = fl_dalloc((void **)&s->hitlist, 4 * ((np + 31) / 32) * 32 * (size_t)kPairListCap)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&s->hitcnt, 4 * np)) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&s->pairdata, 2 * sizeof(float4) * np)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&s->dev_err, 256)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&s->time_dev, 256)) != FL_OK) break;
         if ((r = alloc_grid(s)) != FL_OK) break;

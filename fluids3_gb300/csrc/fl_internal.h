@@ -125,6 +125,9 @@ struct fl_system {
     // positions and grid are unchanged (lists_valid)
     uint32_t *hitlist;     // ceil(N/32) * hcap * 32 entries
     uint32_t *hitcnt;      // per point
+    // per slot, written with the lists: (pos.xyz, density), (veval.xyz, 0),
+    // so the force pass reads a neighbour's data from one 32-byte sector
+    float4 *pairdata;
     int lists_valid;
 
     // m_Time on the device, double-buffered by step parity so a captured

@@ -373,13 +373,15 @@ constexpr int kDensityMaxThreads = 1024;
 // computePressure (fluids4.0/fluid_kernels.cu:112-149). FGRID is the
 // identity after a full sort (cu:83), so neighbour slots are read directly.
 // With LIST the slots of the pairs that pass 0 < d^2 < rd2 are recorded, in
-// visiting order, for the force pass (same positions, same test).
+// visiting order, for the force pass (same positions, same test), together
+// with each point's pair record (position and density, evaluated velocity).
 template <bool PRUNE, bool LIST, bool BATCH>
 __global__ void __launch_bounds__(kDensityMaxThreads, 2)
 k_density(const __grid_constant__ DevParams P0, const SceneTab T, int n, const float4 *__restrict__ pos,
           const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ off,
           const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
-          float *__restrict__ press, uint32_t *__restrict__ hitlist, uint32_t *__restrict__ hitcnt) {
+          const float4 *__restrict__ veval, float *__restrict__ press, uint32_t *__restrict__ hitlist,
+          uint32_t *__restrict__ hitcnt, float4 *__restrict__ pairdata) {
     // pruned: the lanes of a warp take points with the same lower-band bits,
     // which decide the entries of the search block a point visits
     extern __shared__ uint32_t s_dyn[];
@@ -418,7 +420,12 @@ k_density(const __grid_constant__ DevParams P0, const SceneTab T, int n, const f
     sum = sum * P.pmass * P.poly6kern;
     if (sum == 0.0f) sum = 1.0f;
     press[i] = sum;
-    if (LIST) hitcnt[i] = nh;
+    if (LIST) {
+        hitcnt[i] = nh;
+        const float4 e = veval[i];
+        pairdata[2 * (size_t)i] = make_float4(p.x, p.y, p.z, sum);
+        pairdata[2 * (size_t)i + 1] = make_float4(e.x, e.y, e.z, 0.0f);
+    }
 }
 
 // computeForce (fluids4.0/fluid_kernels.cu:180-217) in two stages per warp:
@@ -438,21 +445,17 @@ struct ForcePoint {
     float3 f;
 };
 
-// One pair's term, added in the reference's operation order
-// (fluid_kernels.cu:203-210); j is known to pass 0 < d^2 < rd2.
-__device__ __forceinline__ void add_pair_force(const DevParams &P, ForcePoint &fp, uint32_t j,
-                                               const float4 *__restrict__ pos,
-                                               const float4 *__restrict__ veval,
-                                               const float *__restrict__ press) {
-    const float4 q = pos[j];
+// One pair's term from the neighbour's position q, evaluated velocity vj and
+// density dj, added in the reference's operation order
+// (fluid_kernels.cu:203-210); the pair is known to pass 0 < d^2 < rd2.
+__device__ __forceinline__ void add_pair_terms(const DevParams &P, ForcePoint &fp, float4 q, float4 vj,
+                                               float dj) {
     const float dx = fp.p.x - q.x, dy = fp.p.y - q.y, dz = fp.p.z - q.z;
     const float dsq = dx * dx + dy * dy + dz * dz;
     const float r = sqrtf(dsq * P.d2);
-    const float dj = press[j];
     const float pj = (dj - P.prest_dens) * P.pintstiff;
     const float cr = P.psmoothradius - r;
     const float pterm = P.sim_scale * -0.5f * cr * P.spikykern * (fp.pi + pj) / r;
-    const float4 vj = veval[j];
     const float sx = dx * pterm + (vj.x - fp.vi.x) * P.vterm;
     const float sy = dy * pterm + (vj.y - fp.vi.y) * P.vterm;
     const float sz = dz * pterm + (vj.z - fp.vi.z) * P.vterm;
@@ -460,6 +463,21 @@ __device__ __forceinline__ void add_pair_force(const DevParams &P, ForcePoint &f
     fp.f.x += (sx * cr) * inv;
     fp.f.y += (sy * cr) * inv;
     fp.f.z += (sz * cr) * inv;
+}
+
+// Neighbour j's data from the field arrays.
+__device__ __forceinline__ void add_pair_force(const DevParams &P, ForcePoint &fp, uint32_t j,
+                                               const float4 *__restrict__ pos,
+                                               const float4 *__restrict__ veval,
+                                               const float *__restrict__ press) {
+    add_pair_terms(P, fp, pos[j], veval[j], press[j]);
+}
+
+// Neighbour j's data from its pair record (the same values, one sector).
+__device__ __forceinline__ void add_pair_force_rec(const DevParams &P, ForcePoint &fp, uint32_t j,
+                                                   const float4 *__restrict__ pairdata) {
+    const float4 q = pairdata[2 * (size_t)j];
+    add_pair_terms(P, fp, q, pairdata[2 * (size_t)j + 1], q.w);
 }
 
 __device__ __forceinline__ void drain_hits(const DevParams &P, ForcePoint &fp, uint32_t &nhits,
@@ -486,7 +504,8 @@ __device__ __forceinline__ float3 force_of(const DevParams &P, int i, bool activ
                                            const uint32_t *__restrict__ cnt,
                                            const uint32_t *__restrict__ upbits,
                                            const uint32_t *__restrict__ hitlist,
-                                           const uint32_t *__restrict__ hitcnt) {
+                                           const uint32_t *__restrict__ hitcnt,
+                                           const float4 *__restrict__ pairdata) {
     ForcePoint fp;
     fp.f = make_float3(0.0f, 0.0f, 0.0f);
     uint32_t my_code = 0;
@@ -509,11 +528,11 @@ __device__ __forceinline__ float3 force_of(const DevParams &P, int i, bool activ
         if (!__any_sync(0xffffffffu, over)) {
             const uint32_t most = __reduce_max_sync(0xffffffffu, nh);
             for (uint32_t t = 0; t < most; t++)
-                if (t < nh) add_pair_force(P, fp, hitlist[list_at(P, i, t)], pos, veval, press);
+                if (t < nh) add_pair_force_rec(P, fp, hitlist[list_at(P, i, t)], pairdata);
             return fp.f;
         }
         if (!over) {
-            for (uint32_t t = 0; t < nh; t++) add_pair_force(P, fp, hitlist[list_at(P, i, t)], pos, veval, press);
+            for (uint32_t t = 0; t < nh; t++) add_pair_force_rec(P, fp, hitlist[list_at(P, i, t)], pairdata);
             return fp.f;
         }
         for (int c = 0; c < P.gridAdjCnt; c++) {
@@ -560,13 +579,13 @@ k_force(const __grid_constant__ DevParams P0, const SceneTab T, int n, const flo
         const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ off,
         const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
         const uint32_t *__restrict__ hitlist, const uint32_t *__restrict__ hitcnt,
-        float4 *__restrict__ force) {
+        const float4 *__restrict__ pairdata, float4 *__restrict__ force) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const DevParams &P = (BATCH && i < n) ? T.params[T.point_scene[i]] : P0;
     const uint32_t gc = (i < n) ? gcell[i] : kUndef;
     const bool active = gc != kUndef;
     const float3 f = force_of<PRUNE, LIST>(P, i, active, gc, pos, veval, press, off, cnt, upbits,
-                                           hitlist, hitcnt);
+                                           hitlist, hitcnt, pairdata);
     if (i < n) force[i] = active ? make_float4(f.x, f.y, f.z, 0.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
@@ -683,7 +702,7 @@ k_force_advance(const __grid_constant__ DevParams P0, const SceneTab T, int n, f
                 const uint32_t *__restrict__ off, const uint32_t *__restrict__ cnt,
                 const uint32_t *__restrict__ upbits,
                 const uint32_t *__restrict__ hitlist, const uint32_t *__restrict__ hitcnt,
-                float4 *__restrict__ vel, float4 *__restrict__ force,
+                const float4 *__restrict__ pairdata, float4 *__restrict__ vel, float4 *__restrict__ force,
                 float4 *__restrict__ pos_out, float4 *__restrict__ veval_out,
                 uint32_t *__restrict__ err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -693,7 +712,7 @@ k_force_advance(const __grid_constant__ DevParams P0, const SceneTab T, int n, f
     const uint32_t gc = (i < n) ? gcell[i] : kUndef;
     const bool active = gc != kUndef;
     const float3 f = force_of<PRUNE, LIST>(P, i, active, gc, pos_in, veval_in, press, off, cnt, upbits,
-                                           hitlist, hitcnt);
+                                           hitlist, hitcnt, pairdata);
     if (i >= n) return;
     if (!active) {
         force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -954,7 +973,7 @@ int fl_launch_density(fl_system *s) {
     const int bs = s->blk_density ? s->blk_density : kThreads;
     kern<<<blocks_for(s->n, bs), bs, grouping_smem(bs, kBandKeys), s->stream>>>(
         s->D, fl_scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt,
-        s->upbits, s->f[F_PRESS].cur<float>(), s->hitlist, s->hitcnt);
+        s->upbits, s->f[F_VEVAL].cur<float4>(), s->f[F_PRESS].cur<float>(), s->hitlist, s->hitcnt, s->pairdata);
     FL_LAUNCH_CHECK("density");
     s->lists_valid = 1;
     return FL_OK;
@@ -978,7 +997,7 @@ int fl_launch_force(fl_system *s) {
     kern<<<blocks_for(s->n, bs), bs, 0, s->stream>>>(
         s->D, fl_scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->f[F_VEVAL].cur<float4>(),
         s->f[F_PRESS].cur<float>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt, s->upbits,
-        s->hitlist, s->hitcnt, s->f[F_FORCE].cur<float4>());
+        s->hitlist, s->hitcnt, s->pairdata, s->f[F_FORCE].cur<float4>());
     FL_LAUNCH_CHECK("force");
     return FL_OK;
 }
@@ -992,7 +1011,7 @@ int fl_launch_force_advance(fl_system *s, float dt) {
     kern<<<blocks_for(s->n > 0 ? s->n : 1, bs), bs, 0, s->stream>>>(
         s->D, fl_scene_tab(s), s->n, s->time_dev, s->time_slot, dt, s->f[F_POS].cur<float4>(),
         s->f[F_VEVAL].cur<float4>(), s->f[F_PRESS].cur<float>(), s->f[F_GCELL].cur<uint32_t>(), s->off,
-        s->cnt, s->upbits, s->hitlist, s->hitcnt,
+        s->cnt, s->upbits, s->hitlist, s->hitcnt, s->pairdata,
         s->f[F_VEL].cur<float4>(), s->f[F_FORCE].cur<float4>(),
         s->f[F_POS].nxt<float4>(), s->f[F_VEVAL].nxt<float4>(), s->dev_err);
     FL_LAUNCH_CHECK("force_advance");

@@ -307,6 +307,7 @@ static int backward_step(fl_system *s, fl_tape *t, const float4 *state, const fl
     }();
     s->hitlist = own_list;
     s->hitcnt = own_cnt;
+    if (slot >= 0) s->lists_valid = 0;   // the live lists (and pair records) are not this state's
     if (r != FL_OK) return r;
     t->gcur = x;
     return FL_OK;
