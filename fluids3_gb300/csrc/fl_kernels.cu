@@ -693,8 +693,10 @@ k_advance(const __grid_constant__ DevParams P0, const SceneTab T, int n, float t
 // Force then advance for one point: the last two phases of Run fused.
 // Neighbour reads come from pos_in/veval_in; the new position and evaluated
 // velocity go to the other copies, velocity and force are updated in place.
+// Bounded to 40 registers (12 blocks of 128 per SM): the pair loop waits on
+// its neighbour reads, and the extra resident warps outweigh the spills.
 template <bool PRUNE, bool LIST, bool BATCH>
-__global__ void __launch_bounds__(kForceThreads)
+__global__ void __launch_bounds__(kForceThreads, 12)
 k_force_advance(const __grid_constant__ DevParams P0, const SceneTab T, int n, float *time_dev, int slot,
                 float dt,
                 const float4 *__restrict__ pos_in, const float4 *__restrict__ veval_in,
