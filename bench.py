@@ -60,11 +60,11 @@ ALGO_BYTES = {
     "insert": 20,          # R pos 12, W cell + rank 8
     "scan": 0,             # per cell: R 4, W 4 (+ clear 4) -> 12 B/cell
     "scatter": 12,         # R cell + rank 8, W src 4
-    "sort": 92,            # R pos, vel, veval, clr, gcell, gndx; W pos, vel, veval, clr, gcell
+    "sort": 92,            # cell sort + gather: R pos, vel, veval, clr, gcell, gndx; W pos, vel, veval, clr, gcell
     "density": 16,         # R pos 12, W density 4
     "force_advance": 128,  # force 40 (R pos, veval, density; W F) + advance 88
 }
-KERNELS_PER_STEP = 6
+KERNELS_PER_STEP = 7   # insert, scan, scatter, cell sort, gather, density, force+advance
 
 
 def parse():

@@ -399,23 +399,28 @@ k_density(const __grid_constant__ DevParams P0, const SceneTab T, int n, const f
     const uint32_t my_code = __float_as_uint(p.w);
     float sum = 0.0f;
     uint32_t nh = 0;
+    auto visit = [&](uint32_t j) {
+        const float4 q = pos[j];
+        const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+        float dsq = dx * dx + dy * dy + dz * dz;
+        if (dsq < P.rd2 && dsq > 0.0f) {
+            dsq = (P.rd2 - dsq) * P.d2;
+            sum += dsq * dsq * dsq;
+            if (LIST) {
+                if (nh < (uint32_t)P.hcap) hitlist[list_at(P, i, nh)] = j;
+                nh++;
+            }
+        }
+    };
     for (int c = 0; c < P.gridAdjCnt; c++) {
         CandIter it;
         cand_begin<PRUNE>(it, P, c, base + P.adj[c], my_code, true, off, cnt, upbits);
-        uint32_t j;
-        while (cand_next<PRUNE>(it, P, upbits, j)) {
-            const float4 q = pos[j];
-            const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-            float dsq = dx * dx + dy * dy + dz * dz;
-            if (dsq < P.rd2 && dsq > 0.0f) {
-                dsq = (P.rd2 - dsq) * P.d2;
-                sum += dsq * dsq * dsq;
-                if (LIST) {
-                    if (nh < (uint32_t)P.hcap) hitlist[list_at(P, i, nh)] = j;
-                    nh++;
-                }
-            }
+        if (PRUNE && it.U == 0u) {   // the own cell: no flags to consult, every slot in order
+            for (uint32_t j = it.lo; j < it.hi; j++) visit(j);
+            continue;
         }
+        uint32_t j;
+        while (cand_next<PRUNE>(it, P, upbits, j)) visit(j);
     }
     sum = sum * P.pmass * P.poly6kern;
     if (sum == 0.0f) sum = 1.0f;
