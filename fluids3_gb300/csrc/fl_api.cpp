@@ -145,6 +145,7 @@ static void free_all(fl_system *s) {
         for (int c = 0; c < 2; c++) cudaFree(s->f[k].p[c]);
     cudaFree(s->cell_pre); cudaFree(s->rank_tmp); cudaFree(s->src); cudaFree(s->upbits);
     cudaFree(s->hitlist); cudaFree(s->hitcnt); cudaFree(s->pairdata);
+    cudaFree(s->big_cells); cudaFree(s->big_count);
     cudaFree(s->d_scenes); cudaFree(s->point_scene); cudaFree(s->cell_scene);
     free(s->scene_point_base); free(s->scene_n); free(s->scene_cell_base); free(s->scene_ncells);
     free(s->scene_params);
@@ -207,11 +208,20 @@ extern "C" int fl_create(const fl_params *p, int max_points, fl_system **out) {
         if ((r = fl_dalloc((void **)&s->hitlist, 4 * ((np + 31) / 32) * 32 * (size_t)kPairListCap)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&s->hitcnt, 4 * np)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&s->pairdata, 2 * sizeof(float4) * np)) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&s->big_cells, 4 * fl_big_cells_cap(max_points))) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&s->big_count, 256)) != FL_OK) break;
+        if (cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, s->device) != cudaSuccess ||
+            s->num_sms < 1) {
+            r = fl_fail(FL_ERR_CUDA, "fl_create: SM count");
+            break;
+        }
+        if ((r = fl_kernels_init(s)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&s->dev_err, 256)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&s->time_dev, 256)) != FL_OK) break;
         if ((r = alloc_grid(s)) != FL_OK) break;
         if (cudaMemsetAsync(s->dev_err, 0, 256, s->stream) != cudaSuccess ||
-            cudaMemsetAsync(s->time_dev, 0, 256, s->stream) != cudaSuccess) {
+            cudaMemsetAsync(s->time_dev, 0, 256, s->stream) != cudaSuccess ||
+            cudaMemsetAsync(s->big_count, 0, 256, s->stream) != cudaSuccess) {
             r = fl_fail(FL_ERR_CUDA, "fl_create: memset failed");
             break;
         }

@@ -123,6 +123,10 @@ struct fl_system {
 
     // pairs found by the density pass, reused by the force pass while the
     // positions and grid are unchanged (lists_valid)
+    uint32_t *big_cells;   // cell entries above 128 points, listed by the cell sort (fl_big_cells_cap)
+    uint32_t *big_count;   // [0] their number, [1] k_sort_big's sign-off count (256 B slot, zeroed at creation)
+    int num_sms;
+
     uint32_t *hitlist;     // ceil(N/32) * hcap * 32 entries
     uint32_t *hitcnt;      // per point
     // per slot, written with the lists: (pos.xyz, density), (veval.xyz, 0),
@@ -231,6 +235,10 @@ int fl_launch_scatter_index(fl_system *s);
 //         nxt copies with band codes and the upper-band slot flags (rows 0-2)
 // mode 2: mode 1 that also writes the lower-band slot flags (upbits rows 3-5)
 int fl_launch_sort_cells(fl_system *s, int mode);
+// one-time kernel attributes (shared memory of the crowded-cell sort)
+int fl_kernels_init(fl_system *s);
+// entries of the crowded-cell list for max_points points (cells above 128)
+size_t fl_big_cells_cap(int max_points);
 // gather every field cur -> nxt through src (phase-API counting sort)
 int fl_launch_gather_all(fl_system *s);
 int fl_launch_band_codes(fl_system *s);

@@ -10,6 +10,7 @@
 // float4 (16 B aligned, one vector load per particle); density, colour,
 // cell and within-cell index are 4-byte scalars. All particle fields are
 // held twice (see Field in fl_internal.h).
+#include <algorithm>
 #include <stdio.h>
 
 #include "fl_internal.h"
@@ -109,6 +110,8 @@ struct SortArgs {
     const uint32_t *off, *cnt;
     uint32_t *src, *scratch;
     uint32_t *gndx_pre;                // mode 0: canonical gndx by pre-sort index
+    uint32_t *big_cells, *big_count;   // cell entries above 128 points, for k_sort_big
+    uint32_t big_cap;
     int gcells;                        // internal cell entries (all scenes, bins included)
 };
 
@@ -132,63 +135,12 @@ __device__ __forceinline__ void sort_segment(const SortArgs &a, uint32_t o, uint
     }
 }
 
-// Segments above 128 points: sort each 128-key chunk in registers, then
-// place every key at its rank -- its index within its own chunk plus, for
-// each other chunk, the number of smaller keys there (a binary search) --
-// through the scratch array. Keys are distinct point indices.
-__device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t *a, uint32_t len, uint32_t key) {
-    uint32_t lo = 0, hi = len;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (a[mid] < key) lo = mid + 1; else hi = mid;
-    }
-    return lo;
-}
-
-template <int MODE>
-__device__ void sort_segment_dense(const SortArgs &a, uint32_t o, uint32_t m) {
-    const unsigned lane = lane_id();
-    constexpr uint32_t kChunk = 128;
-    for (uint32_t cb = 0; cb < m; cb += kChunk) {
-        uint32_t v[4];
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-            const uint32_t e = cb + lane * 4 + r;
-            v[r] = (e < m) ? a.src[o + e] : 0xffffffffu;
-        }
-        warp_bitonic<4>(v);
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-            const uint32_t e = cb + lane * 4 + r;
-            if (e < m) a.src[o + e] = v[r];
-        }
-    }
-    __syncwarp();
-    const uint32_t nch = (m + kChunk - 1) / kChunk;
-    for (uint32_t k = lane; k < m; k += 32) {
-        const uint32_t key = a.src[o + k];
-        const uint32_t mine = k / kChunk;
-        uint32_t rank = k - mine * kChunk;
-        for (uint32_t ch = 0; ch < nch; ch++) {
-            if (ch == mine) continue;
-            const uint32_t lo = ch * kChunk;
-            rank += lower_bound_u32(a.src + o + lo, min(kChunk, m - lo), key);
-        }
-        a.scratch[o + rank] = key;
-    }
-    __syncwarp();
-    for (uint32_t k = lane; k < m; k += 32) {
-        const uint32_t key = a.scratch[o + k];
-        a.src[o + k] = key;
-        if (MODE == 0) a.gndx_pre[key] = k;
-    }
-}
-
 // Each warp owns kSortCells consecutive cell entries: one read of their
 // counts and offsets, then the cells that need ordering (a single point is
 // in order already, but mode 0 still records its rank). Cells of up to 64
 // points go through one pipeline, the next cell's keys loading while the
-// current one sorts; larger cells are sorted on their own afterwards.
+// current one sorts; cells of 65-128 points are sorted on their own
+// afterwards; larger ones are listed for k_sort_big.
 constexpr int kSortCells = 4;
 
 template <int MODE>
@@ -242,8 +194,101 @@ k_sort_cells(const __grid_constant__ SortArgs a) {
         rest &= rest - 1u;
         const uint32_t lm = __shfl_sync(0xffffffffu, my_m, k);
         const uint32_t lo = __shfl_sync(0xffffffffu, my_o, k);
-        if (lm <= 128) sort_segment<MODE, 4>(a, lo, lm);
-        else sort_segment_dense<MODE>(a, lo, lm);
+        if (lm <= 128) {
+            sort_segment<MODE, 4>(a, lo, lm);
+        } else if (lane == 0) {
+            const uint32_t slot = atomicAdd(a.big_count, 1u);
+            if (slot < a.big_cap) a.big_cells[slot] = (uint32_t)(c0 + k);
+        }
+    }
+}
+
+// Cells above 128 points (crowded regions: a collapsing scene can hold
+// thousands of points in one cell), one block of kBigThreads per cell: up
+// to kBigChunk keys are sorted by a block bitonic network in shared memory;
+// a larger cell is sorted in chunks of kBigChunk, then every key is placed
+// at its rank -- its index in its own chunk plus, for each other chunk, the
+// number of smaller keys there (a binary search) -- through the scratch
+// array. Keys are distinct point indices. Needs kBigChunk * 4 bytes of
+// dynamic shared memory.
+constexpr int kBigThreads = 1024;
+constexpr uint32_t kBigChunk = 16384;
+
+__device__ __forceinline__ void block_bitonic(uint32_t *s, uint32_t p2) {   // p2: a power of two
+    for (uint32_t size = 2; size <= p2; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t t = threadIdx.x; t < p2 / 2; t += blockDim.x) {
+                const uint32_t i = ((t & ~(stride - 1u)) << 1) | (t & (stride - 1u));
+                const uint32_t j = i + stride;
+                const uint32_t x = s[i], y = s[j];
+                if ((x > y) == ((i & size) == 0)) { s[i] = y; s[j] = x; }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Sorts src[o, o+len) in place through shared memory (all threads call it).
+__device__ __forceinline__ void block_sort_range(uint32_t *s_keys, uint32_t *src, uint32_t o, uint32_t len) {
+    uint32_t p2 = 256;
+    while (p2 < len) p2 <<= 1;
+    for (uint32_t e = threadIdx.x; e < p2; e += blockDim.x) s_keys[e] = (e < len) ? src[o + e] : 0xffffffffu;
+    __syncthreads();
+    block_bitonic(s_keys, p2);
+    for (uint32_t e = threadIdx.x; e < len; e += blockDim.x) src[o + e] = s_keys[e];
+    __syncthreads();
+}
+
+__device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t *a, uint32_t len, uint32_t key) {
+    uint32_t lo = 0, hi = len;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kBigThreads)
+k_sort_big(const __grid_constant__ SortArgs a) {
+    extern __shared__ uint32_t s_keys[];
+    __shared__ uint32_t s_nbig;
+    if (threadIdx.x == 0) s_nbig = min(*(volatile uint32_t *)a.big_count, a.big_cap);
+    __syncthreads();
+    const uint32_t nbig = s_nbig;
+    for (uint32_t b = blockIdx.x; b < nbig; b += gridDim.x) {
+        const uint32_t c = a.big_cells[b];
+        const uint32_t m = a.cnt[c], o = a.off[c];
+        for (uint32_t cb = 0; cb < m; cb += kBigChunk) block_sort_range(s_keys, a.src, o + cb, min(kBigChunk, m - cb));
+        if (m > kBigChunk) {
+            const uint32_t nch = (m + kBigChunk - 1) / kBigChunk;
+            for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) {
+                const uint32_t key = a.src[o + k];
+                const uint32_t mine = k / kBigChunk;
+                uint32_t rank = k - mine * kBigChunk;
+                for (uint32_t ch = 0; ch < nch; ch++) {
+                    if (ch == mine) continue;
+                    const uint32_t lo = ch * kBigChunk;
+                    rank += lower_bound_u32(a.src + o + lo, min(kBigChunk, m - lo), key);
+                }
+                a.scratch[o + rank] = key;
+            }
+            __syncthreads();
+            for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) a.src[o + k] = a.scratch[o + k];
+            __syncthreads();
+        }
+        if (MODE == 0)
+            for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) a.gndx_pre[a.src[o + k]] = k;
+        __syncthreads();
+    }
+    // the last block to finish clears the list for the next sort (every
+    // block has read the count before it signs off)
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(a.big_count + 1, 1u) == gridDim.x - 1) {
+            a.big_count[0] = 0;
+            a.big_count[1] = 0;
+        }
     }
 }
 
@@ -905,20 +950,41 @@ int fl_launch_scatter_index(fl_system *s) {
     return FL_OK;
 }
 
+int fl_kernels_init(fl_system *s) {
+    (void)s;
+    const int smem = (int)(kBigChunk * sizeof(uint32_t));
+    FL_CUDA_TRY(cudaFuncSetAttribute(k_sort_big<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    FL_CUDA_TRY(cudaFuncSetAttribute(k_sort_big<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    return FL_OK;
+}
+
+size_t fl_big_cells_cap(int max_points) { return (size_t)(max_points > 0 ? max_points : 1) / 129 + 1; }
+
 int fl_launch_sort_cells(fl_system *s, int mode) {
     SortArgs a = {};
     a.off = s->off; a.cnt = s->cnt; a.src = s->src; a.scratch = s->rank_tmp;
+    a.big_cells = s->big_cells; a.big_count = s->big_count;
+    a.big_cap = (uint32_t)fl_big_cells_cap(s->max_points);
     a.gcells = s->gcells;
+    if (mode == 0) a.gndx_pre = s->f[F_GNDX].cur<uint32_t>();
     const int bs = s->blk_sort ? s->blk_sort : kThreads;
     const int grid = blocks_for((long long)s->gcells, (bs / 32) * kSortCells);
+    // crowded cells: at most n / 129 of them, one block each, a block per SM;
+    // the list count (big_count[0]) and the blocks' sign-off count
+    // (big_count[1]) start at zero and k_sort_big leaves them so
+    const int big_grid = (int)std::min<size_t>((size_t)s->num_sms, fl_big_cells_cap(s->n));
+    const size_t big_smem = kBigChunk * sizeof(uint32_t);
     if (mode == 0) {
-        a.gndx_pre = s->f[F_GNDX].cur<uint32_t>();
         k_sort_cells<0><<<grid, bs, 0, s->stream>>>(a);
         FL_LAUNCH_CHECK("sort_cells");
+        k_sort_big<0><<<big_grid, kBigThreads, big_smem, s->stream>>>(a);
+        FL_LAUNCH_CHECK("sort_big");
         return FL_OK;
     }
     k_sort_cells<1><<<grid, bs, 0, s->stream>>>(a);
     FL_LAUNCH_CHECK("sort_cells");
+    k_sort_big<1><<<big_grid, kBigThreads, big_smem, s->stream>>>(a);
+    FL_LAUNCH_CHECK("sort_big");
     if (s->n > 0) {
         const int rows = s->D.prune ? mode : 0;
         auto gather = s->batched ? (rows == 2 ? k_gather_sorted<true, 2>

@@ -230,6 +230,50 @@ def test_crowded_cell_canonical_order(m):
         assert_bit_equal(s.GetBuffer(F.FFORCE), ref.force, f"m={m} force")
 
 
+@pytest.mark.parametrize("m", [16384, 16385, 20000])
+def test_crowded_cell_sorted_in_chunks(m):
+    """A cell above one shared-memory chunk of the crowded-cell sort (16,384
+    keys): chunks sorted apiece, then ranked across chunks. Phase API (the
+    rank-only sort) and one fused step (the sort feeding the gather)."""
+    sc = scenes.dam_break(n=m + 6000, seed=9)
+    p = sc.params
+    rng = np.random.default_rng(m)
+    pos = sc.pos.copy()
+    pick = rng.choice(pos.shape[0], size=m, replace=False)
+    c = np.array([p.gridMin[0] + 7.5 * 5.0, p.gridMin[1] + 5.5 * 5.0, p.gridMin[2] + 6.5 * 5.0], np.float32)
+    pos[pick] = c + rng.uniform(-2.0, 2.0, size=(m, 3)).astype(np.float32)
+    with make_system(p, pos, clr=sc.clr) as s:
+        gcell, gndx, gcnt = s.InsertParticlesCUDA(readback=True)
+        ref = O.State.new(p, pos, clr=sc.clr)
+        O.insert(p, ref)
+        assert_bit_equal(gndx, ref.gndx, "gndx")
+        assert gcnt.max() >= m
+        s.PrefixSumCellsCUDA(1)
+        s.CountingSortFullCUDA()
+        O.prefix_sum(p, ref)
+        O.counting_sort(p, ref)
+        st = gpu_state(s)
+        for k in ("pos", "gcell", "gndx", "clr"):
+            assert_bit_equal(st[k], getattr(ref, k), f"m={m} {k}")
+        assert s.IntegrityCheck() == 0
+    with make_system(p, pos, sc.vel, sc.veval, sc.clr) as s:
+        s.RunSteps(1)
+        s.Sync()
+        st = gpu_state(s)
+    ref = O.State.new(p, pos, sc.vel, sc.veval, sc.clr)
+    if m == 20000:   # the oracle's neighbour passes over one cell are O(m^2)
+        O.run(p, ref, 1, 0.0, threads=8)
+        for k in FIELDS:
+            assert_bit_equal(st[k], getattr(ref, k), f"crowded m={m} {k}")
+    else:
+        O.insert(p, ref)
+        O.prefix_sum(p, ref)
+        O.counting_sort(p, ref)
+        # the step's sort fixed these; its advance moved only the positions
+        for k in ("gcell", "gndx", "clr"):
+            assert_bit_equal(st[k], getattr(ref, k), f"m={m} {k}")
+
+
 @pytest.mark.parametrize("m", [90, 700, 2500])
 def test_crowded_cell_fused_steps(m):
     sc = scenes.dam_break(n=5000, seed=18)
