@@ -64,6 +64,8 @@ SIGNATURES = [
     ("fl_batch_set_params", C.c_int, [vp, C.c_int, C.POINTER(FlParams)]),
     ("fl_add_particles", C.c_int, [vp, C.c_int, vp, vp, vp, vp]),
     ("fl_autotune", C.c_int, [vp, C.c_int, vp]),
+    ("fl_launch_shapes", C.c_int, [vp, vp]),
+    ("fl_set_launch_shapes", C.c_int, [vp, vp]),
     ("fl_conservation", C.c_int, [vp, vp]),
     ("fl_pts_write", C.c_int, [C.c_char_p, C.c_int, vp, vp, vp, vp]),
     ("fl_pts_read", C.c_int, [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), vp, vp, vp, vp]),

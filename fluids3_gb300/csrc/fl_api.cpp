@@ -1021,11 +1021,12 @@ static int restore_slot(fl_system *s, int slot) {
     return FL_OK;
 }
 
-// Block-shape autotuner: for each tunable pass in turn (density, force,
-// sort) every candidate block size is timed over `steps` eager steps from
-// the same saved state, the others held at their best so far; the state is
-// restored at the end. Block sizes change no result: each point's work is
-// one thread's (or one warp's, the sort's cell) whatever the block.
+// Launch-shape autotuner: for each knob in turn (density, force and sort
+// block sizes, then the cell sort's cells per warp) every candidate is timed
+// over `steps` eager steps from the same saved state, the others held at
+// their best so far; the state is restored at the end. Shapes change no
+// result: each point's work is one thread's (a cell's sort one warp's)
+// whatever the block, the thread order within it or the cells per warp.
 extern "C" int fl_autotune(fl_system *s, int steps, int *chosen) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_autotune: null system");
     if (steps < 1) return fl_fail(FL_ERR_ARG, "fl_autotune: steps < 1");
@@ -1033,14 +1034,14 @@ extern "C" int fl_autotune(fl_system *s, int steps, int *chosen) {
     if (s->n == 0) return FL_OK;
     const int slot = FL_MAX_CHECKPOINTS;   // the tuner's own checkpoint slot
     FL_TRY(save_slot(s, slot));
-    int *knob[3] = {&s->blk_density, &s->blk_force, &s->blk_sort};
-    const int cand[3][4] = {{128, 256, 512, 1024}, {32, 64, 128, 0}, {64, 128, 256, 0}};
+    int *knob[4] = {&s->blk_density, &s->blk_force, &s->blk_sort, &s->sort_cells};
+    const int cand[4][4] = {{128, 256, 512, 1024}, {32, 64, 128, 0}, {64, 128, 256, 0}, {2, 4, 8, 0}};
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     FL_CUDA_TRY(cudaEventCreate(&e0));
     cudaError_t ce = cudaEventCreate(&e1);
     if (ce != cudaSuccess) { cudaEventDestroy(e0); return fl_fail(FL_ERR_CUDA, "fl_autotune: event"); }
     int r = FL_OK;
-    for (int k = 0; k < 3 && r == FL_OK; k++) {
+    for (int k = 0; k < 4 && r == FL_OK; k++) {
         int best = 0;
         float best_ms = 0.0f;
         for (int c = 0; c < 4 && cand[k][c] && r == FL_OK; c++) {
@@ -1067,6 +1068,30 @@ extern "C" int fl_autotune(fl_system *s, int steps, int *chosen) {
         chosen[0] = s->blk_density; chosen[1] = s->blk_force; chosen[2] = s->blk_sort;
     }
     return r;
+}
+
+extern "C" int fl_set_launch_shapes(fl_system *s, const int *shapes) {
+    if (!s || !shapes) return fl_fail(FL_ERR_ARG, "fl_set_launch_shapes: null argument");
+    const int d = shapes[0], f = shapes[1], so = shapes[2], c = shapes[3];
+    auto block_ok = [](int v, int hi) { return v == 0 || (v >= 32 && v <= hi && v % 32 == 0); };
+    if (!block_ok(d, 1024) || !block_ok(f, 128) || !block_ok(so, 256) || !(c == 0 || c == 2 || c == 4 || c == 8))
+        return fl_fail(FL_ERR_ARG, "fl_set_launch_shapes: density 32..1024, force 32..128, sort 32..256 threads "
+                                   "(multiples of 32), 2, 4 or 8 cells per warp (0: default)");
+    s->blk_density = d;
+    s->blk_force = f;
+    s->blk_sort = so;
+    s->sort_cells = c;
+    destroy_graph(s);   // the captured step holds the old shapes
+    return FL_OK;
+}
+
+extern "C" int fl_launch_shapes(fl_system *s, int *shapes) {
+    if (!s || !shapes) return fl_fail(FL_ERR_ARG, "fl_launch_shapes: null argument");
+    shapes[0] = s->blk_density ? s->blk_density : 256;
+    shapes[1] = s->blk_force ? s->blk_force : 128;
+    shapes[2] = s->blk_sort ? s->blk_sort : 256;
+    shapes[3] = s->sort_cells ? s->sort_cells : 4;
+    return FL_OK;
 }
 
 extern "C" int fl_conservation(fl_system *s, double *out) {

@@ -152,6 +152,7 @@ struct fl_system {
     // threads per block of the sort, density and force passes (0: the
     // compiled default); set by fl_autotune, results do not depend on them
     int blk_sort, blk_density, blk_force;
+    int sort_cells;        // cell entries per warp of the cell sort (0: the compiled default)
 
     // graph replay for fl_run_steps
     cudaGraphExec_t graph_exec;

@@ -135,7 +135,8 @@ __device__ __forceinline__ void sort_segment(const SortArgs &a, uint32_t o, uint
     }
 }
 
-// Each warp owns kSortCells consecutive cell entries: one read of their
+// Each warp owns CELLS consecutive cell entries (2, 4 or 8; the autotuner's
+// cells-per-warp knob, 4 by default): one read of their
 // counts and offsets, then the cells that need ordering (a single point is
 // in order already, but mode 0 still records its rank). Cells of up to 64
 // points go through one pipeline, the next cell's keys loading while the
@@ -143,14 +144,14 @@ __device__ __forceinline__ void sort_segment(const SortArgs &a, uint32_t o, uint
 // afterwards; larger ones are listed for k_sort_big.
 constexpr int kSortCells = 4;
 
-template <int MODE>
+template <int MODE, int CELLS>
 __global__ void __launch_bounds__(kThreads)
 k_sort_cells(const __grid_constant__ SortArgs a) {
-    const int c0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * kSortCells;
+    const int c0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * CELLS;
     if (c0 >= a.gcells) return;
     const unsigned lane = lane_id();
     const int c = c0 + (int)lane;
-    const bool owned = lane < (unsigned)kSortCells && c < a.gcells;
+    const bool owned = lane < (unsigned)CELLS && c < a.gcells;
     const uint32_t my_m = owned ? a.cnt[c] : 0u;
     const uint32_t my_o = owned ? a.off[c] : 0u;
     const unsigned todo_all = __ballot_sync(0xffffffffu, my_m > (MODE == 0 ? 0u : 1u));
@@ -968,20 +969,26 @@ int fl_launch_sort_cells(fl_system *s, int mode) {
     a.gcells = s->gcells;
     if (mode == 0) a.gndx_pre = s->f[F_GNDX].cur<uint32_t>();
     const int bs = s->blk_sort ? s->blk_sort : kThreads;
-    const int grid = blocks_for((long long)s->gcells, (bs / 32) * kSortCells);
+    const int cells = s->sort_cells ? s->sort_cells : kSortCells;
+    const int grid = blocks_for((long long)s->gcells, (bs / 32) * cells);
+    auto sort_kernel = [&](int mode) {
+        if (cells == 2) return mode == 0 ? k_sort_cells<0, 2> : k_sort_cells<1, 2>;
+        if (cells == 8) return mode == 0 ? k_sort_cells<0, 8> : k_sort_cells<1, 8>;
+        return mode == 0 ? k_sort_cells<0, 4> : k_sort_cells<1, 4>;
+    };
     // crowded cells: at most n / 129 of them, one block each, a block per SM;
     // the list count (big_count[0]) and the blocks' sign-off count
     // (big_count[1]) start at zero and k_sort_big leaves them so
     const int big_grid = (int)std::min<size_t>((size_t)s->num_sms, fl_big_cells_cap(s->n));
     const size_t big_smem = kBigChunk * sizeof(uint32_t);
     if (mode == 0) {
-        k_sort_cells<0><<<grid, bs, 0, s->stream>>>(a);
+        sort_kernel(0)<<<grid, bs, 0, s->stream>>>(a);
         FL_LAUNCH_CHECK("sort_cells");
         k_sort_big<0><<<big_grid, kBigThreads, big_smem, s->stream>>>(a);
         FL_LAUNCH_CHECK("sort_big");
         return FL_OK;
     }
-    k_sort_cells<1><<<grid, bs, 0, s->stream>>>(a);
+    sort_kernel(1)<<<grid, bs, 0, s->stream>>>(a);
     FL_LAUNCH_CHECK("sort_cells");
     k_sort_big<1><<<big_grid, kBigThreads, big_smem, s->stream>>>(a);
     FL_LAUNCH_CHECK("sort_big");

@@ -344,10 +344,22 @@ class FluidSystem:
         return out
 
     def Autotune(self, steps: int = 3) -> dict:
-        """Pick the fastest block shapes for this system's work (state kept)."""
-        out = (C.c_int * 3)()
-        call("fl_autotune", self._h, int(steps), out)
-        return {"density": out[0], "force": out[1], "sort": out[2]}
+        """Pick the fastest launch shapes for this system's work (state kept)."""
+        call("fl_autotune", self._h, int(steps), None)
+        return self.LaunchShapes()
+
+    def LaunchShapes(self) -> dict:
+        """Threads per block of the density, force and sort passes and cell
+        entries per warp of the cell sort."""
+        out = (C.c_int * 4)()
+        call("fl_launch_shapes", self._h, out)
+        return {"density": out[0], "force": out[1], "sort": out[2], "sort_cells": out[3]}
+
+    def SetLaunchShapes(self, density: int = 0, force: int = 0, sort: int = 0, sort_cells: int = 0) -> None:
+        """Pin the launch shapes (0: compiled default), e.g. from LaunchShapes()
+        after an Autotune in an earlier run."""
+        shapes = (C.c_int * 4)(int(density), int(force), int(sort), int(sort_cells))
+        call("fl_set_launch_shapes", self._h, shapes)
 
     # -- timing ---------------------------------------------------------------
     def SetTiming(self, enable: bool) -> None:

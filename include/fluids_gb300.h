@@ -294,13 +294,26 @@ int fl_checkpoint_restore(fl_system *s, int slot);
 #define FL_CONSERVATION_VALUES 10
 int fl_conservation(fl_system *s, double *out);
 
-/* Block-shape autotuner (no counterpart in the reference): times the
- * density pass at 128..1024 threads per block and the force and sort passes
- * at three block sizes each, over `steps` steps from the current state
- * (restored afterwards), and keeps the fastest; chosen (nullable) gets the
- * threads per block of density, force, sort. Results are identical for
- * every block size. FL_ERR_STATE while a tape is recording. */
+/* Launch-shape autotuner (no counterpart in the reference): times the
+ * density pass at 128..1024 threads per block, the force and sort passes at
+ * three block sizes each and the cell sort at 2, 4 and 8 cells per warp,
+ * over `steps` steps from the current state (restored afterwards), and
+ * keeps the fastest; chosen (nullable, 3 ints) gets the threads per block
+ * of density, force, sort. Results are identical for every shape.
+ * FL_ERR_STATE while a tape is recording. */
 int fl_autotune(fl_system *s, int steps, int *chosen);
+
+/* The launch shapes in use (no counterpart in the reference): shapes[0..3]
+ * = threads per block of the density, force and sort passes, cell entries
+ * per warp of the cell sort. */
+int fl_launch_shapes(fl_system *s, int *shapes);
+
+/* Pin the launch shapes (no counterpart in the reference), e.g. ones an
+ * earlier fl_autotune chose: the same four values, 0 for the compiled
+ * default; density 32..1024, force 32..128, sort 32..256 threads per block
+ * (multiples of 32), 2, 4 or 8 cells per warp, else FL_ERR_ARG. Results are
+ * identical for every shape. */
+int fl_set_launch_shapes(fl_system *s, const int *shapes);
 
 /* Wait for the system stream; returns FL_ERR_DEVICE if a kernel raised the
  * device error word since the last fl_sync (bits in *dev_flags if non-NULL). */

@@ -528,13 +528,40 @@ def test_autotune_changes_no_result():
             s.RunSteps(5)
         before = a.GetBuffer(F.FPOS)
         chosen = a.Autotune(2)
-        assert chosen["density"] in (64, 128, 256) and chosen["force"] in (32, 64, 128)
-        assert chosen["sort"] in (64, 128, 256)
+        assert chosen["density"] in (128, 256, 512, 1024) and chosen["force"] in (32, 64, 128)
+        assert chosen["sort"] in (64, 128, 256) and chosen["sort_cells"] in (2, 4, 8)
         assert_bit_equal(a.GetBuffer(F.FPOS), before, "state kept")
         a.RunSteps(6)
         b.RunSteps(6)
         for k in (F.FPOS, F.FVEL, F.FVEVAL, F.FPRESS):
             assert_bit_equal(a.GetBuffer(k), b.GetBuffer(k), f"buffer {k}")
+
+
+@pytest.mark.parametrize("shapes", [(32, 32, 32, 2), (64, 64, 64, 8), (512, 96, 160, 4), (1024, 128, 256, 2)])
+def test_every_launch_shape_gives_the_same_steps(shapes):
+    """Threads per block (density, force, sort) and cells per warp of the
+    cell sort, pinned by fl_set_launch_shapes, against the compiled shapes:
+    3 fused steps bit for bit, crowded cells included."""
+    sc = scenes.dam_break(n=6000, seed=31)
+    p = sc.params
+    rng = np.random.default_rng(7)
+    pos = sc.pos.copy()
+    pick = rng.choice(pos.shape[0], size=400, replace=False)   # a cell above 128 points
+    c = np.array([p.gridMin[0] + 7.5 * 5.0, p.gridMin[1] + 5.5 * 5.0, p.gridMin[2] + 6.5 * 5.0], np.float32)
+    pos[pick] = c + rng.uniform(-2.0, 2.0, size=(400, 3)).astype(np.float32)
+    with make_system(p, pos, sc.vel, sc.veval, sc.clr) as a, make_system(p, pos, sc.vel, sc.veval, sc.clr) as b:
+        a.SetLaunchShapes(*shapes)
+        assert tuple(a.LaunchShapes().values()) == shapes
+        a.RunSteps(3)
+        b.RunSteps(3)
+        a.Sync(); b.Sync()
+        sa, sb = gpu_state(a), gpu_state(b)
+        for k in FIELDS:
+            assert_bit_equal(sa[k], sb[k], f"shapes {shapes} {k}")
+        with pytest.raises(F.FluidsError):
+            a.SetLaunchShapes(density=48)
+        with pytest.raises(F.FluidsError):
+            a.SetLaunchShapes(sort_cells=3)
 
 
 def _conservation64(p, pos, vel):
