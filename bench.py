@@ -403,10 +403,11 @@ def adjoint_measurements(args):
     ms_fwd = s.TimeSteps(T, graph=True) / T
     runs = {}
     every_k = max(1, min(args.adjoint_every, T))
-    for every in sorted({every_k, 1}, reverse=True):
+    variants = [(every_k, False), (every_k, True)] + ([(1, False)] if every_k != 1 else [])
+    for every, keep in variants:
         s.RestoreCheckpoint(0)
         f0 = _device_free()
-        s.TapeBegin(T, every)
+        s.TapeBegin(T, every, keep)
         f1 = _device_free()
         s.Sync()
         t0 = time.perf_counter()
@@ -418,7 +419,7 @@ def adjoint_measurements(args):
         gvel = outs[1].cpu().numpy()
         s.TapeEnd()
         gv = float(np.sqrt((gvel.astype(np.float64) ** 2).mean()))
-        runs[every] = {"every": every, "tape_bytes": (f0 - f1) if f0 is not None else None,
+        runs[(every, keep)] = {"every": every, "keep_lists": keep, "tape_bytes": (f0 - f1) if f0 is not None else None,
                        "taped_forward_ms_per_step": (t1 - t0) * 1e3 / T,
                        "backward_ms_per_step": ms_b / T, "ratio": ms_b / T / ms_fwd,
                        "loss": loss, "points_in_loss": counted,
@@ -446,8 +447,10 @@ def adjoint_measurements(args):
                     f"scene), {T} steps; loss vs the initial block shifted 0.3 box widths in +x",
         "steps": T, "forward_ms_per_step": ms_fwd,
         "system_bytes": (free_before - free_sys) if free_before is not None else None,
-        "checkpointed": runs[every_k], "every_step": runs[1],
-        "adjoint_forward_ratio": runs[every_k]["ratio"],
+        "checkpointed": runs[(every_k, False)], "checkpointed_kept_lists": runs[(every_k, True)],
+        "every_step": runs[(1, False)] if (1, False) in runs else runs[(every_k, False)],
+        "adjoint_forward_ratio": runs[(every_k, False)]["ratio"],
+        "adjoint_forward_ratio_kept_lists": runs[(every_k, True)]["ratio"],
         "gradient_vs_horizon": growth,
         "note": "gradients are exact (FP64-checked over 8 steps); over long horizons they overflow FP32 "
                 "because trajectories diverge exponentially (null = non-finite)"}

@@ -15,13 +15,14 @@
 // is piecewise constant and carries no derivative.
 //
 // The reverse pass of one step runs on the recomputed forward state of that
-// step (sorted X, V, E, rho, F and the grid) in four launches:
+// step (sorted X, V, E, rho, F and the grid) in five launches:
 //   k_adj_advance   per point: the advance's adjoint; dL/dF, dL/dV (written
 //                   through the permutation) and the direct parts of dL/dX, dL/dE
+//   k_adj_revwalk   per point s: its reverse pairs outside its own cell (the
+//                   points whose search block holds s), recorded in a list
 //   k_adj_force     per point s, over its own pairs (s the owner) and its
-//                   reverse pairs (the points whose search block holds s):
-//                   dL/dX, dL/dE, dL/drho and the parameter partials; records
-//                   the reverse pairs it finds
+//                   reverse pairs: dL/dX, dL/dE, dL/drho and the parameter
+//                   partials
 //   k_adj_density   per point, own and reverse pairs (both from lists): the
 //                   density's share of dL/dX, written through the permutation
 //   k_param_*       deterministic per-scene sums of the parameter partials
@@ -362,6 +363,28 @@ __device__ __forceinline__ void rev_begin(RevIter &it, const DevParams &P, uint3
     local_coords(P, active ? (int)gc - P.cell_base : 0, it.cx, it.cy, it.cz);
 }
 
+// Entry k of the reverse block: false when it leaves the scan range, is the
+// own cell, is pruned or is empty; else its slot range and word span.
+template <bool PRUNE>
+__device__ __forceinline__ bool rev_entry(RevIter &it, const DevParams &P, int k,
+                                          const uint32_t *__restrict__ off, const uint32_t *__restrict__ cnt) {
+    uint32_t up;
+    const int lc = reverse_cell(P, it.cx, it.cy, it.cz, k, up);
+    if (lc < 0) return false;
+    const int R = P.gridSrch, sh = R - 2;
+    if (k % R == sh && (k / R) % R == sh && k / (R * R) == sh) return false;   // own cell
+    if (PRUNE && (it.code & up) != up) return false;
+    const int cell = P.cell_base + lc;
+    const uint32_t m = cnt[cell];
+    if (m == 0) return false;
+    it.up = up;
+    it.lo = off[cell];
+    it.hi = it.lo + m;
+    it.w = it.lo >> 5;
+    it.w_last = (it.hi - 1) >> 5;
+    return true;
+}
+
 template <bool PRUNE>
 __device__ __forceinline__ bool rev_next(RevIter &it, const DevParams &P, const uint32_t *__restrict__ off,
                                          const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ lobits,
@@ -375,24 +398,11 @@ __device__ __forceinline__ bool rev_next(RevIter &it, const DevParams &P, const 
         // next cell of the reverse block
         bool found = false;
         while (it.k < P.gridAdjCnt) {
-            uint32_t up;
-            const int k = it.k++;
-            const int lc = reverse_cell(P, it.cx, it.cy, it.cz, k, up);
-            if (lc < 0) continue;
-            const int R = P.gridSrch, sh = R - 2;
-            if (k % R == sh && (k / R) % R == sh && k / (R * R) == sh) continue;   // own cell
-            if (PRUNE && (it.code & up) != up) continue;
-            const int cell = P.cell_base + lc;
-            const uint32_t m = cnt[cell];
-            if (m == 0) continue;
-            it.up = up;
-            it.lo = off[cell];
-            it.hi = it.lo + m;
-            it.w = it.lo >> 5;
-            it.w_last = (it.hi - 1) >> 5;
-            it.bits = rev_word<PRUNE>(it, P, lobits, it.w);
-            found = true;
-            break;
+            if (rev_entry<PRUNE>(it, P, it.k++, off, cnt)) {
+                it.bits = rev_word<PRUNE>(it, P, lobits, it.w);
+                found = true;
+                break;
+            }
         }
         if (!found) return false;
     }
@@ -401,18 +411,54 @@ __device__ __forceinline__ bool rev_next(RevIter &it, const DevParams &P, const 
     return true;
 }
 
-// Reverse of computeForce for point s (all threads of the block call it,
-// with grouping_smem(blockDim, kBandKeys) bytes of dynamic shared memory).
-// First each lane walks its reverse block (the points whose search block
-// holds s, outside s's own cell) and records the reverse pairs it finds in
-// revlist; then the warp evaluates, in step, every lane's own pairs (the
-// density pass's list; those in the own cell are reverse pairs too) and
-// its recorded reverse pairs, so the long pair arithmetic runs with the
-// lanes busy. A lane whose own or reverse list overflowed evaluates those
-// pairs while walking them again. Writes the complete dL/dE through the
+
+// The reverse pairs of point s outside its own cell -- the points q whose
+// search block holds s and that pass 0 < d^2 < rd2 -- recorded in revlist
+// (up to hcap, in ascending cell-entry and slot order) with their count in
+// revcnt, for the force and density adjoints; a count of hcap + 1 means
+// the list overflowed (the walk stops there). The block's threads take its
+// points grouped by upper-band bits, which decide the cells of the reverse
+// block a point visits (all threads of the block call it, with
+// grouping_smem(blockDim, kBandKeys) bytes of dynamic shared memory).
+template <bool PRUNE>
+__global__ void __launch_bounds__(kThreads)
+k_adj_revwalk(const __grid_constant__ DevParams P0, const SceneTab T, int n, const float4 *__restrict__ pos,
+              const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ off,
+              const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
+              uint32_t *__restrict__ revlist, uint32_t *__restrict__ revcnt) {
+    extern __shared__ uint32_t s_dyn[];
+    const int s = PRUNE ? band_grouped_slot(n, pos, gcell, 0, s_dyn) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (s >= n) return;
+    const DevParams &P = scene_params(P0, T, s);
+    const uint32_t gc = gcell[s];
+    uint32_t nrev = 0;
+    if (gc != kUndef) {
+        const float4 p4 = pos[s];
+        const uint32_t hcap = (uint32_t)P.hcap;
+        RevIter it;
+        rev_begin<PRUNE>(it, P, gc, __float_as_uint(p4.w), true);
+        uint32_t q;
+        while (rev_next<PRUNE>(it, P, off, cnt, upbits + 3 * (size_t)P.upwords, q)) {
+            const float4 qp = pos[q];
+            const float dsq = dsq_rn(qp.x - p4.x, qp.y - p4.y, qp.z - p4.z);
+            if (dsq < P.rd2 && dsq > 0.0f) {
+                if (nrev == hcap) { nrev++; break; }   // overflowed: the consumers walk again
+                revlist[list_at(P, s, nrev)] = q;
+                nrev++;
+            }
+        }
+    }
+    revcnt[s] = nrev;
+}
+
+// Reverse of computeForce for point s (all 32 lanes of a warp call it):
+// the warp evaluates, in step, every lane's own pairs (the density pass's
+// list; those in the own cell are reverse pairs too) and its reverse pairs
+// (k_adj_revwalk's list), so the long pair arithmetic runs with the lanes
+// busy. A lane whose own or reverse list overflowed evaluates those pairs
+// while walking them again. Writes the complete dL/dE through the
 // permutation, accumulates dL/dX into xa, stores dL/drho and the parameter
-// partials (dL/dvisc, dL/drest_density, dL/dIntStiff) of its own pairs;
-// revlist / revcnt stay for the density adjoint.
+// partials (dL/dvisc, dL/drest_density, dL/dIntStiff) of its own pairs.
 template <bool PRUNE>
 __global__ void __launch_bounds__(kAdjThreads, 8)
 k_adj_force(const __grid_constant__ DevParams P0, const SceneTab T, int n,
@@ -422,11 +468,8 @@ k_adj_force(const __grid_constant__ DevParams P0, const SceneTab T, int n,
             const uint32_t *__restrict__ hitcnt, const uint32_t *__restrict__ src,
             const float4 *__restrict__ fb, float4 *__restrict__ xa, const float4 *__restrict__ ea,
             float *__restrict__ rb, float4 *__restrict__ pc, float4 *__restrict__ e_out,
-            uint32_t *__restrict__ revlist, uint32_t *__restrict__ revcnt) {
-    // pruned: the lanes of a warp take points with the same upper-band bits,
-    // which decide the cells of the reverse block a point visits
-    extern __shared__ uint32_t s_dyn[];
-    const int s = PRUNE ? band_grouped_slot(n, pos, gcell, 0, s_dyn) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
+            const uint32_t *__restrict__ revlist, const uint32_t *__restrict__ revcnt) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const DevParams &P = scene_params(P0, T, s < n ? s : 0);
     const uint32_t gc = (s < n) ? gcell[s] : kUndef;
     const bool active = gc != kUndef;
@@ -450,22 +493,7 @@ k_adj_force(const __grid_constant__ DevParams P0, const SceneTab T, int n,
     }
     const uint32_t hcap = (uint32_t)P.hcap;
     const uint32_t *lobits = upbits + 3 * (size_t)P.upwords;
-
-    // reverse pairs outside the own cell -> revlist
-    uint32_t nrev = 0;
-    if (active) {
-        RevIter it;
-        rev_begin<PRUNE>(it, P, gc, my_code, true);
-        uint32_t q;
-        while (rev_next<PRUNE>(it, P, off, cnt, lobits, q)) {
-            const float4 qp = pos[q];
-            const float dsq = dsq_rn(qp.x - X.x, qp.y - X.y, qp.z - X.z);
-            if (dsq < P.rd2 && dsq > 0.0f) {
-                if (nrev < hcap) revlist[list_at(P, s, nrev)] = q;
-                nrev++;
-            }
-        }
-    }
+    const uint32_t nrev = active ? revcnt[s] : 0u;
 
     // own pairs (own cell: both roles) and reverse pairs from the lists
     auto own_entry = [&](uint32_t j) { return (j >= c_lo && j < c_hi) ? (j | kBothFlag) : j; };
@@ -509,7 +537,6 @@ k_adj_force(const __grid_constant__ DevParams P0, const SceneTab T, int n,
 
     if (s >= n) return;
     const uint32_t dst = src[s];
-    revcnt[s] = nrev;
     if (!active) {
         e_out[dst] = ea[s];
         rb[s] = 0.0f;
@@ -527,7 +554,7 @@ k_adj_force(const __grid_constant__ DevParams P0, const SceneTab T, int n,
 // w = (rd2 - |D|^2) d2 gives dL/dD = -6 d2 w^2 (m poly6 dL/drho_o) D for
 // every pair of owner o. Own pairs from the density pass's list (those in
 // the point's own cell are reverse pairs too), reverse pairs in the other
-// cells from the list k_adj_force recorded (a walk where either list
+// cells from the list k_adj_revwalk recorded (a walk where either list
 // overflowed); the finished dL/dX goes through the permutation.
 template <bool PRUNE>
 __global__ void __launch_bounds__(kAdjThreads)
@@ -712,8 +739,13 @@ int fl_launch_adj_force(fl_system *s, const float2 *rr, const float4 *fb, float4
     if (s->max_points > (int)kSlotMask)
         return fl_fail(FL_ERR_CAPACITY, "adjoint: %d points (at most %u)", s->max_points, kSlotMask);
     const bool pr = adj_prune(s);
+    auto walk = pr ? k_adj_revwalk<true> : k_adj_revwalk<false>;
+    walk<<<blocks_for(s->n, kThreads), kThreads, grouping_smem(kThreads, kBandKeys), s->stream>>>(
+        s->D, fl_scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt,
+        s->upbits, revlist, revcnt);
+    FL_LAUNCH_CHECK("adj_revwalk");
     auto kern = pr ? k_adj_force<true> : k_adj_force<false>;
-    kern<<<blocks_for(s->n, kAdjThreads), kAdjThreads, grouping_smem(kAdjThreads, kBandKeys), s->stream>>>(
+    kern<<<blocks_for(s->n, kAdjThreads), kAdjThreads, 0, s->stream>>>(
         s->D, fl_scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->f[F_VEVAL].cur<float4>(),
         rr, s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt, s->upbits, s->hitlist,
         s->hitcnt, s->src, fb, xa, ea, rb, pc, e_out, revlist, revcnt);

@@ -86,10 +86,10 @@ def test_backward_matches_fp64_adjoint_moving_wall_slope_and_crowding():
     p = sc.params
     p.bound_slope = 0.05
     st, t = stirred_state(sc, 0, seed=13)
-    # a crowded cell: 80 points within one smoothing radius, so the pair
-    # lists overflow and both passes take the walk path for them
+    # a crowd of 1,200 points within one smoothing radius: their pair lists
+    # (128 entries) overflow and both passes walk for them
     rng = np.random.default_rng(14)
-    st.pos[:80] = st.pos[100] + rng.uniform(-0.6, 0.6, (80, 3)).astype(np.float32)
+    st.pos[:1200] = st.pos[1300] + rng.uniform(-0.6, 0.6, (1200, 3)).astype(np.float32)
     s, states = _gpu_record(sc, st, 1.7, 3, 1, params=p)
     w = rng.standard_normal((3, st.n, 3)).astype(np.float32)
     with s:
