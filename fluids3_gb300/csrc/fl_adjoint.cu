@@ -412,6 +412,14 @@ __device__ __forceinline__ bool rev_next(RevIter &it, const DevParams &P, const 
 }
 
 
+// Points whose own or reverse pair list overflowed, appended by k_adj_force
+// and walked by k_adj_crowd_force (below).
+struct CrowdList {
+    uint32_t *pts;
+    uint32_t *count;   // listed points (cleared before each reverse step)
+    uint32_t cap;
+};
+
 // The reverse pairs of point s outside its own cell -- the points q whose
 // search block holds s and that pass 0 < d^2 < rd2 -- recorded in revlist
 // (up to hcap, in ascending cell-entry and slot order) with their count in
@@ -455,10 +463,11 @@ k_adj_revwalk(const __grid_constant__ DevParams P0, const SceneTab T, int n, con
 // the warp evaluates, in step, every lane's own pairs (the density pass's
 // list; those in the own cell are reverse pairs too) and its reverse pairs
 // (k_adj_revwalk's list), so the long pair arithmetic runs with the lanes
-// busy. A lane whose own or reverse list overflowed evaluates those pairs
-// while walking them again. Writes the complete dL/dE through the
-// permutation, accumulates dL/dX into xa, stores dL/drho and the parameter
-// partials (dL/dvisc, dL/drest_density, dL/dIntStiff) of its own pairs.
+// busy. A point whose own or reverse list overflowed is appended to the
+// crowd list instead, and k_adj_crowd_force adds those pairs. Writes dL/dE
+// through the permutation, accumulates dL/dX into xa, stores dL/drho and
+// the parameter partials (dL/dvisc, dL/drest_density, dL/dIntStiff) of its
+// own pairs.
 template <bool PRUNE>
 __global__ void __launch_bounds__(kAdjThreads, 8)
 k_adj_force(const __grid_constant__ DevParams P0, const SceneTab T, int n,
@@ -468,7 +477,7 @@ k_adj_force(const __grid_constant__ DevParams P0, const SceneTab T, int n,
             const uint32_t *__restrict__ hitcnt, const uint32_t *__restrict__ src,
             const float4 *__restrict__ fb, float4 *__restrict__ xa, const float4 *__restrict__ ea,
             float *__restrict__ rb, float4 *__restrict__ pc, float4 *__restrict__ e_out,
-            const uint32_t *__restrict__ revlist, const uint32_t *__restrict__ revcnt) {
+            const uint32_t *__restrict__ revlist, const uint32_t *__restrict__ revcnt, const CrowdList crowd) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const DevParams &P = scene_params(P0, T, s < n ? s : 0);
     const uint32_t gc = (s < n) ? gcell[s] : kUndef;
@@ -510,29 +519,10 @@ k_adj_force(const __grid_constant__ DevParams P0, const SceneTab T, int n,
         }
     }
 
-    // overflowed lists: walk again, evaluating as found
-    if (active && nh > hcap) {
-        const int base = (int)gc - P.nadj;
-        for (int c = 0; c < P.gridAdjCnt; c++) {
-            CandIter it;
-            cand_begin<PRUNE>(it, P, c, base + P.adj[c], my_code, true, off, cnt, upbits);
-            uint32_t j;
-            while (cand_next<PRUNE>(it, P, upbits, j)) {
-                const float4 q = pos[j];
-                const float dsq = dsq_rn(X.x - q.x, X.y - q.y, X.z - q.z);
-                if (dsq < P.rd2 && dsq > 0.0f) adj_pair(P, acc, X, Ev, rs, fs, irs, own_entry(j), pos, veval, rr, fb);
-            }
-        }
-    }
-    if (active && nrev > hcap) {
-        RevIter it;
-        rev_begin<PRUNE>(it, P, gc, my_code, true);
-        uint32_t q;
-        while (rev_next<PRUNE>(it, P, off, cnt, lobits, q)) {
-            const float4 qp = pos[q];
-            const float dsq = dsq_rn(qp.x - X.x, qp.y - X.y, qp.z - X.z);
-            if (dsq < P.rd2 && dsq > 0.0f) adj_pair(P, acc, X, Ev, rs, fs, irs, q | kRevFlag, pos, veval, rr, fb);
-        }
+    // overflowed lists: the point's walks go to the crowd kernels
+    if (active && (nh > hcap || nrev > hcap)) {
+        const uint32_t slot = atomicAdd(crowd.count, 1u);
+        if (slot < crowd.cap) crowd.pts[slot] = (uint32_t)s;
     }
 
     if (s >= n) return;
@@ -637,6 +627,136 @@ k_adj_density(const __grid_constant__ DevParams P0, const SceneTab T, int n,
     x_out[dst] = make_float4(x0.x + xacc.x, x0.y + xacc.y, x0.z + xacc.z, 0.f);
 }
 
+// ---------------------------------------------------------------------------
+// Crowded points. A point whose own or reverse pair list overflowed (a
+// collapsing scene crowds hundreds or thousands of points into a cell) is
+// left out of k_adj_force's list drain and appended to the crowd list;
+// k_adj_crowd_force then gives each listed point a whole block, so its
+// pairs -- the costliest arithmetic of the reverse step -- spread over the
+// GPU instead of one thread walking them all. (The density adjoint's pair
+// terms are light; its overflowed points walk per thread.) The candidates of each walked cell are cut
+// into 32-slot chunks counted from the cell's first slot; chunk g of the
+// point's walk goes to warp g % warps and lane l of that warp takes slot
+// l of the chunk when the band flags keep it. The lanes' sums are added in
+// a fixed order, so a point's result is reproducible, and the same alone or
+// in a batch (chunks do not depend on where a scene's slots start).
+constexpr int kCrowdThreads = 256;
+
+template <bool PRUNE, class F>
+__device__ __forceinline__ void crowd_chunks(const DevParams &P, uint32_t gc, uint32_t code, bool own, bool rev,
+                                             const uint32_t *__restrict__ off, const uint32_t *__restrict__ cnt,
+                                             const uint32_t *__restrict__ upbits, F &&f) {
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    uint32_t g = 0;   // chunks of the walk so far (the same on every thread)
+    auto cell = [&](uint32_t lo, uint32_t hi, uint32_t axes, const uint32_t *rows, bool is_rev) {
+        const uint32_t nq = (hi - lo + 31) >> 5;
+        for (uint32_t q = (warp + nwarps - g % nwarps) % nwarps; q < nq; q += nwarps) {
+            const uint32_t j = lo + 32 * q + lane;
+            if (j >= hi) continue;
+            bool keep = true;
+            if (PRUNE && axes) {
+                const uint32_t w = j >> 5, b = 1u << (j & 31u);
+                if ((axes & 1u) && !(rows[w] & b)) keep = false;
+                if ((axes & 2u) && !(rows[(size_t)P.upwords + w] & b)) keep = false;
+                if ((axes & 4u) && !(rows[2 * (size_t)P.upwords + w] & b)) keep = false;
+            }
+            if (keep) f(j, is_rev);
+        }
+        g += nq;
+    };
+    if (own) {   // the search block, as cand_begin / cand_word prune it
+        const int base = (int)gc - P.nadj;
+        for (int c = 0; c < P.gridAdjCnt; c++) {
+            CandIter it;
+            cand_begin<PRUNE>(it, P, c, base + P.adj[c], code, true, off, cnt, upbits);
+            if (it.lo < it.hi) cell(it.lo, it.hi, it.U, upbits, false);
+        }
+    }
+    if (rev) {   // the reverse block outside the own cell, as rev_entry / rev_word prune it
+        RevIter it;
+        rev_begin<PRUNE>(it, P, gc, code, true);
+        for (int k = 0; k < P.gridAdjCnt; k++)
+            if (rev_entry<PRUNE>(it, P, k, off, cnt)) cell(it.lo, it.hi, it.up, upbits + 3 * (size_t)P.upwords, true);
+    }
+}
+
+// Sums v[0..K) over the block into s_red (thread 0 reads the totals): each
+// warp by a fixed shuffle tree, then the warps in order.
+template <int K>
+__device__ __forceinline__ void block_sum(float (&v)[K], float (*s_red)[K]) {
+#pragma unroll
+    for (int k = 0; k < K; k++)
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], d);
+    if (lane_id() == 0)
+#pragma unroll
+        for (int k = 0; k < K; k++) s_red[threadIdx.x >> 5][k] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            float t = s_red[0][k];
+            for (uint32_t w = 1; w < (blockDim.x >> 5); w++) t += s_red[w][k];
+            v[k] = t;
+        }
+    }
+}
+
+// The force adjoint's walked pairs of each crowded point, added to what
+// k_adj_force wrote for it (dL/dX, dL/dE through the permutation, dL/drho,
+// the parameter partials).
+template <bool PRUNE>
+__global__ void __launch_bounds__(kCrowdThreads)
+k_adj_crowd_force(const __grid_constant__ DevParams P0, const SceneTab T, const float4 *__restrict__ pos,
+                  const float4 *__restrict__ veval, const float2 *__restrict__ rr,
+                  const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ off,
+                  const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
+                  const uint32_t *__restrict__ hitcnt, const uint32_t *__restrict__ revcnt,
+                  const uint32_t *__restrict__ src, const float4 *__restrict__ fb, float4 *__restrict__ xa,
+                  float4 *__restrict__ e_out, float *__restrict__ rb, float4 *__restrict__ pc, const CrowdList L) {
+    __shared__ float s_red[kCrowdThreads / 32][10];
+    __shared__ uint32_t s_nlist;
+    if (threadIdx.x == 0) s_nlist = min(*(volatile uint32_t *)L.count, L.cap);
+    __syncthreads();
+    const uint32_t nlist = s_nlist;
+    for (uint32_t b = blockIdx.x; b < nlist; b += gridDim.x) {
+        const int s = (int)L.pts[b];
+        const DevParams &P = scene_params(P0, T, s);
+        const uint32_t gc = gcell[s];
+        const float4 p4 = pos[s];
+        const float3 X = xyz(p4), Ev = xyz(veval[s]), fs = xyz(fb[s]);
+        const float2 r2 = rr[s];
+        const uint32_t c_lo = off[gc], c_hi = c_lo + cnt[gc], hcap = (uint32_t)P.hcap;
+        AdjAcc part;
+        part.x = part.e = make_float3(0.f, 0.f, 0.f);
+        part.r = part.gv = part.gr = part.gk = 0.0f;
+        crowd_chunks<PRUNE>(P, gc, __float_as_uint(p4.w), hitcnt[s] > hcap, revcnt[s] > hcap, off, cnt, upbits,
+                            [&](uint32_t j, bool is_rev) {
+            const float4 q = pos[j];
+            if (!is_rev) {
+                const float dsq = dsq_rn(X.x - q.x, X.y - q.y, X.z - q.z);
+                if (dsq < P.rd2 && dsq > 0.0f)
+                    adj_pair(P, part, X, Ev, r2.x, fs, r2.y, (j >= c_lo && j < c_hi) ? (j | kBothFlag) : j, pos,
+                             veval, rr, fb);
+            } else {
+                const float dsq = dsq_rn(q.x - X.x, q.y - X.y, q.z - X.z);
+                if (dsq < P.rd2 && dsq > 0.0f) adj_pair(P, part, X, Ev, r2.x, fs, r2.y, j | kRevFlag, pos, veval, rr, fb);
+            }
+        });
+        float v[10] = {part.x.x, part.x.y, part.x.z, part.e.x, part.e.y, part.e.z, part.r, part.gv, part.gr, part.gk};
+        block_sum<10>(v, s_red);
+        if (threadIdx.x == 0) {
+            const uint32_t dst = src[s];
+            const float4 x0 = xa[s], e0 = e_out[dst], c0 = pc[s];
+            xa[s] = make_float4(x0.x + v[0], x0.y + v[1], x0.z + v[2], 0.f);
+            e_out[dst] = make_float4(e0.x + v[3], e0.y + v[4], e0.z + v[5], 0.f);
+            rb[s] += v[6];
+            pc[s] = make_float4(c0.x + v[7], c0.y + v[8], c0.z + v[9], 0.f);
+        }
+        __syncthreads();
+    }
+}
+
 // Parameter partials summed per scene in double, in a fixed order: block
 // (chunk, scene) sums its chunk, then one thread per scene adds the chunk
 // sums in chunk order onto the running totals.
@@ -733,8 +853,11 @@ int fl_launch_adj_advance(fl_system *s, const float *time_ptr, const float4 *for
     return FL_OK;
 }
 
+static int crowd_grid(const fl_system *s) { return 4 * s->num_sms; }
+
 int fl_launch_adj_force(fl_system *s, const float2 *rr, const float4 *fb, float4 *xa, const float4 *ea, float *rb,
-                        float4 *pc, float4 *e_out, uint32_t *revlist, uint32_t *revcnt) {
+                        float4 *pc, float4 *e_out, uint32_t *revlist, uint32_t *revcnt, uint32_t *crowd,
+                        uint32_t *crowd_count) {
     if (s->n == 0) return FL_OK;
     if (s->max_points > (int)kSlotMask)
         return fl_fail(FL_ERR_CAPACITY, "adjoint: %d points (at most %u)", s->max_points, kSlotMask);
@@ -748,8 +871,14 @@ int fl_launch_adj_force(fl_system *s, const float2 *rr, const float4 *fb, float4
     kern<<<blocks_for(s->n, kAdjThreads), kAdjThreads, 0, s->stream>>>(
         s->D, fl_scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->f[F_VEVAL].cur<float4>(),
         rr, s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt, s->upbits, s->hitlist,
-        s->hitcnt, s->src, fb, xa, ea, rb, pc, e_out, revlist, revcnt);
+        s->hitcnt, s->src, fb, xa, ea, rb, pc, e_out, revlist, revcnt, CrowdList{crowd, crowd_count, (uint32_t)s->n});
     FL_LAUNCH_CHECK("adj_force");
+    auto crowd_kern = pr ? k_adj_crowd_force<true> : k_adj_crowd_force<false>;
+    crowd_kern<<<crowd_grid(s), kCrowdThreads, 0, s->stream>>>(
+        s->D, fl_scene_tab(s), s->f[F_POS].cur<float4>(), s->f[F_VEVAL].cur<float4>(), rr,
+        s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt, s->upbits, s->hitcnt, revcnt, s->src, fb, xa, e_out, rb, pc,
+        CrowdList{crowd, crowd_count, (uint32_t)s->n});
+    FL_LAUNCH_CHECK("adj_crowd_force");
     return FL_OK;
 }
 

@@ -218,8 +218,11 @@ void fl_tape_free(fl_system *s);
 int fl_launch_adj_advance(fl_system *s, const float *time_ptr, const float4 *force, const float4 *xo_b,
                           const float4 *vo_b, const float4 *eo_b, float4 *xa, float4 *ea, float4 *fb, float4 *v_out,
                           float2 *rr);
+// crowd / crowd_count: the list of points whose pair lists overflowed
+// (capacity n; the count starts at zero)
 int fl_launch_adj_force(fl_system *s, const float2 *rr, const float4 *fb, float4 *xa, const float4 *ea, float *rb,
-                        float4 *pc, float4 *e_out, uint32_t *revlist, uint32_t *revcnt);
+                        float4 *pc, float4 *e_out, uint32_t *revlist, uint32_t *revcnt, uint32_t *crowd,
+                        uint32_t *crowd_count);
 int fl_launch_adj_density(fl_system *s, const uint32_t *revlist, const uint32_t *revcnt, const float *rb,
                           const float4 *xa, float4 *x_out);
 int fl_param_chunks(int max_scene_points);
