@@ -202,10 +202,18 @@ def test_backward_is_linear_in_the_cotangent():
     assert np.all(np.abs(g12[3] - want) <= 1e-4 * np.abs(want) + 1e-9)
 
 
-def test_batched_backward_equals_each_scene_alone():
+@pytest.mark.parametrize("crowd", [False, True])
+def test_batched_backward_equals_each_scene_alone(crowd):
+    """Gradients of each scene in a batch equal the scene's alone, bit for
+    bit; with crowd, 300 points of each scene cluster so their pair lists
+    overflow and the crowd kernel walks them (scene slot bases are not
+    multiples of 32 here)."""
     scs = scenes.batch_scenes(nscenes=3, nmin=1500, nmax=4000, seed=23)
     for k, sc in enumerate(scs):
         sc.vel[:] = np.float32(0.1 * (k + 1))
+        if crowd:
+            c = sc.pos[sc.n // 2].copy()
+            sc.pos[:300] = c + np.random.default_rng(40 + k).uniform(-0.5, 0.5, (300, 3)).astype(np.float32)
     rng = np.random.default_rng(24)
     ws = [rng.standard_normal((3, sc.n, 3)).astype(np.float32) for sc in scs]
     alone = []
