@@ -335,7 +335,7 @@ __device__ __forceinline__ void local_coords(const DevParams &P, int lc, int &cx
 // flag word.
 struct RevIter {
     int k, cx, cy, cz;
-    uint32_t code, up;
+    uint32_t gc, code, up;
     uint32_t w, w_last, lo, hi, bits;
 };
 
@@ -356,6 +356,7 @@ __device__ __forceinline__ uint32_t rev_word(const RevIter &it, const DevParams 
 template <bool PRUNE>
 __device__ __forceinline__ void rev_begin(RevIter &it, const DevParams &P, uint32_t gc, uint32_t code, bool active) {
     it.k = active ? 0 : P.gridAdjCnt;
+    it.gc = gc;
     it.code = code;
     it.up = 0;
     it.w = it.w_last = it.lo = it.hi = 0;
@@ -369,12 +370,23 @@ template <bool PRUNE>
 __device__ __forceinline__ bool rev_entry(RevIter &it, const DevParams &P, int k,
                                           const uint32_t *__restrict__ off, const uint32_t *__restrict__ cnt) {
     uint32_t up;
-    const int lc = reverse_cell(P, it.cx, it.cy, it.cz, k, up);
-    if (lc < 0) return false;
-    const int R = P.gridSrch, sh = R - 2;
-    if (k % R == sh && (k / R) % R == sh && k / (R * R) == sh) return false;   // own cell
-    if (PRUNE && (it.code & up) != up) return false;
-    const int cell = P.cell_base + lc;
+    int cell;
+    if (PRUNE) {
+        // gridSrch 2: the block is cells c .. c+1 per axis, entry k at offset
+        // (k & 1, k >> 2, (k >> 1) & 1) in x, y, z; entry 0 is the own cell
+        const int x = k & 1, z = (k >> 1) & 1, y = k >> 2;
+        if (k == 0) return false;
+        if (it.cx + x > P.gridScanMax.x || it.cy + y > P.gridScanMax.y || it.cz + z > P.gridScanMax.z) return false;
+        up = (uint32_t)(x | (y << 1) | (z << 2));
+        if ((it.code & up) != up) return false;
+        cell = (int)it.gc + x + P.gridRes.x * (z + P.gridRes.z * y);
+    } else {
+        const int lc = reverse_cell(P, it.cx, it.cy, it.cz, k, up);
+        if (lc < 0) return false;
+        const int R = P.gridSrch, sh = R - 2;
+        if (k % R == sh && (k / R) % R == sh && k / (R * R) == sh) return false;   // own cell
+        cell = P.cell_base + lc;
+    }
     const uint32_t m = cnt[cell];
     if (m == 0) return false;
     it.up = up;
