@@ -64,7 +64,7 @@ ALGO_BYTES = {
     "density": 16,         # R pos 12, W density 4
     "force_advance": 128,  # force 40 (R pos, veval, density; W F) + advance 88
 }
-KERNELS_PER_STEP = 7   # insert, scan, scatter, cell sort, gather, density, force+advance
+KERNELS_PER_STEP = 8   # insert, scan, scatter, cell sort, crowded-cell sort, gather, density, force+advance
 
 
 def parse():

@@ -833,8 +833,8 @@ static int record(fl_system *s, TimingState *t, int k) {
 
 static int run_step(fl_system *s, TimingState *t) {
     // InsertParticles, PrefixSumCells, CountingSortFull, ComputePressure,
-    // ComputeForce + Advance (cpp:507-515) as seven launches (the sort is a
-    // cell sort of the point indices and a gather).
+    // ComputeForce + Advance (cpp:507-515) as eight launches (the sort is a
+    // cell sort of the point indices, one for crowded cells, and a gather).
     const bool taped = fl_tape_recording(s) != 0;
     if (taped) FL_TRY(fl_tape_pre_step(s));
     FL_TRY(record(s, t, 0));
