@@ -68,8 +68,8 @@ k_scatter_index(int n, const uint32_t *__restrict__ cell_pre, const uint32_t *__
 // segment of src at a time, ascending, so slot off[c]+k holds the k-th lowest
 // index in cell c -- the order a serial insert (gndx = cnt[cell]++) yields.
 // Segments up to 128 points are sorted in registers by a warp bitonic
-// network (K keys per lane, element e = lane*K + r); larger ones take a
-// chunked rank path (sort_segment_dense).
+// network (K keys per lane, element e = lane*K + r); larger ones by a block
+// each (k_sort_big).
 template <int K>
 __device__ __forceinline__ void warp_bitonic(uint32_t (&v)[K]) {
     const unsigned lane = lane_id();
