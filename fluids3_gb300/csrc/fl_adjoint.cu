@@ -455,16 +455,26 @@ k_adj_revwalk(const __grid_constant__ DevParams P0, const SceneTab T, int n, con
     if (gc != kUndef) {
         const float4 p4 = pos[s];
         const uint32_t hcap = (uint32_t)P.hcap;
+        const uint32_t *lobits = upbits + 3 * (size_t)P.upwords;
         RevIter it;
         rev_begin<PRUNE>(it, P, gc, __float_as_uint(p4.w), true);
-        uint32_t q;
-        while (rev_next<PRUNE>(it, P, off, cnt, upbits + 3 * (size_t)P.upwords, q)) {
-            const float4 qp = pos[q];
-            const float dsq = dsq_rn(qp.x - p4.x, qp.y - p4.y, qp.z - p4.z);
-            if (dsq < P.rd2 && dsq > 0.0f) {
-                if (nrev == hcap) { nrev++; break; }   // overflowed: the consumers walk again
-                revlist[list_at(P, s, nrev)] = q;
-                nrev++;
+        // one cell of the reverse block at a time (the lanes of a warp meet at
+        // each cell's end), 32 slots per flag word, ascending
+        for (int k = 0; k < P.gridAdjCnt && nrev <= hcap; k++) {
+            if (!rev_entry<PRUNE>(it, P, k, off, cnt)) continue;
+            for (uint32_t w = it.lo >> 5; w <= it.w_last && nrev <= hcap; w++) {
+                uint32_t bits = rev_word<PRUNE>(it, P, lobits, w);
+                while (bits) {
+                    const uint32_t q = (w << 5) + (uint32_t)(__ffs(bits) - 1);
+                    bits &= bits - 1u;
+                    const float4 qp = pos[q];
+                    const float dsq = dsq_rn(qp.x - p4.x, qp.y - p4.y, qp.z - p4.z);
+                    if (dsq < P.rd2 && dsq > 0.0f) {
+                        if (nrev == hcap) { nrev++; break; }   // overflowed: the consumers walk again
+                        revlist[list_at(P, s, nrev)] = q;
+                        nrev++;
+                    }
+                }
             }
         }
     }

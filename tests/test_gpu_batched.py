@@ -69,6 +69,30 @@ def test_batch_matches_each_scene_alone(graph):
                          f"scene {k} gridoff")
 
 
+def test_batch_with_crowded_cells_matches_each_scene_alone():
+    """Crowded cells (above 128 points, sorted by a block each) in two of the
+    scenes: the batch still steps each scene as it steps alone."""
+    scs = small_batch()
+    for k in (0, 2):
+        sc = scs[k]
+        m = min(600, sc.n // 2)
+        c = sc.pos[sc.n // 3].copy()
+        sc.pos[:m] = c + np.random.default_rng(60 + k).uniform(-1.5, 1.5, (m, 3)).astype(np.float32)
+    cat = scenes.concat(scs)
+    with F.FluidSystem.batch([sc.params for sc in scs], [sc.n for sc in scs]) as b:
+        b.SetParticles(cat["pos"], cat["vel"], cat["veval"], clr=cat["clr"])
+        b.RunSteps(4)
+        b.Sync()
+        st = b.state()
+        assert st["gridcnt"].max() > 128
+        infos = [b.SceneInfo(k) for k in range(len(scs))]
+    for k, sc in enumerate(scs):
+        want = plain_state(sc, 4, True)
+        got = per_scene(st, infos[k])
+        for f in FIELDS:
+            assert_bit_equal(got[f], want[f], f"scene {k} {f}")
+
+
 def test_batch_phase_api_matches_oracle():
     scs = small_batch(k=5, seed=11)
     cat = scenes.concat(scs)
