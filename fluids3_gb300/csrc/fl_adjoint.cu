@@ -425,7 +425,7 @@ __device__ __forceinline__ bool rev_next(RevIter &it, const DevParams &P, const 
 
 
 // Points whose own or reverse pair list overflowed, appended by k_adj_force
-// and walked by k_adj_crowd_force (below).
+// and walked by the crowd kernels (below).
 struct CrowdList {
     uint32_t *pts;
     uint32_t *count;   // listed points (cleared before each reverse step)
@@ -566,8 +566,13 @@ k_adj_force(const __grid_constant__ DevParams P0, const SceneTab T, int n,
 // w = (rd2 - |D|^2) d2 gives dL/dD = -6 d2 w^2 (m poly6 dL/drho_o) D for
 // every pair of owner o. Own pairs from the density pass's list (those in
 // the point's own cell are reverse pairs too), reverse pairs in the other
-// cells from the list k_adj_revwalk recorded (a walk where either list
-// overflowed); the finished dL/dX goes through the permutation.
+// cells from the list k_adj_revwalk recorded; the finished dL/dX goes
+// through the permutation. With walk_overflow off (as fl_backward launches
+// it) a point whose list overflowed is left to k_adj_crowd_density, which
+// spreads its pairs over a block; on, the point walks them itself. (The
+// per-thread walk is kept compiled in: without it this kernel's list loops
+// were given fewer registers and more resident warps, and ran 40% slower
+// on the wave tank.)
 template <bool PRUNE>
 __global__ void __launch_bounds__(kAdjThreads)
 k_adj_density(const __grid_constant__ DevParams P0, const SceneTab T, int n,
@@ -576,7 +581,8 @@ k_adj_density(const __grid_constant__ DevParams P0, const SceneTab T, int n,
               const uint32_t *__restrict__ upbits, const uint32_t *__restrict__ hitlist,
               const uint32_t *__restrict__ hitcnt, const uint32_t *__restrict__ revlist,
               const uint32_t *__restrict__ revcnt, const uint32_t *__restrict__ src,
-              const float *__restrict__ rb, const float4 *__restrict__ xa, float4 *__restrict__ x_out) {
+              const float *__restrict__ rb, const float4 *__restrict__ xa, float4 *__restrict__ x_out,
+              bool walk_overflow) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const DevParams &P = scene_params(P0, T, s);
@@ -618,7 +624,7 @@ k_adj_density(const __grid_constant__ DevParams P0, const SceneTab T, int n,
     const uint32_t nh = hitcnt[s];
     if (nh <= (uint32_t)P.hcap) {
         for (uint32_t t = 0; t < nh; t++) both(hitlist[list_at(P, s, t)]);
-    } else {
+    } else if (walk_overflow) {
         const int base = (int)gc - P.nadj;
         for (int c = 0; c < P.gridAdjCnt; c++) {
             CandIter it;
@@ -635,7 +641,7 @@ k_adj_density(const __grid_constant__ DevParams P0, const SceneTab T, int n,
     const uint32_t nr = revcnt[s];
     if (nr <= (uint32_t)P.hcap) {
         for (uint32_t t = 0; t < nr; t++) rev(revlist[list_at(P, s, t)]);
-    } else {
+    } else if (walk_overflow) {
         const uint32_t *lobits = upbits + 3 * (size_t)P.upwords;
         RevIter it;
         rev_begin<PRUNE>(it, P, gc, my_code, true);
@@ -652,11 +658,10 @@ k_adj_density(const __grid_constant__ DevParams P0, const SceneTab T, int n,
 // ---------------------------------------------------------------------------
 // Crowded points. A point whose own or reverse pair list overflowed (a
 // collapsing scene crowds hundreds or thousands of points into a cell) is
-// left out of k_adj_force's list drain and appended to the crowd list;
-// k_adj_crowd_force then gives each listed point a whole block, so its
-// pairs -- the costliest arithmetic of the reverse step -- spread over the
-// GPU instead of one thread walking them all. (The density adjoint's pair
-// terms are light; its overflowed points walk per thread.) The candidates of each walked cell are cut
+// left out of k_adj_force's and k_adj_density's list drains and appended to
+// the crowd list; k_adj_crowd_force and k_adj_crowd_density then give each
+// listed point a whole block, so its pairs spread over the GPU instead of
+// one thread walking them all. The candidates of each walked cell are cut
 // into 32-slot chunks counted from the cell's first slot; chunk g of the
 // point's walk goes to warp g % warps and lane l of that warp takes slot
 // l of the chunk when the band flags keep it. The lanes' sums are added in
@@ -774,6 +779,68 @@ k_adj_crowd_force(const __grid_constant__ DevParams P0, const SceneTab T, const 
             e_out[dst] = make_float4(e0.x + v[3], e0.y + v[4], e0.z + v[5], 0.f);
             rb[s] += v[6];
             pc[s] = make_float4(c0.x + v[7], c0.y + v[8], c0.z + v[9], 0.f);
+        }
+        __syncthreads();
+    }
+}
+
+// The density adjoint's walked pairs of each crowded point (k_adj_density
+// leaves them out when walk_overflow is off), added to the dL/dX
+// k_adj_density wrote for it.
+template <bool PRUNE>
+__global__ void __launch_bounds__(kCrowdThreads)
+k_adj_crowd_density(const __grid_constant__ DevParams P0, const SceneTab T, const float4 *__restrict__ pos,
+                    const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ off,
+                    const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
+                    const uint32_t *__restrict__ hitcnt, const uint32_t *__restrict__ revcnt,
+                    const uint32_t *__restrict__ src, const float *__restrict__ rb, float4 *__restrict__ x_out,
+                    const CrowdList L) {
+    __shared__ float s_red[kCrowdThreads / 32][3];
+    __shared__ uint32_t s_nlist;
+    if (threadIdx.x == 0) s_nlist = min(*(volatile uint32_t *)L.count, L.cap);
+    __syncthreads();
+    const uint32_t nlist = s_nlist;
+    for (uint32_t b = blockIdx.x; b < nlist; b += gridDim.x) {
+        const int s = (int)L.pts[b];
+        const DevParams &P = scene_params(P0, T, s);
+        const uint32_t gc = gcell[s];
+        const float4 p4 = pos[s];
+        const float3 X = xyz(p4);
+        const float kmp = -6.0f * P.d2 * P.pmass * P.poly6kern;
+        const float gs = kmp * rb[s];
+        const uint32_t c_lo = off[gc], c_hi = c_lo + cnt[gc], hcap = (uint32_t)P.hcap;
+        float3 part = make_float3(0.f, 0.f, 0.f);
+        auto rev = [&](uint32_t o, float4 q) {   // owner o: - g_o w^2 (X_o - X_s)
+            const float3 D = make_float3(q.x - X.x, q.y - X.y, q.z - X.z);
+            const float w = (P.rd2 - (D.x * D.x + D.y * D.y + D.z * D.z)) * P.d2;
+            const float k = kmp * rb[o] * w * w;
+            part.x -= k * D.x; part.y -= k * D.y; part.z -= k * D.z;
+        };
+        crowd_chunks<PRUNE>(P, gc, __float_as_uint(p4.w), hitcnt[s] > hcap, revcnt[s] > hcap, off, cnt, upbits,
+                            [&](uint32_t j, bool is_rev) {
+            const float4 q = pos[j];
+            if (!is_rev) {
+                const float dsq = dsq_rn(p4.x - q.x, p4.y - q.y, p4.z - q.z);
+                if (dsq < P.rd2 && dsq > 0.0f) {
+                    if (gs != 0.0f) {   // owner s: + gs w^2 (X_s - X_j)
+                        const float3 D = make_float3(X.x - q.x, X.y - q.y, X.z - q.z);
+                        const float w = (P.rd2 - (D.x * D.x + D.y * D.y + D.z * D.z)) * P.d2;
+                        const float k = gs * w * w;
+                        part.x += k * D.x; part.y += k * D.y; part.z += k * D.z;
+                    }
+                    if (j >= c_lo && j < c_hi) rev(j, q);
+                }
+            } else {
+                const float dsq = dsq_rn(q.x - X.x, q.y - X.y, q.z - X.z);
+                if (dsq < P.rd2 && dsq > 0.0f) rev(j, q);
+            }
+        });
+        float v[3] = {part.x, part.y, part.z};
+        block_sum<3>(v, s_red);
+        if (threadIdx.x == 0) {
+            const uint32_t dst = src[s];
+            const float4 x0 = x_out[dst];
+            x_out[dst] = make_float4(x0.x + v[0], x0.y + v[1], x0.z + v[2], 0.f);
         }
         __syncthreads();
     }
@@ -905,14 +972,19 @@ int fl_launch_adj_force(fl_system *s, const float2 *rr, const float4 *fb, float4
 }
 
 int fl_launch_adj_density(fl_system *s, const uint32_t *revlist, const uint32_t *revcnt, const float *rb,
-                          const float4 *xa, float4 *x_out) {
+                          const float4 *xa, float4 *x_out, uint32_t *crowd, uint32_t *crowd_count) {
     if (s->n == 0) return FL_OK;
     const bool pr = adj_prune(s);
     auto kern = pr ? k_adj_density<true> : k_adj_density<false>;
     kern<<<blocks_for(s->n, kAdjThreads), kAdjThreads, 0, s->stream>>>(
         s->D, fl_scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->f[F_GCELL].cur<uint32_t>(), s->off,
-        s->cnt, s->upbits, s->hitlist, s->hitcnt, revlist, revcnt, s->src, rb, xa, x_out);
+        s->cnt, s->upbits, s->hitlist, s->hitcnt, revlist, revcnt, s->src, rb, xa, x_out, false);
     FL_LAUNCH_CHECK("adj_density");
+    auto crowd_kern = pr ? k_adj_crowd_density<true> : k_adj_crowd_density<false>;
+    crowd_kern<<<crowd_grid(s), kCrowdThreads, 0, s->stream>>>(
+        s->D, fl_scene_tab(s), s->f[F_POS].cur<float4>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt, s->upbits,
+        s->hitcnt, revcnt, s->src, rb, x_out, CrowdList{crowd, crowd_count, (uint32_t)s->n});
+    FL_LAUNCH_CHECK("adj_crowd_density");
     return FL_OK;
 }
 

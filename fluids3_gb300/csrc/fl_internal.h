@@ -224,7 +224,7 @@ int fl_launch_adj_force(fl_system *s, const float2 *rr, const float4 *fb, float4
                         float4 *pc, float4 *e_out, uint32_t *revlist, uint32_t *revcnt, uint32_t *crowd,
                         uint32_t *crowd_count);
 int fl_launch_adj_density(fl_system *s, const uint32_t *revlist, const uint32_t *revcnt, const float *rb,
-                          const float4 *xa, float4 *x_out);
+                          const float4 *xa, float4 *x_out, uint32_t *crowd, uint32_t *crowd_count);
 int fl_param_chunks(int max_scene_points);
 int fl_launch_param_reduce(fl_system *s, const float4 *pc, const int *sbase, const int *sn, int nchunks,
                            double *partial, double *acc);

@@ -310,7 +310,8 @@ static int backward_step(fl_system *s, fl_tape *t, const float4 *state, const fl
                                      t->fb, t->g[x][1], t->rr));
         FL_TRY(fl_launch_adj_force(s, t->rr, t->fb, t->xa, t->ea, t->rb, t->pc, t->g[x][2], t->revlist,
                                    t->revcnt, t->crowd, t->crowd_count));
-        FL_TRY(fl_launch_adj_density(s, t->revlist, t->revcnt, t->rb, t->xa, t->g[x][0]));
+        FL_TRY(fl_launch_adj_density(s, t->revlist, t->revcnt, t->rb, t->xa, t->g[x][0], t->crowd,
+                                     t->crowd_count));
         FL_TRY(fl_launch_param_reduce(s, t->pc, t->sbase, t->sn, t->nchunks, t->partial, t->acc));
         return FL_OK;
     }();
