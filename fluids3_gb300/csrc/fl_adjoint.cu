@@ -15,7 +15,7 @@
 // is piecewise constant and carries no derivative.
 //
 // The reverse pass of one step runs on the recomputed forward state of that
-// step (sorted X, V, E, rho, F and the grid) in five launches:
+// step (sorted X, V, E, rho, F and the grid):
 //   k_adj_advance   per point: the advance's adjoint; dL/dF, dL/dV (written
 //                   through the permutation) and the direct parts of dL/dX, dL/dE
 //   k_adj_revwalk   per point s: its reverse pairs outside its own cell (the
@@ -25,6 +25,8 @@
 //                   partials
 //   k_adj_density   per point, own and reverse pairs (both from lists): the
 //                   density's share of dL/dX, written through the permutation
+//   k_adj_crowd_*   the same two for points whose lists overflowed, a block
+//                   per point
 //   k_param_*       deterministic per-scene sums of the parameter partials
 // Every sum is a per-thread gather (no atomics), so the result is
 // bit-reproducible from run to run. The search block of a point in cell c
