@@ -4,8 +4,8 @@
 Workload (N=1): the 4,000,000-point wave tank -- a jittered lattice filling
 the low-x 40% of a ~330-unit box, dam-break parameters (h = 0.01 m, cell 2h,
 gridSrch 2), X- wall forcing at frequency 0.2 and amplitude 0.3. One step
-is one full Run: insert, scan, index scatter, canonical sort + gather,
-density, force + advance (six kernels).
+is one full Run: insert, scan, index scatter, canonical cell sort (and the
+crowded-cell sort), gather, density, force + advance (eight kernels).
 
   value   device-timed throughput, state resident in HBM, graph replay of
           exactly K steps between CUDA events on the system stream, run as

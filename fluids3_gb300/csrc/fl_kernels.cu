@@ -312,7 +312,7 @@ __device__ __forceinline__ CellCtx cell_ctx(const DevParams &P0, const SceneTab 
     return cx;
 }
 
-// The move of the fused sort, one thread per sorted slot s: the point
+// The move of the fused step's sort, one thread per sorted slot s: the point
 // src[s] (canonical order, set by k_sort_cells in mode 1) goes to slot s
 // with its band code in pos.w, its cell in gcell and its rank within the
 // cell in gndx (countingSortFull, fluids4.0/fluid_kernels.cu:56-87, with
