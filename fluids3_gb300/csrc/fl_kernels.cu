@@ -20,9 +20,9 @@ namespace {
 #include "fl_device.cuh"
 
 // insertParticles (fluids4.0/fluid_kernels.cu:22-53) with warp-aggregated
-// counting: lanes of a warp that land in the same cell elect one leader,
-// which adds the group size with a single atomic; each lane's arrival rank is
-// the group's base plus its position among the group's lanes. The rank is
+// counting: a run of consecutive lanes that land in the same cell elects its
+// first lane, which adds the run's length with a single atomic; each lane's
+// arrival rank is the run's base plus its position in the run. The rank is
 // only an intermediate: the canonical within-cell order is fixed later by
 // k_sort_cells.
 // Batched systems: a point's cell is offset by its scene's cell_base, so
@@ -43,15 +43,23 @@ k_insert(const __grid_constant__ DevParams P0, const SceneTab T, int n, const fl
         cell_out[i] = cell;
         if (gcell_out) gcell_out[i] = (local == (uint32_t)P.ncells) ? kUndef : cell;
     }
+    // Points come in the previous step's sorted order, so equal cells sit in
+    // runs of consecutive lanes: each run reserves its slots with one atomic
+    // (valid lanes are a prefix of the warp).
     const unsigned active = __ballot_sync(0xffffffffu, valid);
     if (!valid) return;
-    const unsigned peers = __match_any_sync(active, cell);
-    const int leader = __ffs(peers) - 1;
     const unsigned lane = lane_id();
+    const uint32_t prev = __shfl_up_sync(active, cell, 1);
+    const bool head = lane == 0 || prev != cell;
+    const unsigned heads = __ballot_sync(active, head);
+    const unsigned upto = (lane == 31) ? 0xffffffffu : ((2u << lane) - 1u);   // lanes 0..lane
+    const int first = 31 - __clz(heads & upto);                              // this run's head
+    const unsigned later = heads & ~upto;
+    const int end = later ? __ffs(later) - 1 : 32 - __clz(active);            // one past the run
     uint32_t base = 0;
-    if ((int)lane == leader) base = atomicAdd(&cnt[cell], (uint32_t)__popc(peers));
-    base = __shfl_sync(peers, base, leader);
-    rank_out[i] = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+    if (head) base = atomicAdd(&cnt[cell], (uint32_t)(end - (int)lane));
+    base = __shfl_sync(active, base, first);
+    rank_out[i] = base + (uint32_t)((int)lane - first);
 }
 
 // Place each point's index at its arrival slot inside its cell's segment.
