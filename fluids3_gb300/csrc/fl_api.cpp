@@ -559,20 +559,25 @@ extern "C" int fl_set_particles(fl_system *s, int n, const float *pos, const flo
         FL_TRY(fl_ensure_stage(s, 4 * v3));
         const float *src3[4] = {pos, vel, veval, force};
         const int fid[4] = {F_POS, F_VEL, F_VEVAL, F_FORCE};
+        const float *msrc[4];
+        float4 *mdst[4];
+        int nm = 0;
         for (int k = 0; k < 4; k++) {
             float4 *dst = s->f[fid[k]].cur<float4>();
             if (!src3[k]) {
                 FL_CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(float4) * (size_t)n, s->stream));
                 continue;
             }
-            if (const void *mapped = mapped_device_ptr(src3[k])) {
-                FL_TRY(fl_launch_unpack3(s, (const float *)mapped, dst, n));   // read over the host link
+            if (const void *mapped = mapped_device_ptr(src3[k])) {   // read over the host link, below
+                msrc[nm] = (const float *)mapped;
+                mdst[nm++] = dst;
                 continue;
             }
             float *slice = (float *)((char *)s->stage + k * v3);
             FL_CUDA_TRY(cudaMemcpyAsync(slice, src3[k], v3, cudaMemcpyHostToDevice, s->stream));
             FL_TRY(fl_launch_unpack3(s, slice, dst, n));
         }
+        FL_TRY(fl_launch_unpack3_set(s, nm, msrc, mdst, n));
         const void *src1[2] = {press, clr};
         const int fid1[2] = {F_PRESS, F_CLR};
         for (int k = 0; k < 2; k++) {

@@ -253,6 +253,8 @@ int fl_launch_advance(fl_system *s, float time, float dt, float ss);
 int fl_launch_pack3(fl_system *s, const float4 *src, float *dst, int n);
 int fl_launch_set_time(fl_system *s, int slot, float value);
 int fl_launch_unpack3(fl_system *s, const float *src, float4 *dst, int n);
+// up to 4 float3 -> float4 fields in one pass (src[k] may be host-mapped)
+int fl_launch_unpack3_set(fl_system *s, int count, const float *const *src, float4 *const *dst, int n);
 int fl_launch_grid_identity(fl_system *s, uint32_t *dst, int n, const uint32_t *gcell);
 int fl_launch_gcell_ref(fl_system *s, uint32_t *dst);
 int fl_launch_integrity(fl_system *s, unsigned long long *bad_dev);

@@ -807,6 +807,26 @@ __global__ void k_unpack3(int n, const float *__restrict__ src, float4 *__restri
     dst[i] = make_float4(src[3 * i + 0], src[3 * i + 1], src[3 * i + 2], 0.0f);
 }
 
+// Up to four float3 fields at once (uploads read straight from page-locked
+// host memory: one pass keeps more of the link's requests in flight).
+struct Unpack3Set {
+    const float *src[4];
+    float4 *dst[4];
+    int count;
+};
+
+__global__ void k_unpack3_set(int n, const __grid_constant__ Unpack3Set u) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float3 v[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        if (k < u.count) v[k] = make_float3(u.src[k][3 * i + 0], u.src[k][3 * i + 1], u.src[k][3 * i + 2]);
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        if (k < u.count) u.dst[k][i] = make_float4(v[k].x, v[k].y, v[k].z, 0.0f);
+}
+
 // FGCELL readback of a batched system: internal cell entries count one
 // out-of-range bin per earlier scene; the reference layout does not.
 __global__ void k_gcell_ref(int n, const uint32_t *__restrict__ gcell, const uint16_t *__restrict__ scene,
@@ -1126,6 +1146,16 @@ int fl_launch_pack3(fl_system *s, const float4 *src, float *dst, int n) {
     if (n == 0) return FL_OK;
     k_pack3<<<blocks_for(n, kThreads), kThreads, 0, s->stream>>>(n, src, dst);
     FL_LAUNCH_CHECK("pack3");
+    return FL_OK;
+}
+
+int fl_launch_unpack3_set(fl_system *s, int count, const float *const *src, float4 *const *dst, int n) {
+    if (n == 0 || count == 0) return FL_OK;
+    Unpack3Set u = {};
+    u.count = count;
+    for (int k = 0; k < count; k++) { u.src[k] = src[k]; u.dst[k] = dst[k]; }
+    k_unpack3_set<<<blocks_for(n, kThreads), kThreads, 0, s->stream>>>(n, u);
+    FL_LAUNCH_CHECK("unpack3_set");
     return FL_OK;
 }
 
