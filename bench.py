@@ -617,7 +617,13 @@ def our_arm(args, rank, world, local_rank):
                             "dissipate it, the moving X- wall feeds it"}
 
     # -- e2e: host buffers through the C ABI ------------------------------------
+    # inputs of every e2e step: the timed segments' start state advanced half
+    # a segment (the mean regime of the timed steps; the fluid clumps as a
+    # segment goes on)
     e2e_steps = args.e2e_steps or min(args.steps, 20)
+    s.RestoreCheckpoint(0)
+    s.RunSteps(max(1, seg_steps // 2))
+    s.Sync()
     n = scene.n
     pin_pos = F.PinnedArray((n, 3), np.float32)
     pin_vel = F.PinnedArray((n, 3), np.float32)
@@ -632,14 +638,19 @@ def our_arm(args, rank, world, local_rank):
     vp = lambda a: a.ctypes.data_as(C.c_void_p)
     h2d = n * (12 * 3 + 4)
     d2h = n * 12
-    barrier()
-    s.Sync()
-    te0 = time.perf_counter()
-    for _ in range(e2e_steps):
+
+    def e2e_step():
         F._lib.check("fl_set_particles", lib.fl_set_particles(
             s.handle, n, vp(pin_pos.array), vp(pin_vel.array), vp(pin_vev.array), None, None, vp(pin_clr.array)))
         F._lib.check("fl_run", lib.fl_run(s.handle))
         F._lib.check("fl_get_buffer", lib.fl_get_buffer(s.handle, F.FPOS, vp(pin_out.array), d2h))
+
+    e2e_step()   # untimed warm-up: first uploads, the captured step graph released
+    barrier()
+    s.Sync()
+    te0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
     te1 = time.perf_counter()
     barrier()
     e2e_s = allmax(dist, te1 - te0)
@@ -687,7 +698,9 @@ def our_arm(args, rank, world, local_rank):
         "phases_ms": {k: round(v, 5) for k, v in phases.items()}, "phase_steps": nsteps_timed,
         "cpu_baseline": cpu,
         "e2e": {"value": world * n * e2e_steps / e2e_s / 1e6, "unit": METRIC, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+                "d2h_bytes_per_step": d2h, "steps": e2e_steps,
+                "inputs": f"every step uploads the state {max(1, seg_steps // 2)} steps into a timed segment "
+                          "(its mean regime) from page-locked host memory and reads the positions back"},
         "autotuned_block_shapes": tuned,
         "conservation": conservation,
         "batched": batched,
