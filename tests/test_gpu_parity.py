@@ -604,3 +604,37 @@ def test_conservation_sums_match_fp64_of_the_oracle_state():
             s.RunSteps(7)
             alone = s.Conservation()[0]
         assert np.allclose(per[k], alone, rtol=1e-12, atol=1e-12 * np.abs(alone).max()), k
+
+
+def test_pinned_host_buffers_match_pageable_ones():
+    """Uploads from page-locked host memory (read by the unpack kernel over
+    the host link, several fields in one pass), from a mix of page-locked,
+    pageable and absent fields, and a readback into page-locked memory, all
+    give what pageable buffers give."""
+    import ctypes as C
+    sc = scenes.dam_break(n=5000, seed=33)
+    pins = {k: F.PinnedArray((sc.n, 3), np.float32) for k in ("pos", "vel", "vev", "out")}
+    try:
+        pins["pos"].array[:] = sc.pos
+        pins["vel"].array[:] = sc.vel
+        pins["vev"].array[:] = sc.veval
+        with make_system(sc.params, sc.pos, sc.vel, sc.veval, sc.clr) as a, \
+                F.FluidSystem(sc.params, sc.n) as b, F.FluidSystem(sc.params, sc.n) as c:
+            b.SetParticles(pins["pos"].array, pins["vel"].array, pins["vev"].array, clr=sc.clr)
+            c.SetParticles(pins["pos"].array, sc.vel, None, clr=sc.clr)
+            sa, sb, sc_ = gpu_state(a), gpu_state(b), gpu_state(c)
+            for k in ("pos", "vel", "veval", "clr"):
+                assert_bit_equal(sb[k], sa[k], f"all page-locked {k}")
+            for k in ("pos", "vel", "clr"):
+                assert_bit_equal(sc_[k], sa[k], f"mixed {k}")
+            assert not sc_["veval"].any()
+            a.RunSteps(3)
+            b.RunSteps(3)
+            b.Sync()
+            out = pins["out"].array
+            F._lib.check("fl_get_buffer", F.lib().fl_get_buffer(
+                b.handle, F.FPOS, out.ctypes.data_as(C.c_void_p), out.nbytes))
+            assert_bit_equal(out, a.GetBuffer(F.FPOS), "page-locked readback")
+    finally:
+        for p in pins.values():
+            p.free()
