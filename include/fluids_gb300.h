@@ -201,8 +201,9 @@ int fl_add_particles(fl_system *s, int k, const float *pos, const float *vel, co
 int fl_get_buffer(fl_system *s, int buf_id, void *host_dst, size_t bytes);
 
 /* Page-locked host memory for the transfer calls above. It is mapped into
- * the device's address space, so fl_set_particles and fl_get_buffer move
- * float3 fields between it and HBM in one kernel pass (no staging copy). */
+ * the device's address space: fl_set_particles reads float3 fields from it
+ * in one kernel pass (no staging copy), and fl_get_buffer fills it with one
+ * copy-engine transfer of the packed field. */
 int fl_host_alloc(size_t bytes, void **out);
 int fl_host_free(void *p);
 
