@@ -23,6 +23,9 @@ crowded-cell sort), gather, density, force + advance (eight kernels).
           launch time (per-phase CUDA events over a second K-step region)
   cpu_baseline  the reference's CPU path (the reference kernels built for the
           host where available, else the oracle port) on a bounded sample
+  reference_gpu  the reference's own GPU kernels (its kernel module built for
+          sm_103a with its build's flags, driven as its Run drives them) on
+          the same workload, state and segment protocol as value
 
   batched  256 scenes stepped as one batched system vs one at a time
   adjoint  adjoint/forward time per step: the differentiated 65,536-point
@@ -79,6 +82,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=None, help="steps in the e2e region (default: min(K, 20))")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ref-gpu", action="store_true",
+                    help="skip timing the reference's own GPU kernels on the same workload")
     ap.add_argument("--batch-scenes", type=int, default=256,
                     help="scenes in the batched-vs-one-at-a-time comparison (0 skips it)")
     ap.add_argument("--batch-steps", type=int, default=20)
@@ -234,6 +239,51 @@ def cpu_reference_rate(scene, budget_s: float, threads: int):
     return {"value": n * steps / el / 1e6, "unit": METRIC, "cores": threads, "kind": kind,
             "sample": f"{steps} full steps over the first {n:,} of the {scene.n:,} points (same box, grid "
                       f"and parameters), {el:.1f} s, {threads} host threads"}, el
+
+
+def reference_gpu_rate(scene, warm: dict, t_start: float, steps: int, segment: int, value: float) -> dict:
+    """The reference's own GPU step on this GPU: fluids4.0/fluid_kernels.cu
+    built for sm_103a with its build's flags, driven as FluidSystem::Run
+    drives it (phase by phase on the default stream, cuCtxSynchronize at the
+    end of every step). Same workload and protocol as `value`: the
+    post-warm-up state, K steps run as segments of at most `segment` steps
+    that each restart from it (the restart upload is not timed)."""
+    from oracle import ref_gpu as R
+
+    if not R.available():
+        return {"unavailable": "the reference's GPU module was not built (reference tree absent at build time)"}
+    import torch
+
+    n = scene.n
+    with R.RefGpu(scene.params, n) as ref:
+        ref.set_state(warm["pos"], warm["vel"], warm["veval"], warm["clr"])
+        t = t_start
+        for _ in range(3):   # module's first launches
+            t = ref.run(t)
+        total_ms, left, n_in = 0.0, steps, []
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        while left > 0:
+            chunk = min(left, segment) if segment > 0 else left
+            ref.set_state(warm["pos"], warm["vel"], warm["veval"], warm["clr"])
+            t = t_start
+            ev0.record()
+            for _ in range(chunk):
+                t = ref.run(t)
+            ev1.record()
+            torch.cuda.synchronize()
+            total_ms += ev0.elapsed_time(ev1)
+            n_in.append(int(ref.get(R.FGRIDCNT).sum(dtype=np.int64)))
+            left -= chunk
+    rate = n * steps / (total_ms / 1e3) / 1e6
+    return {"value": rate, "unit": METRIC, "ms_per_step": total_ms / steps, "steps": steps,
+            "kind": "reference kernels on this GPU",
+            "build": "fluids4.0/fluid_kernels.cu, nvcc -gencode arch=compute_103a,code=sm_103a -O3 "
+                     "--use_fast_math --maxrregcount=32 (the reference build's flags)",
+            "driver": "RUN_GPU_FULL phase sequence through the CUDA driver API, 512 threads per block, "
+                      "default stream, cuCtxSynchronize per step (fluid_system.cpp:506-524)",
+            "timing": "CUDA events on the default stream around each segment",
+            "points_in_range_at_segment_ends": n_in,
+            "value_over_reference": value / rate}
 
 
 def reference_arm(args, rank, world):
@@ -571,6 +621,10 @@ def our_arm(args, rank, world, local_rank):
     s.SaveCheckpoint(0)
     s.RunSteps(2)                       # capture the graph for the tuned shapes
     s.RestoreCheckpoint(0)
+    warm = None
+    if rank == 0 and not args.no_ref_gpu:   # start state of the timed segments, for the reference's GPU leg
+        warm = {"pos": s.GetBuffer(F.FPOS), "vel": s.GetBuffer(F.FVEL), "veval": s.GetBuffer(F.FVEVAL),
+                "clr": s.GetBuffer(F.FCLR), "time": s.time}
 
     # -- timed region: exactly K steps, graph replay ---------------------------
     clocks = ClockSampler(local_rank).start()
@@ -685,6 +739,12 @@ def our_arm(args, rank, world, local_rank):
     cpu = None
     if not args.no_cpu_baseline:
         cpu, _ = cpu_reference_rate(scene, args.cpu_seconds, cpu_threads())
+    ref_gpu = None
+    if warm is not None:
+        try:
+            ref_gpu = reference_gpu_rate(scene, warm, warm["time"], args.steps, args.segment, value)
+        except (OSError, RuntimeError, ValueError) as e:
+            ref_gpu = {"unavailable": f"{type(e).__name__}: {e}"}
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -697,6 +757,7 @@ def our_arm(args, rank, world, local_rank):
                           "frac": step_bytes / (ms / args.steps / 1e3) / 1e9 / peak},
         "phases_ms": {k: round(v, 5) for k, v in phases.items()}, "phase_steps": nsteps_timed,
         "cpu_baseline": cpu,
+        "reference_gpu": ref_gpu,
         "e2e": {"value": world * n * e2e_steps / e2e_s / 1e6, "unit": METRIC, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": e2e_steps,
                 "inputs": f"every step uploads the state {max(1, seg_steps // 2)} steps into a timed segment "

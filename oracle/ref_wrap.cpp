@@ -14,6 +14,7 @@
  * Built by oracle/build_ref.sh into oracle/_ref/; only tests/, bench.py's
  * reference arm and the smoke check load it, never the product.
  */
+#include <stddef.h>
 #include <stdint.h>
 #include <string.h>
 #include <stdlib.h>
@@ -163,5 +164,26 @@ void ref_run(int n, int steps, float *time, float dt, int threads) {
 }
 
 int ref_sizeof_fparams(void) { return (int)sizeof(FParams); }
+
+/* Byte offset of FParams field `name` as the reference header lays it out
+ * (fluids4.0/fluid.h:155-192); "sizeof FParams", "sizeof FBufs" and
+ * "FBufs.mgpu" give those; -1 for an unknown name. Lets a test check the
+ * field-by-field restatement that drives the reference's GPU module. */
+long ref_layout(const char *name) {
+#define L(f) if (!strcmp(name, #f)) return (long)offsetof(FParams, f);
+    L(mode) L(example) L(sim_scale) L(capture) L(numThreads) L(numBlocks) L(gridThreads) L(gridBlocks)
+    L(szPnts) L(szHash) L(szGrid) L(stride) L(pnum) L(chk) L(pdist) L(pmass) L(prest_dens) L(pintstiff)
+    L(pradius) L(psmoothradius) L(pspacing) L(r2) L(pvisc) L(AL) L(AL2) L(VL) L(VL2) L(d2) L(rd2) L(vterm)
+    L(poly6kern) L(spikykern) L(lapkern) L(gausskern) L(grid_size) L(grid_density) L(gridSize) L(gridDelta)
+    L(gridMin) L(gridMax) L(gridRes) L(gridScanMax) L(gridSrch) L(gridTotal) L(gridAdjCnt) L(gridActive)
+    L(gridAdj) L(bound_slope) L(bound_stiff) L(bound_friction) L(bound_damp) L(bound_wall_force)
+    L(bound_wall_freq) L(bound_min) L(bound_max) L(init_min) L(init_max) L(grav_dir) L(grav_pos) L(gravity)
+    L(grav_amt) L(emit_rate) L(emit_pos) L(emit_ang) L(emit_dang) L(emit_spread) L(brickRes) L(pemit) L(pmem)
+#undef L
+    if (!strcmp(name, "sizeof FParams")) return (long)sizeof(FParams);
+    if (!strcmp(name, "sizeof FBufs")) return (long)sizeof(FBufs);
+    if (!strcmp(name, "FBufs.mgpu")) return (long)offsetof(FBufs, mgpu);
+    return -1;
+}
 
 } /* extern "C" */
