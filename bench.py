@@ -274,6 +274,24 @@ def reference_gpu_rate(scene, warm: dict, t_start: float, steps: int, segment: i
             total_ms += ev0.elapsed_time(ev1)
             n_in.append(int(ref.get(R.FGRIDCNT).sum(dtype=np.int64)))
             left -= chunk
+        # per-phase device times over one segment from the same state: events
+        # between the phases of each Run (a separate, untimed pass)
+        names = ("insert", "prefix_sum", "counting_sort", "pressure", "force", "advance")
+        acc = dict.fromkeys(names, 0.0)
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(len(names) + 1)]
+        ref.set_state(warm["pos"], warm["vel"], warm["veval"], warm["clr"])
+        t = t_start
+        k = min(steps, segment) if segment > 0 else steps
+        for _ in range(k):
+            evs[0].record()
+            for a, phase in enumerate((ref.insert, lambda: ref.prefix_sum(1), ref.counting_sort, ref.pressure,
+                                       ref.force, lambda: ref.advance(t))):
+                phase()
+                evs[a + 1].record()
+            torch.cuda.synchronize()
+            t = float(np.float32(t) + np.float32(ref.dt))
+            for a, name in enumerate(names):
+                acc[name] += evs[a].elapsed_time(evs[a + 1])
     rate = n * steps / (total_ms / 1e3) / 1e6
     return {"value": rate, "unit": METRIC, "ms_per_step": total_ms / steps, "steps": steps,
             "kind": "reference kernels on this GPU",
@@ -283,6 +301,7 @@ def reference_gpu_rate(scene, warm: dict, t_start: float, steps: int, segment: i
                       "default stream, cuCtxSynchronize per step (fluid_system.cpp:506-524)",
             "timing": "CUDA events on the default stream around each segment",
             "points_in_range_at_segment_ends": n_in,
+            "phases_ms": {name: round(v / k, 5) for name, v in acc.items()}, "phase_steps": k,
             "value_over_reference": value / rate}
 
 
