@@ -17,8 +17,10 @@ crowded-cell sort), gather, density, force + advance (eight kernels).
           any implementation; segments keep every timed step in the
           configured regime.
   e2e     the same metric through the public C ABI with host buffers: per
-          step, pinned host -> device upload of the step's inputs
-          (fl_set_particles), fl_run, device -> host read of the positions
+          step, fl_run_from_host (the step's inputs uploaded from pinned host
+          memory, then the step; velocities and colours arrive on a copy
+          engine during the step's first kernels) and a device -> host read
+          of the positions (fl_get_buffer)
   roofline  the dominant kernel's algorithmic bytes per launch / its mean
           launch time (per-phase CUDA events over a second K-step region)
   cpu_baseline  the reference's CPU path (the reference kernels built for the
@@ -713,9 +715,8 @@ def our_arm(args, rank, world, local_rank):
     d2h = n * 12
 
     def e2e_step():
-        F._lib.check("fl_set_particles", lib.fl_set_particles(
-            s.handle, n, vp(pin_pos.array), vp(pin_vel.array), vp(pin_vev.array), None, None, vp(pin_clr.array)))
-        F._lib.check("fl_run", lib.fl_run(s.handle))
+        F._lib.check("fl_run_from_host", lib.fl_run_from_host(
+            s.handle, n, vp(pin_pos.array), vp(pin_vel.array), vp(pin_vev.array), vp(pin_clr.array)))
         F._lib.check("fl_get_buffer", lib.fl_get_buffer(s.handle, F.FPOS, vp(pin_out.array), d2h))
 
     e2e_step()   # untimed warm-up: first uploads, the captured step graph released

@@ -159,6 +159,9 @@ static void free_all(fl_system *s) {
     }
     for (int k = 0; k < 8; k++)
         if (s->ev[k]) cudaEventDestroy(s->ev[k]);
+    if (s->ev_early) cudaEventDestroy(s->ev_early);
+    if (s->ev_late) cudaEventDestroy(s->ev_late);
+    if (s->side) cudaStreamDestroy(s->side);
     if (s->stream) cudaStreamDestroy(s->stream);
 }
 
@@ -909,6 +912,93 @@ extern "C" int fl_run(fl_system *s) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_run: null system");
     FL_TRY(begin_run(s));
     FL_TRY(run_step(s, active_timing(s)));
+    if (s->time_host_valid) s->time += s->P.dt;   // AdvanceTime (cpp:529), same float add
+    s->have_insert = 0;
+    s->have_offsets = 1;
+    s->have_grid = 1;
+    return FL_OK;
+}
+
+// The step of fl_run_from_host: run_step with the velocities and colours
+// gathered late, from the staging the side stream fills (ev_late), just
+// before the force pass, their first reader.
+static int run_step_late(fl_system *s, const float *vel3, const uint32_t *clr) {
+    FL_TRY(clear_grid(s));
+    FL_TRY(fl_launch_insert(s, nullptr));
+    FL_TRY(fl_launch_scan(s, s->gcells, 0));
+    FL_TRY(fl_launch_scatter_index(s));
+    FL_TRY(fl_launch_sort_cells(s, 1, false));
+    flip(s, F_POS); flip(s, F_VEL); flip(s, F_VEVAL); flip(s, F_CLR); flip(s, F_GCELL); flip(s, F_GNDX);
+    FL_TRY(fl_launch_density(s));
+    FL_CUDA_TRY(cudaStreamWaitEvent(s->stream, s->ev_late, 0));
+    FL_TRY(fl_launch_gather_late(s, vel3, clr, s->f[F_VEL].cur<float4>(), s->f[F_CLR].cur<uint32_t>()));
+    FL_TRY(fl_launch_force_advance(s, s->P.dt));
+    flip(s, F_POS); flip(s, F_VEVAL);
+    s->codes_valid = 0;
+    s->lists_valid = 0;
+    s->time_slot ^= 1;
+    return FL_OK;
+}
+
+static int ensure_side(fl_system *s) {
+    if (!s->side) FL_CUDA_TRY(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+    if (!s->ev_early) FL_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_early, cudaEventDisableTiming));
+    if (!s->ev_late) FL_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_late, cudaEventDisableTiming));
+    return FL_OK;
+}
+
+// TransferToCUDA + Run (fluids4.0/fluid_system.cpp:2312-2321, 506-524) in one
+// call, for a state kept in host memory between steps. With the point fields
+// in page-locked memory, positions and evaluated velocities are read over
+// the host link first; velocities and colours, first needed by the force
+// pass, follow on a copy engine (side stream) while insert, sort and density
+// run, and k_gather_late puts them in sorted order. Results equal
+// fl_set_particles followed by fl_run, bit for bit; other host memory, a
+// batched system, a recording tape or phase timing take that path.
+extern "C" int fl_run_from_host(fl_system *s, int n, const float *pos, const float *vel, const float *veval,
+                                const uint32_t *clr) {
+    if (!s || !pos) return fl_fail(FL_ERR_ARG, "fl_run_from_host: null system or pos");
+    if (n < 0) return fl_fail(FL_ERR_ARG, "fl_run_from_host: n < 0");
+    if (n > s->max_points)
+        return fl_fail(FL_ERR_CAPACITY, "fl_run_from_host: %d points exceed capacity %d", n, s->max_points);
+    const void *mpos = mapped_device_ptr(pos);
+    const void *mvev = veval ? mapped_device_ptr(veval) : nullptr;
+    const bool pinned = mpos && (!veval || mvev) && (!vel || mapped_device_ptr(vel)) &&
+                        (!clr || mapped_device_ptr(clr));
+    if (n == 0 || !pinned || s->batched || s->timing || fl_tape_recording(s)) {
+        FL_TRY(fl_set_particles(s, n, pos, vel, veval, nullptr, nullptr, clr));
+        FL_TRY(fl_run(s));
+        FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+        return FL_OK;
+    }
+    destroy_graph(s);
+    FL_TRY(ensure_side(s));
+    FL_TRY(fl_ensure_stage(s, 16 * (size_t)n));
+    s->n = n;
+    const size_t n4 = 16 * (size_t)n;
+    // early: positions and evaluated velocities over the link; force and
+    // density cleared (fl_set_particles with those absent)
+    const float *msrc[2] = {(const float *)mpos, (const float *)mvev};
+    float4 *mdst[2] = {s->f[F_POS].cur<float4>(), s->f[F_VEVAL].cur<float4>()};
+    if (!veval) FL_CUDA_TRY(cudaMemsetAsync(s->f[F_VEVAL].cur<float4>(), 0, n4, s->stream));
+    FL_TRY(fl_launch_unpack3_set(s, veval ? 2 : 1, msrc, mdst, n));
+    FL_CUDA_TRY(cudaMemsetAsync(s->f[F_FORCE].cur<float4>(), 0, n4, s->stream));
+    FL_CUDA_TRY(cudaMemsetAsync(s->f[F_PRESS].cur<float>(), 0, 4 * (size_t)n, s->stream));
+    // late: velocities and colours on the copy engine once the link is free
+    float *stage_vel = vel ? (float *)s->stage : nullptr;
+    uint32_t *stage_clr = clr ? (uint32_t *)((char *)s->stage + 12 * (size_t)n) : nullptr;
+    FL_CUDA_TRY(cudaEventRecord(s->ev_early, s->stream));
+    FL_CUDA_TRY(cudaStreamWaitEvent(s->side, s->ev_early, 0));
+    if (vel) FL_CUDA_TRY(cudaMemcpyAsync(stage_vel, vel, 12 * (size_t)n, cudaMemcpyHostToDevice, s->side));
+    if (clr) FL_CUDA_TRY(cudaMemcpyAsync(stage_clr, clr, 4 * (size_t)n, cudaMemcpyHostToDevice, s->side));
+    FL_CUDA_TRY(cudaEventRecord(s->ev_late, s->side));
+    fl_reset_progress(s);
+    FL_TRY(begin_run(s));
+    const int r = run_step_late(s, stage_vel, stage_clr);
+    // the host arrays are the caller's again once the step is done
+    const cudaError_t e = cudaStreamSynchronize(s->stream);
+    FL_TRY(r);
+    if (e != cudaSuccess) return fl_fail(FL_ERR_CUDA, "fl_run_from_host: %s", cudaGetErrorString(e));
     if (s->time_host_valid) s->time += s->P.dt;   // AdvanceTime (cpp:529), same float add
     s->have_insert = 0;
     s->have_offsets = 1;

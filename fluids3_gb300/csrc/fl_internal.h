@@ -170,6 +170,12 @@ struct fl_system {
     // adjoint tape (fl_tape.cpp), null until fl_tape_begin
     struct fl_tape *tape;
 
+    // fl_run_from_host: the copy-engine stream that brings velocities and
+    // colours in while the step's first kernels run, and its two events
+    // (created on first use)
+    cudaStream_t side;
+    cudaEvent_t ev_early, ev_late;
+
     // per-phase event timing (PERF_PUSH/PERF_POP of Run, cpp:507-515)
     int timing;
     cudaEvent_t ev[8];
@@ -238,7 +244,13 @@ int fl_launch_scatter_index(fl_system *s);
 // mode 1: sorted src, then a gather of pos/vel/veval/clr/gcell/gndx into the
 //         nxt copies with band codes and the upper-band slot flags (rows 0-2)
 // mode 2: mode 1 that also writes the lower-band slot flags (upbits rows 3-5)
-int fl_launch_sort_cells(fl_system *s, int mode);
+// move_vel_clr false (mode 1, plain systems): the gather leaves velocity and
+// colour to fl_launch_gather_late
+int fl_launch_sort_cells(fl_system *s, int mode, bool move_vel_clr = true);
+// velocity (packed float3) and colour staging -> sorted slots through src
+// (null source: zeros)
+int fl_launch_gather_late(fl_system *s, const float *vel3, const uint32_t *clr, float4 *vel_out,
+                          uint32_t *clr_out);
 // one-time kernel attributes (shared memory of the crowded-cell sort)
 int fl_kernels_init(fl_system *s);
 // entries of the crowded-cell list for max_points points (cells above 128)

@@ -327,7 +327,7 @@ __device__ __forceinline__ CellCtx cell_ctx(const DevParams &P0, const SceneTab 
 // the canonical within-cell order). The 32 slots of a warp are one word of
 // each slot-flag row, so the warp stores the words whole: rows 0-2 the
 // upper-band flags (ROWS >= 1), rows 3-5 the lower-band flags (ROWS == 2).
-template <bool BATCH, int ROWS>
+template <bool BATCH, int ROWS, bool VC = true>
 __global__ void __launch_bounds__(kThreads)
 k_gather_sorted(const __grid_constant__ DevParams P0, const SceneTab T, int n, const uint32_t *__restrict__ src,
                 const uint32_t *__restrict__ cell_pre, const uint32_t *__restrict__ off,
@@ -349,9 +349,9 @@ k_gather_sorted(const __grid_constant__ DevParams P0, const SceneTab T, int n, c
         if (ROWS >= 1) code = band_code(P, local, p);
         p.w = __uint_as_float(code);
         pos_out[s] = p;
-        vel_out[s] = vel_in[i];
+        if (VC) vel_out[s] = vel_in[i];
         veval_out[s] = veval_in[i];
-        clr_out[s] = clr_in[i];
+        if (VC) clr_out[s] = clr_in[i];
         gcell_out[s] = (local == P.ncells) ? kUndef : c;
         gndx_out[s] = (uint32_t)s - off[c];
         upwords = (uint32_t)P.upwords;
@@ -366,6 +366,21 @@ k_gather_sorted(const __grid_constant__ DevParams P0, const SceneTab T, int n, c
             if (lane == 0) upbits[(size_t)row * upwords + word] = b;
         }
     }
+}
+
+// The velocities and colours of a step whose state came from host memory
+// (fl_run_from_host), gathered into sorted order after the copy engine has
+// delivered them: packed float3 and uint staging (null: zeros, as
+// fl_set_particles clears an absent field), read through src.
+__global__ void __launch_bounds__(kThreads)
+k_gather_late(int n, const uint32_t *__restrict__ src, const float *__restrict__ vel3,
+              const uint32_t *__restrict__ clr, float4 *__restrict__ vel_out, uint32_t *__restrict__ clr_out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const uint32_t i = src[s];
+    vel_out[s] = vel3 ? make_float4(vel3[3 * (size_t)i], vel3[3 * (size_t)i + 1], vel3[3 * (size_t)i + 2], 0.0f)
+                      : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    clr_out[s] = clr ? clr[i] : 0u;
 }
 
 // Band codes and upper-band slot flags for an already sorted grid
@@ -989,7 +1004,7 @@ int fl_kernels_init(fl_system *s) {
 
 size_t fl_big_cells_cap(int max_points) { return (size_t)(max_points > 0 ? max_points : 1) / 129 + 1; }
 
-int fl_launch_sort_cells(fl_system *s, int mode) {
+int fl_launch_sort_cells(fl_system *s, int mode, bool move_vel_clr) {
     SortArgs a = {};
     a.off = s->off; a.cnt = s->cnt; a.src = s->src; a.scratch = s->rank_tmp;
     a.big_cells = s->big_cells; a.big_count = s->big_count;
@@ -1022,10 +1037,13 @@ int fl_launch_sort_cells(fl_system *s, int mode) {
     FL_LAUNCH_CHECK("sort_big");
     if (s->n > 0) {
         const int rows = s->D.prune ? mode : 0;
-        auto gather = s->batched ? (rows == 2 ? k_gather_sorted<true, 2>
-                                              : rows == 1 ? k_gather_sorted<true, 1> : k_gather_sorted<true, 0>)
-                                 : (rows == 2 ? k_gather_sorted<false, 2>
-                                              : rows == 1 ? k_gather_sorted<false, 1> : k_gather_sorted<false, 0>);
+        if (!move_vel_clr && (s->batched || rows == 2))
+            return fl_fail(FL_ERR_STATE, "sort: deferred velocities only on a plain system's step");
+        auto gather = !move_vel_clr ? (rows == 1 ? k_gather_sorted<false, 1, false> : k_gather_sorted<false, 0, false>)
+                      : s->batched ? (rows == 2 ? k_gather_sorted<true, 2>
+                                                : rows == 1 ? k_gather_sorted<true, 1> : k_gather_sorted<true, 0>)
+                                   : (rows == 2 ? k_gather_sorted<false, 2>
+                                                : rows == 1 ? k_gather_sorted<false, 1> : k_gather_sorted<false, 0>);
         gather<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(
             s->D, fl_scene_tab(s), s->n, s->src, s->cell_pre, s->off, s->f[F_POS].cur<float4>(),
             s->f[F_VEL].cur<float4>(), s->f[F_VEVAL].cur<float4>(), s->f[F_CLR].cur<uint32_t>(),
@@ -1034,6 +1052,14 @@ int fl_launch_sort_cells(fl_system *s, int mode) {
         FL_LAUNCH_CHECK("gather_sorted");
     }
     s->codes_valid = s->D.prune;
+    return FL_OK;
+}
+
+int fl_launch_gather_late(fl_system *s, const float *vel3, const uint32_t *clr, float4 *vel_out,
+                          uint32_t *clr_out) {
+    if (s->n == 0) return FL_OK;
+    k_gather_late<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(s->n, s->src, vel3, clr, vel_out, clr_out);
+    FL_LAUNCH_CHECK("gather_late");
     return FL_OK;
 }
 

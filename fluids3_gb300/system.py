@@ -269,6 +269,21 @@ class FluidSystem:
         """One RUN_GPU_FULL step (cpp:506-524) on the fused kernels, then time += dt."""
         call("fl_run", self._h)
 
+    def RunFromHost(self, pos, vel=None, veval=None, clr=None) -> None:
+        """TransferToCUDA + Run in one call (fl_run_from_host): the state from
+        host arrays, then one step; equal to SetParticles + Run. Arrays in
+        page-locked memory (PinnedArray) let the velocity and colour uploads
+        overlap the step's first kernels."""
+        pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+        n = pos.shape[0]
+
+        def f3(a):
+            return None if a is None else np.ascontiguousarray(a, dtype=np.float32).reshape(n, 3)
+
+        c = None if clr is None else np.ascontiguousarray(clr, dtype=np.uint32).reshape(n)
+        arrs = (pos, f3(vel), f3(veval), c)
+        call("fl_run_from_host", self._h, n, *[_ptr(a) for a in arrs])
+
     def RunSteps(self, nsteps: int) -> None:
         """``nsteps`` Run steps replayed from a captured CUDA graph."""
         call("fl_run_steps", self._h, int(nsteps))

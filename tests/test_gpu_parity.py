@@ -638,3 +638,45 @@ def test_pinned_host_buffers_match_pageable_ones():
     finally:
         for p in pins.values():
             p.free()
+
+
+@pytest.mark.parametrize("case", ["page_locked", "no_vel_no_clr", "pageable", "escapes"])
+def test_run_from_host_equals_set_particles_then_run(case):
+    """fl_run_from_host (the state from host arrays and one step, velocities
+    and colours arriving on a copy engine while the step's first kernels
+    run) gives what fl_set_particles + fl_run give, bit for bit, call after
+    call with each step's result fed back as the next input; the system then
+    steps on normally. Pageable arrays take the two-call path."""
+    sc = scenes.wave_tank(n=60_000)
+    n = sc.n
+    host = {"pos": sc.pos.copy(), "vel": sc.vel.copy(), "veval": sc.veval.copy(), "clr": sc.clr.copy()}
+    if case == "escapes":
+        host["pos"][:3] = [(-500.0, 1.0, 1.0), (1.0, -300.0, 1.0), (np.nan, 0.0, 0.0)]
+    with_vc = case != "no_vel_no_clr"
+    pins = {}
+    if case != "pageable":
+        pins = {k: F.PinnedArray((n, 3), np.float32) for k in ("pos", "vel", "veval")}
+        pins["clr"] = F.PinnedArray((n,), np.uint32)
+    try:
+        with F.FluidSystem(sc.params, n) as a, F.FluidSystem(sc.params, n) as b:
+            for it in range(3):
+                if pins:
+                    for k, p in pins.items():
+                        p.array[:] = host[k]
+                src = {k: (pins[k].array if pins else host[k]) for k in host}
+                a.SetParticles(host["pos"], host["vel"] if with_vc else None, host["veval"],
+                               clr=host["clr"] if with_vc else None)
+                a.Run()
+                b.RunFromHost(src["pos"], src["vel"] if with_vc else None, src["veval"],
+                              clr=src["clr"] if with_vc else None)
+                sa, sb = gpu_state(a), gpu_state(b)
+                for k in FIELDS + ("gridcnt", "gridoff"):
+                    assert_bit_equal(sb[k], sa[k], f"call {it}: {k}")
+                assert a.time == b.time
+                host = {"pos": sa["pos"], "vel": sa["vel"], "veval": sa["veval"], "clr": sa["clr"]}
+            a.RunSteps(2)
+            b.RunSteps(2)
+            assert_bit_equal(b.GetBuffer(F.FPOS), a.GetBuffer(F.FPOS), "steps after")
+    finally:
+        for p in pins.values():
+            p.free()
