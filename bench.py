@@ -18,7 +18,7 @@ crowded-cell sort), gather, density, force + advance (eight kernels).
           configured regime.
   e2e     the same metric through the public C ABI with host buffers: per
           step, fl_run_from_host (the step's inputs uploaded from pinned host
-          memory, then the step; velocities and colours arrive on a copy
+          memory, then the step; all but the positions arrive on a copy
           engine during the step's first kernels) and a device -> host read
           of the positions (fl_get_buffer)
   roofline  the dominant kernel's algorithmic bytes per launch / its mean

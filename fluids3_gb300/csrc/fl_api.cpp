@@ -919,19 +919,21 @@ extern "C" int fl_run(fl_system *s) {
     return FL_OK;
 }
 
-// The step of fl_run_from_host: run_step with the velocities and colours
-// gathered late, from the staging the side stream fills (ev_late), just
-// before the force pass, their first reader.
-static int run_step_late(fl_system *s, const float *vel3, const uint32_t *clr) {
+// The step of fl_run_from_host: run_step with the velocities, evaluated
+// velocities and colours gathered late, from the staging the side stream
+// fills (ev_late), just before the force pass, their first reader (the
+// density pass reads only positions; the evaluated-velocity half of its
+// pair records is completed by the late gather).
+static int run_step_late(fl_system *s, const float *vel3, const float *veval3, const uint32_t *clr) {
     FL_TRY(clear_grid(s));
     FL_TRY(fl_launch_insert(s, nullptr));
     FL_TRY(fl_launch_scan(s, s->gcells, 0));
     FL_TRY(fl_launch_scatter_index(s));
-    FL_TRY(fl_launch_sort_cells(s, 1, false));
+    FL_TRY(fl_launch_sort_cells(s, 1, true));
     flip(s, F_POS); flip(s, F_VEL); flip(s, F_VEVAL); flip(s, F_CLR); flip(s, F_GCELL); flip(s, F_GNDX);
     FL_TRY(fl_launch_density(s));
     FL_CUDA_TRY(cudaStreamWaitEvent(s->stream, s->ev_late, 0));
-    FL_TRY(fl_launch_gather_late(s, vel3, clr, s->f[F_VEL].cur<float4>(), s->f[F_CLR].cur<uint32_t>()));
+    FL_TRY(fl_launch_gather_late(s, vel3, veval3, clr));
     FL_TRY(fl_launch_force_advance(s, s->P.dt));
     flip(s, F_POS); flip(s, F_VEVAL);
     s->codes_valid = 0;
@@ -949,8 +951,8 @@ static int ensure_side(fl_system *s) {
 
 // TransferToCUDA + Run (fluids4.0/fluid_system.cpp:2312-2321, 506-524) in one
 // call, for a state kept in host memory between steps. With the point fields
-// in page-locked memory, positions and evaluated velocities are read over
-// the host link first; velocities and colours, first needed by the force
+// in page-locked memory, the positions are read over the host link first;
+// velocities, evaluated velocities and colours, first needed by the force
 // pass, follow on a copy engine (side stream) while insert, sort and density
 // run, and k_gather_late puts them in sorted order. Results equal
 // fl_set_particles followed by fl_run, bit for bit; other host memory, a
@@ -973,28 +975,29 @@ extern "C" int fl_run_from_host(fl_system *s, int n, const float *pos, const flo
     }
     destroy_graph(s);
     FL_TRY(ensure_side(s));
-    FL_TRY(fl_ensure_stage(s, 16 * (size_t)n));
+    const size_t n3 = 12 * (size_t)n;
+    FL_TRY(fl_ensure_stage(s, 2 * n3 + 4 * (size_t)n));
     s->n = n;
-    const size_t n4 = 16 * (size_t)n;
-    // early: positions and evaluated velocities over the link; force and
-    // density cleared (fl_set_particles with those absent)
-    const float *msrc[2] = {(const float *)mpos, (const float *)mvev};
-    float4 *mdst[2] = {s->f[F_POS].cur<float4>(), s->f[F_VEVAL].cur<float4>()};
-    if (!veval) FL_CUDA_TRY(cudaMemsetAsync(s->f[F_VEVAL].cur<float4>(), 0, n4, s->stream));
-    FL_TRY(fl_launch_unpack3_set(s, veval ? 2 : 1, msrc, mdst, n));
-    FL_CUDA_TRY(cudaMemsetAsync(s->f[F_FORCE].cur<float4>(), 0, n4, s->stream));
+    // early: positions over the link; force and density cleared
+    // (fl_set_particles with those absent)
+    const float *msrc[1] = {(const float *)mpos};
+    float4 *mdst[1] = {s->f[F_POS].cur<float4>()};
+    FL_TRY(fl_launch_unpack3_set(s, 1, msrc, mdst, n));
+    FL_CUDA_TRY(cudaMemsetAsync(s->f[F_FORCE].cur<float4>(), 0, 16 * (size_t)n, s->stream));
     FL_CUDA_TRY(cudaMemsetAsync(s->f[F_PRESS].cur<float>(), 0, 4 * (size_t)n, s->stream));
-    // late: velocities and colours on the copy engine once the link is free
+    // late: the other fields on the copy engine once the link is free
     float *stage_vel = vel ? (float *)s->stage : nullptr;
-    uint32_t *stage_clr = clr ? (uint32_t *)((char *)s->stage + 12 * (size_t)n) : nullptr;
+    float *stage_vev = veval ? (float *)((char *)s->stage + n3) : nullptr;
+    uint32_t *stage_clr = clr ? (uint32_t *)((char *)s->stage + 2 * n3) : nullptr;
     FL_CUDA_TRY(cudaEventRecord(s->ev_early, s->stream));
     FL_CUDA_TRY(cudaStreamWaitEvent(s->side, s->ev_early, 0));
-    if (vel) FL_CUDA_TRY(cudaMemcpyAsync(stage_vel, vel, 12 * (size_t)n, cudaMemcpyHostToDevice, s->side));
+    if (vel) FL_CUDA_TRY(cudaMemcpyAsync(stage_vel, vel, n3, cudaMemcpyHostToDevice, s->side));
+    if (veval) FL_CUDA_TRY(cudaMemcpyAsync(stage_vev, veval, n3, cudaMemcpyHostToDevice, s->side));
     if (clr) FL_CUDA_TRY(cudaMemcpyAsync(stage_clr, clr, 4 * (size_t)n, cudaMemcpyHostToDevice, s->side));
     FL_CUDA_TRY(cudaEventRecord(s->ev_late, s->side));
     fl_reset_progress(s);
     FL_TRY(begin_run(s));
-    const int r = run_step_late(s, stage_vel, stage_clr);
+    const int r = run_step_late(s, stage_vel, stage_vev, stage_clr);
     // the host arrays are the caller's again once the step is done
     const cudaError_t e = cudaStreamSynchronize(s->stream);
     FL_TRY(r);

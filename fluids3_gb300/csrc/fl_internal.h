@@ -244,13 +244,13 @@ int fl_launch_scatter_index(fl_system *s);
 // mode 1: sorted src, then a gather of pos/vel/veval/clr/gcell/gndx into the
 //         nxt copies with band codes and the upper-band slot flags (rows 0-2)
 // mode 2: mode 1 that also writes the lower-band slot flags (upbits rows 3-5)
-// move_vel_clr false (mode 1, plain systems): the gather leaves velocity and
-// colour to fl_launch_gather_late
-int fl_launch_sort_cells(fl_system *s, int mode, bool move_vel_clr = true);
-// velocity (packed float3) and colour staging -> sorted slots through src
-// (null source: zeros)
-int fl_launch_gather_late(fl_system *s, const float *vel3, const uint32_t *clr, float4 *vel_out,
-                          uint32_t *clr_out);
+// late (mode 1, plain systems): the gather moves positions only and leaves
+// velocities, evaluated velocities and colours to fl_launch_gather_late
+int fl_launch_sort_cells(fl_system *s, int mode, bool late = false);
+// velocity, evaluated velocity (packed float3) and colour staging -> the
+// sorted live copies through src (null source: zeros), and the evaluated
+// velocity half of every pair record; after the density pass
+int fl_launch_gather_late(fl_system *s, const float *vel3, const float *veval3, const uint32_t *clr);
 // one-time kernel attributes (shared memory of the crowded-cell sort)
 int fl_kernels_init(fl_system *s);
 // entries of the crowded-cell list for max_points points (cells above 128)

@@ -327,7 +327,7 @@ __device__ __forceinline__ CellCtx cell_ctx(const DevParams &P0, const SceneTab 
 // the canonical within-cell order). The 32 slots of a warp are one word of
 // each slot-flag row, so the warp stores the words whole: rows 0-2 the
 // upper-band flags (ROWS >= 1), rows 3-5 the lower-band flags (ROWS == 2).
-template <bool BATCH, int ROWS, bool VC = true>
+template <bool BATCH, int ROWS, bool LATE = false>
 __global__ void __launch_bounds__(kThreads)
 k_gather_sorted(const __grid_constant__ DevParams P0, const SceneTab T, int n, const uint32_t *__restrict__ src,
                 const uint32_t *__restrict__ cell_pre, const uint32_t *__restrict__ off,
@@ -349,9 +349,11 @@ k_gather_sorted(const __grid_constant__ DevParams P0, const SceneTab T, int n, c
         if (ROWS >= 1) code = band_code(P, local, p);
         p.w = __uint_as_float(code);
         pos_out[s] = p;
-        if (VC) vel_out[s] = vel_in[i];
-        veval_out[s] = veval_in[i];
-        if (VC) clr_out[s] = clr_in[i];
+        if (!LATE) {   // LATE: velocities, evaluated velocities, colours come from k_gather_late
+            vel_out[s] = vel_in[i];
+            veval_out[s] = veval_in[i];
+            clr_out[s] = clr_in[i];
+        }
         gcell_out[s] = (local == P.ncells) ? kUndef : c;
         gndx_out[s] = (uint32_t)s - off[c];
         upwords = (uint32_t)P.upwords;
@@ -368,18 +370,28 @@ k_gather_sorted(const __grid_constant__ DevParams P0, const SceneTab T, int n, c
     }
 }
 
-// The velocities and colours of a step whose state came from host memory
-// (fl_run_from_host), gathered into sorted order after the copy engine has
-// delivered them: packed float3 and uint staging (null: zeros, as
-// fl_set_particles clears an absent field), read through src.
+// The velocities, evaluated velocities and colours of a step whose state
+// came from host memory (fl_run_from_host), gathered into sorted order once
+// the copy engine has delivered them: packed float3 and uint staging (null:
+// zeros, as fl_set_particles clears an absent field), read through src. The
+// evaluated velocity also completes slot s's pair record (the density pass
+// ran before it arrived and wrote only the record's first half correctly).
+__device__ __forceinline__ float4 load3_or_zero(const float *__restrict__ a, uint32_t i) {
+    return a ? make_float4(a[3 * (size_t)i], a[3 * (size_t)i + 1], a[3 * (size_t)i + 2], 0.0f)
+             : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
 __global__ void __launch_bounds__(kThreads)
 k_gather_late(int n, const uint32_t *__restrict__ src, const float *__restrict__ vel3,
-              const uint32_t *__restrict__ clr, float4 *__restrict__ vel_out, uint32_t *__restrict__ clr_out) {
+              const float *__restrict__ veval3, const uint32_t *__restrict__ clr, float4 *__restrict__ vel_out,
+              float4 *__restrict__ veval_out, uint32_t *__restrict__ clr_out, float4 *__restrict__ pairdata) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const uint32_t i = src[s];
-    vel_out[s] = vel3 ? make_float4(vel3[3 * (size_t)i], vel3[3 * (size_t)i + 1], vel3[3 * (size_t)i + 2], 0.0f)
-                      : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    vel_out[s] = load3_or_zero(vel3, i);
+    const float4 e = load3_or_zero(veval3, i);
+    veval_out[s] = e;
+    pairdata[2 * (size_t)s + 1] = e;
     clr_out[s] = clr ? clr[i] : 0u;
 }
 
@@ -1004,7 +1016,7 @@ int fl_kernels_init(fl_system *s) {
 
 size_t fl_big_cells_cap(int max_points) { return (size_t)(max_points > 0 ? max_points : 1) / 129 + 1; }
 
-int fl_launch_sort_cells(fl_system *s, int mode, bool move_vel_clr) {
+int fl_launch_sort_cells(fl_system *s, int mode, bool late) {
     SortArgs a = {};
     a.off = s->off; a.cnt = s->cnt; a.src = s->src; a.scratch = s->rank_tmp;
     a.big_cells = s->big_cells; a.big_count = s->big_count;
@@ -1037,9 +1049,9 @@ int fl_launch_sort_cells(fl_system *s, int mode, bool move_vel_clr) {
     FL_LAUNCH_CHECK("sort_big");
     if (s->n > 0) {
         const int rows = s->D.prune ? mode : 0;
-        if (!move_vel_clr && (s->batched || rows == 2))
-            return fl_fail(FL_ERR_STATE, "sort: deferred velocities only on a plain system's step");
-        auto gather = !move_vel_clr ? (rows == 1 ? k_gather_sorted<false, 1, false> : k_gather_sorted<false, 0, false>)
+        if (late && (s->batched || rows == 2))
+            return fl_fail(FL_ERR_STATE, "sort: late velocities only on a plain system's step");
+        auto gather = late ? (rows == 1 ? k_gather_sorted<false, 1, true> : k_gather_sorted<false, 0, true>)
                       : s->batched ? (rows == 2 ? k_gather_sorted<true, 2>
                                                 : rows == 1 ? k_gather_sorted<true, 1> : k_gather_sorted<true, 0>)
                                    : (rows == 2 ? k_gather_sorted<false, 2>
@@ -1055,10 +1067,11 @@ int fl_launch_sort_cells(fl_system *s, int mode, bool move_vel_clr) {
     return FL_OK;
 }
 
-int fl_launch_gather_late(fl_system *s, const float *vel3, const uint32_t *clr, float4 *vel_out,
-                          uint32_t *clr_out) {
+int fl_launch_gather_late(fl_system *s, const float *vel3, const float *veval3, const uint32_t *clr) {
     if (s->n == 0) return FL_OK;
-    k_gather_late<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(s->n, s->src, vel3, clr, vel_out, clr_out);
+    k_gather_late<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(
+        s->n, s->src, vel3, veval3, clr, s->f[F_VEL].cur<float4>(), s->f[F_VEVAL].cur<float4>(),
+        s->f[F_CLR].cur<uint32_t>(), s->pairdata);
     FL_LAUNCH_CHECK("gather_late");
     return FL_OK;
 }

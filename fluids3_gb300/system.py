@@ -272,8 +272,8 @@ class FluidSystem:
     def RunFromHost(self, pos, vel=None, veval=None, clr=None) -> None:
         """TransferToCUDA + Run in one call (fl_run_from_host): the state from
         host arrays, then one step; equal to SetParticles + Run. Arrays in
-        page-locked memory (PinnedArray) let the velocity and colour uploads
-        overlap the step's first kernels."""
+        page-locked memory (PinnedArray) let the uploads of everything but
+        the positions overlap the step's first kernels."""
         pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
         n = pos.shape[0]
 

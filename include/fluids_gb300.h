@@ -203,8 +203,8 @@ int fl_add_particles(fl_system *s, int k, const float *pos, const float *vel, co
  * the step is done, so the arrays may be reused at once. Results equal
  * fl_set_particles (force and density absent) followed by fl_run, bit for
  * bit. With every given array in page-locked memory (fl_host_alloc) on a
- * single-scene system, positions and evaluated velocities are read over the
- * host link first and velocities and colours follow on a copy engine while
+ * single-scene system, the positions are read over the host link first and
+ * velocities, evaluated velocities and colours follow on a copy engine while
  * the insert, sort and density kernels run. */
 int fl_run_from_host(fl_system *s, int n, const float *pos, const float *vel, const float *veval,
                      const uint32_t *clr);
