@@ -17,10 +17,10 @@ crowded-cell sort), gather, density, force + advance (eight kernels).
           any implementation; segments keep every timed step in the
           configured regime.
   e2e     the same metric through the public C ABI with host buffers: per
-          step, fl_run_from_host (the step's inputs uploaded from pinned host
-          memory, then the step; all but the positions arrive on a copy
-          engine during the step's first kernels) and a device -> host read
-          of the positions (fl_get_buffer)
+          step one fl_run_from_host call -- the step's inputs uploaded from
+          pinned host memory (all but the positions on a copy engine during
+          the step's first kernels), the step, and the new positions read
+          back into pinned host memory (in slot ranges during the force pass)
   roofline  the dominant kernel's algorithmic bytes per launch / its mean
           launch time (per-phase CUDA events over a second K-step region)
   cpu_baseline  the reference's CPU path (the reference kernels built for the
@@ -716,8 +716,8 @@ def our_arm(args, rank, world, local_rank):
 
     def e2e_step():
         F._lib.check("fl_run_from_host", lib.fl_run_from_host(
-            s.handle, n, vp(pin_pos.array), vp(pin_vel.array), vp(pin_vev.array), vp(pin_clr.array)))
-        F._lib.check("fl_get_buffer", lib.fl_get_buffer(s.handle, F.FPOS, vp(pin_out.array), d2h))
+            s.handle, n, vp(pin_pos.array), vp(pin_vel.array), vp(pin_vev.array), vp(pin_clr.array),
+            vp(pin_out.array)))
 
     e2e_step()   # untimed warm-up: first uploads, the captured step graph released
     barrier()

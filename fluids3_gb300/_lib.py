@@ -50,7 +50,7 @@ SIGNATURES = [
     ("fl_compute_force", C.c_int, [vp]),
     ("fl_advance", C.c_int, [vp, C.c_float, C.c_float, C.c_float]),
     ("fl_run", C.c_int, [vp]),
-    ("fl_run_from_host", C.c_int, [vp, C.c_int, vp, vp, vp, vp]),
+    ("fl_run_from_host", C.c_int, [vp, C.c_int, vp, vp, vp, vp, vp]),
     ("fl_run_steps", C.c_int, [vp, C.c_int]),
     ("fl_checkpoint_save", C.c_int, [vp, C.c_int]),
     ("fl_checkpoint_restore", C.c_int, [vp, C.c_int]),

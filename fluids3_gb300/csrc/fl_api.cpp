@@ -12,6 +12,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <map>
 #include <vector>
 
@@ -161,6 +162,8 @@ static void free_all(fl_system *s) {
         if (s->ev[k]) cudaEventDestroy(s->ev[k]);
     if (s->ev_early) cudaEventDestroy(s->ev_early);
     if (s->ev_late) cudaEventDestroy(s->ev_late);
+    for (int k = 0; k < 4; k++)
+        if (s->ev_chunk[k]) cudaEventDestroy(s->ev_chunk[k]);
     if (s->side) cudaStreamDestroy(s->side);
     if (s->stream) cudaStreamDestroy(s->stream);
 }
@@ -924,7 +927,8 @@ extern "C" int fl_run(fl_system *s) {
 // fills (ev_late), just before the force pass, their first reader (the
 // density pass reads only positions; the evaluated-velocity half of its
 // pair records is completed by the late gather).
-static int run_step_late(fl_system *s, const float *vel3, const float *veval3, const uint32_t *clr) {
+static int run_step_late(fl_system *s, const float *vel3, const float *veval3, const uint32_t *clr,
+                         float *pos_out) {
     FL_TRY(clear_grid(s));
     FL_TRY(fl_launch_insert(s, nullptr));
     FL_TRY(fl_launch_scan(s, s->gcells, 0));
@@ -934,7 +938,28 @@ static int run_step_late(fl_system *s, const float *vel3, const float *veval3, c
     FL_TRY(fl_launch_density(s));
     FL_CUDA_TRY(cudaStreamWaitEvent(s->stream, s->ev_late, 0));
     FL_TRY(fl_launch_gather_late(s, vel3, veval3, clr));
-    FL_TRY(fl_launch_force_advance(s, s->P.dt));
+    if (!pos_out) {
+        FL_TRY(fl_launch_force_advance(s, s->P.dt));
+    } else {
+        // the force pass in up to four slot ranges of whole blocks; as each
+        // ends, the side stream packs its new positions and a copy engine
+        // takes them to pos_out while the next range computes
+        const int bs = fl_force_block(s);
+        const int nblk = (s->n + bs - 1) / bs;
+        const int chunks = std::max(1, std::min(4, s->n / (1 << 20)));
+        const float4 *pnew = s->f[F_POS].nxt<float4>();
+        float *stage = (float *)s->stage;
+        for (int c = 0; c < chunks; c++) {
+            const int b = (int)((long long)nblk * c / chunks) * bs;
+            const int e = (c + 1 == chunks) ? s->n : (int)((long long)nblk * (c + 1) / chunks) * bs;
+            FL_TRY(fl_launch_force_advance(s, s->P.dt, b, e));
+            FL_CUDA_TRY(cudaEventRecord(s->ev_chunk[c], s->stream));
+            FL_CUDA_TRY(cudaStreamWaitEvent(s->side, s->ev_chunk[c], 0));
+            FL_TRY(fl_launch_pack3(s, pnew + b, stage + 3 * (size_t)b, e - b, s->side));
+            FL_CUDA_TRY(cudaMemcpyAsync(pos_out + 3 * (size_t)b, stage + 3 * (size_t)b, 12 * (size_t)(e - b),
+                                        cudaMemcpyDeviceToHost, s->side));
+        }
+    }
     flip(s, F_POS); flip(s, F_VEVAL);
     s->codes_valid = 0;
     s->lists_valid = 0;
@@ -943,9 +968,17 @@ static int run_step_late(fl_system *s, const float *vel3, const float *veval3, c
 }
 
 static int ensure_side(fl_system *s) {
-    if (!s->side) FL_CUDA_TRY(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+    if (!s->side) {
+        // the highest priority, so the readback's pack kernels take SMs as the
+        // running force blocks retire instead of queueing behind the next range
+        int least = 0, greatest = 0;
+        FL_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        FL_CUDA_TRY(cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, greatest));
+    }
     if (!s->ev_early) FL_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_early, cudaEventDisableTiming));
     if (!s->ev_late) FL_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_late, cudaEventDisableTiming));
+    for (int k = 0; k < 4; k++)
+        if (!s->ev_chunk[k]) FL_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_chunk[k], cudaEventDisableTiming));
     return FL_OK;
 }
 
@@ -958,7 +991,7 @@ static int ensure_side(fl_system *s) {
 // fl_set_particles followed by fl_run, bit for bit; other host memory, a
 // batched system, a recording tape or phase timing take that path.
 extern "C" int fl_run_from_host(fl_system *s, int n, const float *pos, const float *vel, const float *veval,
-                                const uint32_t *clr) {
+                                const uint32_t *clr, float *pos_out) {
     if (!s || !pos) return fl_fail(FL_ERR_ARG, "fl_run_from_host: null system or pos");
     if (n < 0) return fl_fail(FL_ERR_ARG, "fl_run_from_host: n < 0");
     if (n > s->max_points)
@@ -966,10 +999,11 @@ extern "C" int fl_run_from_host(fl_system *s, int n, const float *pos, const flo
     const void *mpos = mapped_device_ptr(pos);
     const void *mvev = veval ? mapped_device_ptr(veval) : nullptr;
     const bool pinned = mpos && (!veval || mvev) && (!vel || mapped_device_ptr(vel)) &&
-                        (!clr || mapped_device_ptr(clr));
+                        (!clr || mapped_device_ptr(clr)) && (!pos_out || mapped_device_ptr(pos_out));
     if (n == 0 || !pinned || s->batched || s->timing || fl_tape_recording(s)) {
         FL_TRY(fl_set_particles(s, n, pos, vel, veval, nullptr, nullptr, clr));
         FL_TRY(fl_run(s));
+        if (pos_out) FL_TRY(fl_get_buffer(s, FL_FPOS, pos_out, 12 * (size_t)n));
         FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
         return FL_OK;
     }
@@ -997,9 +1031,12 @@ extern "C" int fl_run_from_host(fl_system *s, int n, const float *pos, const flo
     FL_CUDA_TRY(cudaEventRecord(s->ev_late, s->side));
     fl_reset_progress(s);
     FL_TRY(begin_run(s));
-    const int r = run_step_late(s, stage_vel, stage_vev, stage_clr);
-    // the host arrays are the caller's again once the step is done
-    const cudaError_t e = cudaStreamSynchronize(s->stream);
+    const int r = run_step_late(s, stage_vel, stage_vev, stage_clr, pos_out);
+    // the host arrays are the caller's again once the step (and the
+    // readback on the side stream) is done
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    const cudaError_t e2 = cudaStreamSynchronize(s->side);
+    if (e == cudaSuccess) e = e2;
     FL_TRY(r);
     if (e != cudaSuccess) return fl_fail(FL_ERR_CUDA, "fl_run_from_host: %s", cudaGetErrorString(e));
     if (s->time_host_valid) s->time += s->P.dt;   // AdvanceTime (cpp:529), same float add

@@ -175,6 +175,7 @@ struct fl_system {
     // (created on first use)
     cudaStream_t side;
     cudaEvent_t ev_early, ev_late;
+    cudaEvent_t ev_chunk[4];   // force-pass chunks whose positions go back while the next computes
 
     // per-phase event timing (PERF_PUSH/PERF_POP of Run, cpp:507-515)
     int timing;
@@ -260,9 +261,12 @@ int fl_launch_gather_all(fl_system *s);
 int fl_launch_band_codes(fl_system *s);
 int fl_launch_density(fl_system *s);
 int fl_launch_force(fl_system *s);
-int fl_launch_force_advance(fl_system *s, float dt);
+// slots [begin, end) (end < 0: n); both whole blocks of fl_force_block(s)
+// threads, except end == n
+int fl_launch_force_advance(fl_system *s, float dt, int begin = 0, int end = -1);
+int fl_force_block(const fl_system *s);
 int fl_launch_advance(fl_system *s, float time, float dt, float ss);
-int fl_launch_pack3(fl_system *s, const float4 *src, float *dst, int n);
+int fl_launch_pack3(fl_system *s, const float4 *src, float *dst, int n, cudaStream_t stream = nullptr);
 int fl_launch_set_time(fl_system *s, int slot, float value);
 int fl_launch_unpack3(fl_system *s, const float *src, float4 *dst, int n);
 // up to 4 float3 -> float4 fields in one pass (src[k] may be host-mapped)

@@ -792,8 +792,8 @@ k_force_advance(const __grid_constant__ DevParams P0, const SceneTab T, int n, f
                 const uint32_t *__restrict__ hitlist, const uint32_t *__restrict__ hitcnt,
                 const float4 *__restrict__ pairdata, float4 *__restrict__ vel, float4 *__restrict__ force,
                 float4 *__restrict__ pos_out, float4 *__restrict__ veval_out,
-                uint32_t *__restrict__ err) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+                uint32_t *__restrict__ err, int base) {
+    const int i = base + blockIdx.x * blockDim.x + threadIdx.x;   // base: a whole number of blocks
     const float time = time_dev[slot];
     if (i == 0) time_dev[slot ^ 1] = time + dt;
     const DevParams &P = (BATCH && i < n) ? T.params[T.point_scene[i]] : P0;
@@ -1149,18 +1149,24 @@ int fl_launch_force(fl_system *s) {
     return FL_OK;
 }
 
-int fl_launch_force_advance(fl_system *s, float dt) {
+int fl_force_block(const fl_system *s) { return s->blk_force ? s->blk_force : kForceThreads; }
+
+int fl_launch_force_advance(fl_system *s, float dt, int begin, int end) {
     const bool pr = use_prune(s);
     auto kern = s->lists_valid
                     ? (s->batched ? force_advance_kernel<true, true>(pr) : force_advance_kernel<true, false>(pr))
                     : (s->batched ? force_advance_kernel<false, true>(pr) : force_advance_kernel<false, false>(pr));
-    const int bs = s->blk_force ? s->blk_force : kForceThreads;
-    kern<<<blocks_for(s->n > 0 ? s->n : 1, bs), bs, 0, s->stream>>>(
+    const int bs = fl_force_block(s);
+    if (end < 0) end = s->n;
+    if (begin % bs != 0 || (end != s->n && end % bs != 0) || begin > end)
+        return fl_fail(FL_ERR_ARG, "force_advance: slot range [%d, %d) not in whole blocks of %d", begin, end, bs);
+    const int count = end - begin;
+    kern<<<blocks_for(count > 0 ? count : 1, bs), bs, 0, s->stream>>>(
         s->D, fl_scene_tab(s), s->n, s->time_dev, s->time_slot, dt, s->f[F_POS].cur<float4>(),
         s->f[F_VEVAL].cur<float4>(), s->f[F_PRESS].cur<float>(), s->f[F_GCELL].cur<uint32_t>(), s->off,
         s->cnt, s->upbits, s->hitlist, s->hitcnt, s->pairdata,
         s->f[F_VEL].cur<float4>(), s->f[F_FORCE].cur<float4>(),
-        s->f[F_POS].nxt<float4>(), s->f[F_VEVAL].nxt<float4>(), s->dev_err);
+        s->f[F_POS].nxt<float4>(), s->f[F_VEVAL].nxt<float4>(), s->dev_err, begin);
     FL_LAUNCH_CHECK("force_advance");
     return FL_OK;
 }
@@ -1181,9 +1187,9 @@ int fl_launch_set_time(fl_system *s, int slot, float value) {
     return FL_OK;
 }
 
-int fl_launch_pack3(fl_system *s, const float4 *src, float *dst, int n) {
+int fl_launch_pack3(fl_system *s, const float4 *src, float *dst, int n, cudaStream_t stream) {
     if (n == 0) return FL_OK;
-    k_pack3<<<blocks_for(n, kThreads), kThreads, 0, s->stream>>>(n, src, dst);
+    k_pack3<<<blocks_for(n, kThreads), kThreads, 0, stream ? stream : s->stream>>>(n, src, dst);
     FL_LAUNCH_CHECK("pack3");
     return FL_OK;
 }

@@ -269,11 +269,12 @@ class FluidSystem:
         """One RUN_GPU_FULL step (cpp:506-524) on the fused kernels, then time += dt."""
         call("fl_run", self._h)
 
-    def RunFromHost(self, pos, vel=None, veval=None, clr=None) -> None:
-        """TransferToCUDA + Run in one call (fl_run_from_host): the state from
-        host arrays, then one step; equal to SetParticles + Run. Arrays in
-        page-locked memory (PinnedArray) let the uploads of everything but
-        the positions overlap the step's first kernels."""
+    def RunFromHost(self, pos, vel=None, veval=None, clr=None, pos_out=None) -> None:
+        """TransferToCUDA + Run (+ the new positions into pos_out, an (N,3)
+        float32 array) in one call (fl_run_from_host); equal to SetParticles
+        + Run (+ GetBuffer(FPOS)). Arrays in page-locked memory (PinnedArray)
+        let the uploads of everything but the positions overlap the step's
+        first kernels and the readback overlap its force pass."""
         pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
         n = pos.shape[0]
 
@@ -281,7 +282,10 @@ class FluidSystem:
             return None if a is None else np.ascontiguousarray(a, dtype=np.float32).reshape(n, 3)
 
         c = None if clr is None else np.ascontiguousarray(clr, dtype=np.uint32).reshape(n)
-        arrs = (pos, f3(vel), f3(veval), c)
+        if pos_out is not None and (pos_out.dtype != np.float32 or pos_out.shape != (n, 3)
+                                    or not pos_out.flags.c_contiguous):
+            raise ValueError("pos_out must be a C-contiguous (N, 3) float32 array")
+        arrs = (pos, f3(vel), f3(veval), c, pos_out)
         call("fl_run_from_host", self._h, n, *[_ptr(a) for a in arrs])
 
     def RunSteps(self, nsteps: int) -> None:

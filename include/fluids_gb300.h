@@ -20,7 +20,7 @@
  *   ComputeForceCUDA (cpp:2521-2525)               fl_compute_force
  *   AdvanceCUDA (cpp:2527-2531)                    fl_advance
  *   Run, case RUN_GPU_FULL (cpp:506-524)           fl_run / fl_run_steps
- *   TransferToCUDA + Run                           fl_run_from_host
+ *   TransferToCUDA + Run + TransferFromCUDA        fl_run_from_host
  *   IntegrityCheck (cpp:2426-2453)                 fl_integrity_check
  *
  * Errors: every call returns FL_OK (0) or a negative FL_ERR_* code and never
@@ -197,17 +197,20 @@ int fl_set_particles(fl_system *s, int n, const float *pos, const float *vel,
 int fl_add_particles(fl_system *s, int k, const float *pos, const float *vel, const float *veval,
                      const uint32_t *clr);
 
-/* TransferToCUDA + Run (cpp:2312-2321, 506-524) in one call, for a state
- * kept in host memory between steps: n points from host SoA arrays (pos
- * required; vel, veval, clr may be NULL: zero), then one step; returns when
- * the step is done, so the arrays may be reused at once. Results equal
- * fl_set_particles (force and density absent) followed by fl_run, bit for
- * bit. With every given array in page-locked memory (fl_host_alloc) on a
- * single-scene system, the positions are read over the host link first and
- * velocities, evaluated velocities and colours follow on a copy engine while
- * the insert, sort and density kernels run. */
+/* TransferToCUDA + Run + TransferFromCUDA's positions (cpp:2312-2330,
+ * 506-524) in one call, for a state kept in host memory between steps: n
+ * points from host SoA arrays (pos required; vel, veval, clr may be NULL:
+ * zero), one step, and, when pos_out is given, the new positions into it
+ * (n x float3, what fl_get_buffer(FL_FPOS) returns). Returns when all of it
+ * is done, so the arrays may be reused at once. Results equal
+ * fl_set_particles (force and density absent), fl_run and fl_get_buffer,
+ * bit for bit. With every given array in page-locked memory (fl_host_alloc)
+ * on a single-scene system, the positions are read over the host link
+ * first, velocities, evaluated velocities and colours follow on a copy
+ * engine while the insert, sort and density kernels run, and the new
+ * positions go back in slot ranges while the force pass computes the next. */
 int fl_run_from_host(fl_system *s, int n, const float *pos, const float *vel, const float *veval,
-                     const uint32_t *clr);
+                     const uint32_t *clr, float *pos_out);
 
 /* Copy buffer `buf_id` (FL_F* id) into host memory in fluid.h layout.
  * `bytes` must be at least the buffer size (N or C elements). */

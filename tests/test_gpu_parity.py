@@ -655,21 +655,24 @@ def test_run_from_host_equals_set_particles_then_run(case):
     with_vc = case != "no_vel_no_clr"
     pins = {}
     if case != "pageable":
-        pins = {k: F.PinnedArray((n, 3), np.float32) for k in ("pos", "vel", "veval")}
+        pins = {k: F.PinnedArray((n, 3), np.float32) for k in ("pos", "vel", "veval", "out")}
         pins["clr"] = F.PinnedArray((n,), np.uint32)
+    out = pins["out"].array if pins else np.empty((n, 3), np.float32)
     try:
         with F.FluidSystem(sc.params, n) as a, F.FluidSystem(sc.params, n) as b:
             for it in range(3):
                 if pins:
-                    for k, p in pins.items():
-                        p.array[:] = host[k]
+                    for k in host:
+                        pins[k].array[:] = host[k]
                 src = {k: (pins[k].array if pins else host[k]) for k in host}
                 a.SetParticles(host["pos"], host["vel"] if with_vc else None, host["veval"],
                                clr=host["clr"] if with_vc else None)
                 a.Run()
                 b.RunFromHost(src["pos"], src["vel"] if with_vc else None, src["veval"],
-                              clr=src["clr"] if with_vc else None)
+                              clr=src["clr"] if with_vc else None, pos_out=out if it != 1 else None)
                 sa, sb = gpu_state(a), gpu_state(b)
+                if it != 1:
+                    assert_bit_equal(out, sa["pos"], f"call {it}: positions read back")
                 for k in FIELDS + ("gridcnt", "gridoff"):
                     assert_bit_equal(sb[k], sa[k], f"call {it}: {k}")
                 assert a.time == b.time
@@ -677,6 +680,32 @@ def test_run_from_host_equals_set_particles_then_run(case):
             a.RunSteps(2)
             b.RunSteps(2)
             assert_bit_equal(b.GetBuffer(F.FPOS), a.GetBuffer(F.FPOS), "steps after")
+    finally:
+        for p in pins.values():
+            p.free()
+
+
+def test_run_from_host_reads_back_in_slot_ranges():
+    """Above 2^21 points the force pass of fl_run_from_host runs in slot
+    ranges whose positions go back while the next range computes: the
+    positions read back and the state still equal SetParticles + Run +
+    GetBuffer."""
+    sc = scenes.wave_tank(n=2_200_000)
+    n = sc.n
+    pins = {k: F.PinnedArray((n, 3), np.float32) for k in ("pos", "vel", "veval", "out")}
+    pins["clr"] = F.PinnedArray((n,), np.uint32)
+    try:
+        for k, a in (("pos", sc.pos), ("vel", sc.vel), ("veval", sc.veval), ("clr", sc.clr)):
+            pins[k].array[:] = a
+        with F.FluidSystem(sc.params, n) as a, F.FluidSystem(sc.params, n) as b:
+            a.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
+            a.Run()
+            b.RunFromHost(pins["pos"].array, pins["vel"].array, pins["veval"].array, clr=pins["clr"].array,
+                          pos_out=pins["out"].array)
+            sa, sb = gpu_state(a), gpu_state(b)
+            assert_bit_equal(pins["out"].array, sa["pos"], "positions read back")
+            for k in FIELDS:
+                assert_bit_equal(sb[k], sa[k], k)
     finally:
         for p in pins.values():
             p.free()
