@@ -1172,25 +1172,32 @@ extern "C" int fl_autotune(fl_system *s, int steps, int *chosen) {
     FL_CUDA_TRY(cudaEventCreate(&e0));
     cudaError_t ce = cudaEventCreate(&e1);
     if (ce != cudaSuccess) { cudaEventDestroy(e0); return fl_fail(FL_ERR_CUDA, "fl_autotune: event"); }
+    // one knob at a time; its candidates timed in three interleaved rounds,
+    // each keeping its fastest (shapes differ by a few percent, about the
+    // spread of a single short measurement)
     int r = FL_OK;
     for (int k = 0; k < 4 && r == FL_OK; k++) {
-        int best = 0;
-        float best_ms = 0.0f;
-        for (int c = 0; c < 4 && cand[k][c] && r == FL_OK; c++) {
-            *knob[k] = cand[k][c];
-            destroy_graph(s);
-            if ((r = restore_slot(s, slot)) != FL_OK) break;
-            if ((r = fl_run(s)) != FL_OK) break;            // warm: first launch of this shape
-            if ((r = restore_slot(s, slot)) != FL_OK) break;
-            cudaEventRecord(e0, s->stream);
-            for (int t = 0; t < steps && r == FL_OK; t++) r = fl_run(s);
-            cudaEventRecord(e1, s->stream);
-            if (cudaEventSynchronize(e1) != cudaSuccess) { r = fl_fail(FL_ERR_CUDA, "fl_autotune: timing"); break; }
-            float ms = 0.0f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            if (best == 0 || ms < best_ms) { best = cand[k][c]; best_ms = ms; }
+        float min_ms[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        for (int round = 0; round < 3 && r == FL_OK; round++) {
+            for (int c = 0; c < 4 && cand[k][c] && r == FL_OK; c++) {
+                *knob[k] = cand[k][c];
+                destroy_graph(s);
+                if ((r = restore_slot(s, slot)) != FL_OK) break;
+                if (round == 0 && (r = fl_run(s)) != FL_OK) break;   // warm: first launch of this shape
+                if (round == 0 && (r = restore_slot(s, slot)) != FL_OK) break;
+                cudaEventRecord(e0, s->stream);
+                for (int t = 0; t < steps && r == FL_OK; t++) r = fl_run(s);
+                cudaEventRecord(e1, s->stream);
+                if (cudaEventSynchronize(e1) != cudaSuccess) { r = fl_fail(FL_ERR_CUDA, "fl_autotune: timing"); break; }
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (round == 0 || ms < min_ms[c]) min_ms[c] = ms;
+            }
         }
-        *knob[k] = best;
+        int best = 0;
+        for (int c = 0; c < 4 && cand[k][c]; c++)
+            if (best == 0 || min_ms[c] < min_ms[best - 1]) best = c + 1;
+        *knob[k] = cand[k][best - 1];
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
