@@ -201,8 +201,9 @@ int fl_add_particles(fl_system *s, int k, const float *pos, const float *vel, co
  * 506-524) in one call, for a state kept in host memory between steps: n
  * points from host SoA arrays (pos required; vel, veval, clr may be NULL:
  * zero), one step, and, when pos_out is given, the new positions into it
- * (n x float3, what fl_get_buffer(FL_FPOS) returns). Returns when all of it
- * is done, so the arrays may be reused at once. Results equal
+ * (n x float3, what fl_get_buffer(FL_FPOS) returns; it may be pos itself,
+ * which is read in full before any new position is written). Returns when
+ * all of it is done, so the arrays may be reused at once. Results equal
  * fl_set_particles (force and density absent), fl_run and fl_get_buffer,
  * bit for bit. With every given array in page-locked memory (fl_host_alloc)
  * on a single-scene system, the positions are read over the host link

@@ -709,3 +709,27 @@ def test_run_from_host_reads_back_in_slot_ranges():
     finally:
         for p in pins.values():
             p.free()
+
+
+def test_run_from_host_writes_positions_back_in_place():
+    """pos_out may be the positions array itself (a state kept in host
+    memory, updated in place each step): equal to SetParticles + Run +
+    GetBuffer, call after call."""
+    sc = scenes.wave_tank(n=60_000)
+    n = sc.n
+    pins = {k: F.PinnedArray((n, 3), np.float32) for k in ("pos", "vel", "veval")}
+    try:
+        for k, a in (("pos", sc.pos), ("vel", sc.vel), ("veval", sc.veval)):
+            pins[k].array[:] = a
+        with F.FluidSystem(sc.params, n) as a, F.FluidSystem(sc.params, n) as b:
+            pos = sc.pos.copy()
+            for it in range(3):
+                a.SetParticles(pos, sc.vel, sc.veval)
+                a.Run()
+                pos = a.GetBuffer(F.FPOS)
+                b.RunFromHost(pins["pos"].array, pins["vel"].array, pins["veval"].array,
+                              pos_out=pins["pos"].array)
+                assert_bit_equal(pins["pos"].array, pos, f"call {it}")
+    finally:
+        for p in pins.values():
+            p.free()
