@@ -307,6 +307,29 @@ def reference_gpu_rate(scene, warm: dict, t_start: float, steps: int, segment: i
             "value_over_reference": value / rate}
 
 
+def reference_gpu_rollout_ms(sc, steps: int):
+    """Milliseconds per step of the reference's own GPU kernels over the same
+    rollout from the same start (its Run per step, cuCtxSynchronize included;
+    CUDA events on the default stream); None where the module is absent."""
+    from oracle import ref_gpu as R
+
+    if not R.available() or steps <= 0:
+        return None
+    import torch
+    with R.RefGpu(sc.params, sc.n) as ref:
+        ref.set_state(sc.pos, sc.vel, sc.veval, sc.clr)
+        ref.run(0.0)                                   # the module's first launches
+        ref.set_state(sc.pos, sc.vel, sc.veval, sc.clr)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t = 0.0
+        e0.record()
+        for _ in range(steps):
+            t = ref.run(t)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+
 def reference_arm(args, rank, world):
     """The reference's CPU implementation of the step on this machine's host cores.
     A step is one full step over a bounded sample of the workload -- its first
@@ -517,6 +540,7 @@ def adjoint_measurements(args):
         "workload": f"{sc.name}: 65,536-point dam break, box scaled x1.26 (same density as the 32,768-point "
                     f"scene), {T} steps; loss vs the initial block shifted 0.3 box widths in +x",
         "steps": T, "forward_ms_per_step": ms_fwd,
+        "reference_gpu_forward_ms_per_step": reference_gpu_rollout_ms(sc, T),
         "system_bytes": (free_before - free_sys) if free_before is not None else None,
         "checkpointed": runs[(every_k, False)], "checkpointed_kept_lists": runs[(every_k, True)],
         "every_step": runs[(1, False)] if (1, False) in runs else runs[(every_k, False)],
