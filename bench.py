@@ -776,6 +776,7 @@ def our_arm(args, rank, world, local_rank):
                 "bound_observed": rec.get("bound_observed"),
                 "issue_active_pct_ncu": rec.get("issue_active_pct"),
                 "issue_roofline_frac_ncu": rec.get("issue_roofline_frac"),
+                "fp32_fma_pipe_pct_ncu": rec.get("fp32_fma_pipe_pct"),
                 "issue_roofline_note": "warp instructions / (time x 152 SMs x 4 schedulers x SM clock), "
                                        "from the committed ncu capture: the roof this kernel meets",
                 "profile": "profiles/ncu_wave_tank_4m.md"}
