@@ -59,16 +59,19 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "Mparticle-steps/s"
-# Algorithmic bytes per point per kernel: each input read once, each output
-# written once (canonical figures; grid terms per cell are added separately).
+# Algorithmic bytes per point per phase of the step: each input read once,
+# each output written once (the per-unit figures of the step's functions;
+# grid terms per cell are added separately): 256 B per point in all.
 ALGO_BYTES = {
     "insert": 20,          # R pos 12, W cell + rank 8
     "scan": 0,             # per cell: R 4, W 4 (+ clear 4) -> 12 B/cell
-    "scatter": 12,         # R cell + rank 8, W src 4
-    "sort": 92,            # cell sort + gather: R pos, vel, veval, clr, gcell, gndx; W pos, vel, veval, clr, gcell
+    "sort": 92,            # R pos, vel, veval, clr, gcell, gndx; W pos, vel, veval, clr, gcell
     "density": 16,         # R pos 12, W density 4
     "force_advance": 128,  # force 40 (R pos, veval, density; W F) + advance 88
 }
+# Bytes per point this implementation moves beyond those: the index scatter
+# between the counting atomics and the cell sort (R cell + rank, W index).
+IMPL_BYTES = {"scatter": 12}
 KERNELS_PER_STEP = 8   # insert, scan, scatter, cell sort, crowded-cell sort, gather, density, force+advance
 
 
@@ -81,6 +84,8 @@ def parse():
     ap.add_argument("--n", type=int, default=4_000_000, help="points in the wave tank")
     ap.add_argument("--segment", type=int, default=50,
                     help="timed steps run as rollouts of at most this many steps from the warm state")
+    ap.add_argument("--long-steps", type=int, default=0,
+                    help="also time this many continuous steps from the warm state, per 100-step run")
     ap.add_argument("--e2e-steps", type=int, default=None, help="steps in the e2e region (default: min(K, 20))")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -88,7 +93,8 @@ def parse():
                     help="skip timing the reference's own GPU kernels on the same workload")
     ap.add_argument("--batch-scenes", type=int, default=256,
                     help="scenes in the batched-vs-one-at-a-time comparison (0 skips it)")
-    ap.add_argument("--batch-steps", type=int, default=20)
+    ap.add_argument("--batch-steps", type=int, default=500,
+                    help="continuous steps of the batched comparison")
     ap.add_argument("--adjoint-steps", type=int, default=200,
                     help="steps of the differentiated 65,536-point rollout (0 skips the adjoint section)")
     ap.add_argument("--adjoint-every", type=int, default=20, help="checkpoint interval of that rollout")
@@ -243,7 +249,24 @@ def cpu_reference_rate(scene, budget_s: float, threads: int):
                       f"and parameters), {el:.1f} s, {threads} host threads"}, el
 
 
-def reference_gpu_rate(scene, warm: dict, t_start: float, steps: int, segment: int, value: float) -> dict:
+def continuous_profile(s, steps: int, chunk: int = 100) -> dict:
+    """Device time of `steps` continuous steps from the current state, per
+    run of `chunk` steps (graph replay, CUDA events), with the largest cell
+    at the end of each run: how the step cost grows as the fluid clumps."""
+    import fluids3_gb300 as F
+    rows, done, total = [], 0, 0.0
+    while done < steps:
+        k = min(chunk, steps - done)
+        ms = s.TimeSteps(k, graph=True)
+        done += k
+        total += ms
+        rows.append({"steps": done, "ms_per_step": ms / k, "largest_cell": int(s.GetBuffer(F.FGRIDCNT).max())})
+    return {"steps": steps, "ms_total": total, "value": s.NumPoints() * steps / (total / 1e3) / 1e6,
+            "unit": METRIC, "runs": rows}
+
+
+def reference_gpu_rate(scene, warm: dict, t_start: float, steps: int, segment: int, value: float,
+                       value_continuous: float | None = None) -> dict:
     """The reference's own GPU step on this GPU: fluids4.0/fluid_kernels.cu
     built for sm_103a with its build's flags, driven as FluidSystem::Run
     drives it (phase by phase on the default stream, cuCtxSynchronize at the
@@ -276,6 +299,15 @@ def reference_gpu_rate(scene, warm: dict, t_start: float, steps: int, segment: i
             total_ms += ev0.elapsed_time(ev1)
             n_in.append(int(ref.get(R.FGRIDCNT).sum(dtype=np.int64)))
             left -= chunk
+        # the same steps as one continuous trajectory from the warm state
+        ref.set_state(warm["pos"], warm["vel"], warm["veval"], warm["clr"])
+        t = t_start
+        ev0.record()
+        for _ in range(steps):
+            t = ref.run(t)
+        ev1.record()
+        torch.cuda.synchronize()
+        cont_ms = ev0.elapsed_time(ev1)
         # per-phase device times over one segment from the same state: events
         # between the phases of each Run (a separate, untimed pass)
         names = ("insert", "prefix_sum", "counting_sort", "pressure", "force", "advance")
@@ -295,7 +327,10 @@ def reference_gpu_rate(scene, warm: dict, t_start: float, steps: int, segment: i
             for a, name in enumerate(names):
                 acc[name] += evs[a].elapsed_time(evs[a + 1])
     rate = n * steps / (total_ms / 1e3) / 1e6
+    rate_cont = n * steps / (cont_ms / 1e3) / 1e6
     return {"value": rate, "unit": METRIC, "ms_per_step": total_ms / steps, "steps": steps,
+            "value_continuous": rate_cont, "ms_per_step_continuous": cont_ms / steps,
+            "value_continuous_over_reference": (value_continuous / rate_cont) if value_continuous else None,
             "kind": "reference kernels on this GPU",
             "build": "fluids4.0/fluid_kernels.cu, nvcc -gencode arch=compute_103a,code=sm_103a -O3 "
                      "--use_fast_math --maxrregcount=32 (the reference build's flags)",
@@ -339,8 +374,11 @@ def reference_arm(args, rank, world):
         return
     from fluids3_gb300 import scenes
     from oracle import oracle as O
+    from oracle import params_oracle as PO
 
-    scene = scenes.wave_tank(n=args.n)
+    # parameters from the oracle's own restatement of the reference's
+    # derivation: nothing of the product library is loaded in this arm
+    scene = scenes.wave_tank(n=args.n, derive=PO.derive_flparams)
     p = scene.params
     threads = cpu_threads()
     kind = "reference" if O.ref_available() else "port"
@@ -380,37 +418,46 @@ def batched_comparison(args):
     """The batched multi-scene workload: `args.batch_scenes` scenes of
     2,048..65,536 points (log-uniform), each with its own box, grid,
     viscosity and rest density, stepped (a) together as one batched system
-    and (b) one at a time, each as its own plain system -- same steps, same
-    timing protocol (graph replay, segments restarting from the warm state).
-    Every scene's final state is compared bit for bit between (a) and (b)."""
+    and (b) one at a time, each as its own plain system. Both start from the
+    state after the warm-up steps and run `args.batch_steps` continuous steps
+    (graph replay, no restarts) with the same launch shapes: the batch's
+    autotuned shapes, pinned on every plain system. Every scene's final state
+    (positions, velocities, evaluated velocities, cells) is compared bit for
+    bit between (a) and (b)."""
     import fluids3_gb300 as F
     from fluids3_gb300 import scenes
 
     scs = scenes.batch_scenes(args.batch_scenes)
     total = sum(sc.n for sc in scs)
     k = args.batch_steps
-    seg = args.segment
+    warm = max(args.warmup, 3)
     cat = scenes.concat(scs)
     b = F.FluidSystem.batch([sc.params for sc in scs], [sc.n for sc in scs])
     b.SetParticles(cat["pos"], cat["vel"], cat["veval"], clr=cat["clr"])
-    b.RunSteps(max(args.warmup, 3))
-    tuned = b.Autotune(3) if not args.no_autotune else None
+    b.RunSteps(warm)
+    if not args.no_autotune:
+        b.Autotune(3)
+    shapes = b.LaunchShapes()
     b.SaveCheckpoint(0)
     b.RunSteps(2)                       # capture the graph for the tuned shapes
     b.RestoreCheckpoint(0)
-    ms_b = b.TimeSteps(k, graph=True, restart_every=seg, restart_slot=0)
+    ms_b = b.TimeSteps(k, graph=True)
     b.Sync()
     st_b = {f: b.GetBuffer(getattr(F, "F" + f.upper())) for f in ("pos", "vel", "veval", "gcell")}
     infos = [b.SceneInfo(q) for q in range(len(scs))]
+    largest_cell = int(b.GetBuffer(F.FGRIDCNT).max())
     b.close()
     ms_seq = 0.0
     same = 0
     for q, sc in enumerate(scs):
         s = F.FluidSystem(sc.params, sc.n)
         s.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
-        s.RunSteps(max(args.warmup, 3))
+        s.RunSteps(warm)
+        s.SetLaunchShapes(**shapes)
         s.SaveCheckpoint(0)
-        ms_seq += s.TimeSteps(k, graph=True, restart_every=seg, restart_slot=0)
+        s.RunSteps(2)
+        s.RestoreCheckpoint(0)
+        ms_seq += s.TimeSteps(k, graph=True)
         s.Sync()
         a, n = infos[q]["point_base"], infos[q]["n"]
         ok = True
@@ -424,10 +471,12 @@ def batched_comparison(args):
         s.close()
     vb = total * k / (ms_b / 1e3) / 1e6
     vs = total * k / (ms_seq / 1e3) / 1e6
-    return {"scenes": len(scs), "points": total, "steps": k, "value": vb, "unit": METRIC,
+    return {"scenes": len(scs), "points": total, "steps": k, "warmup_steps": warm, "value": vb, "unit": METRIC,
             "one_at_a_time_value": vs, "speedup": vb / vs, "ms_per_step": ms_b / k,
             "one_at_a_time_ms_per_step": ms_seq / k, "scenes_bit_identical": same,
-            "autotuned_block_shapes": tuned, "one_at_a_time_block_shapes": "compiled defaults",
+            "launch_shapes_both": shapes, "largest_cell_at_end": largest_cell,
+            "protocol": f"{k} continuous graph-replayed steps after {warm} warm-up steps, both arms with the "
+                        "batch's autotuned launch shapes; final pos/vel/veval/gcell compared per scene",
             "workload": "scenes log-uniform 2,048..65,536 points, fill U[0.2,0.6] of own box, "
                         "visc U[0.1,0.5], rest density U[500,700], dam-break parameters otherwise"}
 
@@ -685,6 +734,15 @@ def our_arm(args, rank, world, local_rank):
     clocks.stop()
     ms = allmax(dist, ms)
     status = s.DeviceStatus()
+    # the same K steps as one continuous trajectory from the warm state (no
+    # restarts; beside `value`, which restarts every --segment steps)
+    s.RestoreCheckpoint(0)
+    barrier()
+    ms_cont = allmax(dist, s.TimeSteps(args.steps, graph=True))
+    long_run = None
+    if args.long_steps > 0:
+        s.RestoreCheckpoint(0)
+        long_run = continuous_profile(s, args.long_steps)
 
     # -- per-kernel times: the same K steps again from the saved state, eager,
     #    each launch bracketed by CUDA events
@@ -763,7 +821,7 @@ def our_arm(args, rank, world, local_rank):
     adjoint = adjoint_measurements(args) if args.adjoint_steps > 0 else None
     fit = fit_measurement(args) if args.fit_iters > 0 else None
     value = job_value(world, scene.n, args.steps, ms)
-    dominant = max((k for k in phases if k != "scan"), key=lambda k: phases[k])
+    dominant = max((k for k in phases if k in ALGO_BYTES and k != "scan"), key=lambda k: phases[k])
     dur_ms = phases[dominant]
     algo = ALGO_BYTES[dominant] * n_in
     achieved = algo / (dur_ms / 1e3) / 1e9
@@ -780,14 +838,15 @@ def our_arm(args, rank, world, local_rank):
                 "issue_roofline_note": "warp instructions / (time x 152 SMs x 4 schedulers x SM clock), "
                                        "from the committed ncu capture: the roof this kernel meets",
                 "profile": "profiles/ncu_wave_tank_4m.md"}
-    step_bytes = sum(ALGO_BYTES[k] for k in ALGO_BYTES) * n_in + 12 * (p.gridTotal + 1)
+    step_bytes = sum(ALGO_BYTES.values()) * n_in + 12 * (p.gridTotal + 1)
     cpu = None
     if not args.no_cpu_baseline:
         cpu, _ = cpu_reference_rate(scene, args.cpu_seconds, cpu_threads())
     ref_gpu = None
     if warm is not None:
         try:
-            ref_gpu = reference_gpu_rate(scene, warm, warm["time"], args.steps, args.segment, value)
+            ref_gpu = reference_gpu_rate(scene, warm, warm["time"], args.steps, args.segment, value,
+                                         job_value(world, scene.n, args.steps, ms_cont))
         except (OSError, RuntimeError, ValueError) as e:
             ref_gpu = {"unavailable": f"{type(e).__name__}: {e}"}
     line = {
@@ -796,8 +855,13 @@ def our_arm(args, rank, world, local_rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: seeded jittered lattice (splitmix64), no dataset",
         "config": config_of(scene, args),
+        "value_continuous": job_value(world, scene.n, args.steps, ms_cont),
+        "ms_per_step_continuous": ms_cont / args.steps,
+        "long_continuous": long_run,
         "roofline": roofline,
         "step_roofline": {"algorithmic_bytes_per_step": step_bytes,
+                          "bytes_per_point": sum(ALGO_BYTES.values()),
+                          "implementation_bytes_per_point_not_counted": IMPL_BYTES,
                           "achieved_gbs": step_bytes / (ms / args.steps / 1e3) / 1e9,
                           "frac": step_bytes / (ms / args.steps / 1e3) / 1e9 / peak},
         "phases_ms": {k: round(v, 5) for k, v in phases.items()}, "phase_steps": nsteps_timed,

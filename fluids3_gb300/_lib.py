@@ -61,6 +61,8 @@ SIGNATURES = [
     ("fl_time_steps", C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]),
     ("fl_get_phase_times", C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     ("fl_prefix_sum_noalloc", C.c_int, [vp, vp, C.c_int, C.c_int, vp, vp]),
+    ("fl_test_scan_timeout", C.c_int, [vp, C.c_int]),
+    ("fl_test_scan_noalloc_timeout", C.c_int, [vp, vp, C.c_int, vp, C.c_int, vp]),
     ("fl_batch_get_params", C.c_int, [vp, C.c_int, C.POINTER(FlParams)]),
     ("fl_batch_set_params", C.c_int, [vp, C.c_int, C.POINTER(FlParams)]),
     ("fl_add_particles", C.c_int, [vp, C.c_int, vp, vp, vp, vp]),

@@ -75,7 +75,9 @@ __device__ __forceinline__ Walls wall_terms(const DevParams &P, float time, floa
                       __fmul_rn(__fsub_rn(pos.x, P.bound_min.x), P.bound_slope))), ss));
     w.yhi = __fsub_rn(P.pradius, __fmul_rn(__fsub_rn(P.bound_max.y, pos.y), ss));
     w.ph = __fadd_rn(__fmul_rn(time, P.bound_wall_freq), __fdiv_rn(pos.z, 400.f));
-    w.wall = __fmul_rn(__fadd_rn(__fmul_rn(sinf(w.ph), 0.5f), 0.5f), P.bound_wall_force);
+    // the forward forms this product in double (the reference's literals)
+    w.wall = __double2float_rn(__dmul_rn(__dadd_rn(__dmul_rn((double)sinf(w.ph), 0.5), 0.5),
+                                         (double)P.bound_wall_force));
     w.xlo = __fsub_rn(P.pradius, __fmul_rn(__fsub_rn(pos.x, __fadd_rn(P.bound_min.x, w.wall)), ss));
     w.xhi = __fsub_rn(P.pradius, __fmul_rn(__fsub_rn(P.bound_max.x, pos.x), ss));
     w.zlo = __fsub_rn(P.pradius, __fmul_rn(__fsub_rn(pos.z, P.bound_min.z), ss));

@@ -703,8 +703,12 @@ __device__ __forceinline__ void advance_point(const DevParams &P, float time, fl
         accel.y += nrm.y - veval.y * P.bound_friction;
         accel.z += nrm.z - veval.z * P.bound_friction;
     }
-    // X- moving wall (cu:371-377): stiffness scaled by the wall term
-    const float wall = (sinf(time * P.bound_wall_freq + pos.z / 400.f) * 0.5f + 0.5f) * P.bound_wall_force;
+    // X- moving wall (cu:371-377): stiffness scaled by the wall term. The
+    // reference forms `sin(..) * 0.5 + 0.5` and the amplitude product with
+    // double literals, so the product is formed in double and rounded once
+    // to float, as there (three FP64 operations per point).
+    const float wall = (float)(((double)sinf(time * P.bound_wall_freq + pos.z / 400.f) * 0.5 + 0.5) *
+                               (double)P.bound_wall_force);
     diff = P.pradius - (pos.x - (P.bound_min.x + wall)) * ss;
     if (diff > kEpsilon) {
         float3 nrm = make_float3(1.0f, 0.0f, 0.0f);

@@ -12,8 +12,10 @@
 // The host zeroes the descriptors and the ticket before every launch (one
 // memset that also clears the counts in the fused step); the epoch field
 // is a second guard against reading a descriptor left by another launch.
-// Every wait is bounded: after kSpinLimit polls the CTA records
-// FL_DEV_SPIN_TIMEOUT in the device error word and stops waiting.
+// Every wait is bounded: after `spin_limit` polls (kSpinLimit in the step)
+// the CTA records FL_DEV_SPIN_TIMEOUT in the device error word and stops
+// waiting. `first_tile` offsets the ticket (0 in the step); the test hook
+// below uses it to withhold tile 0 so that the wait runs out.
 #include "fl_internal.h"
 
 namespace {
@@ -38,14 +40,15 @@ __device__ __forceinline__ uint64_t pack(uint64_t flag, uint32_t epoch, uint32_t
 
 __global__ void __launch_bounds__(kThreads)
 k_scan(const uint32_t *__restrict__ in, uint32_t *__restrict__ out, uint64_t *status,
-       uint32_t *ticket, int ntiles, uint32_t epoch, int inclusive, uint32_t *err) {
+       uint32_t *ticket, int ntiles, uint32_t epoch, int inclusive, uint32_t *err, int spin_limit,
+       uint32_t first_tile) {
     __shared__ uint32_t s_tile;
     __shared__ uint32_t s_warp[kThreads / 32];
     __shared__ uint32_t s_prefix;
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
 
     if (threadIdx.x == 0) {
-        s_tile = atomicAdd(ticket, 1u);
+        s_tile = first_tile + atomicAdd(ticket, 1u);
     }
     __syncthreads();
     const uint32_t tile = s_tile;
@@ -99,7 +102,7 @@ k_scan(const uint32_t *__restrict__ in, uint32_t *__restrict__ out, uint64_t *st
                     d = ld_acquire(&status[j]);
                     if ((d >> 62) != 0 && (uint32_t)((d >> 32) & 0x3fffffffu) == (epoch & 0x3fffffffu))
                         break;
-                    if (++spins > kSpinLimit) {
+                    if (++spins > spin_limit) {
                         atomicOr(err, FL_DEV_SPIN_TIMEOUT);
                         d = pack(kFlagPrefix, epoch, 0);
                         break;
@@ -147,8 +150,27 @@ int fl_launch_scan(fl_system *s, int count, int clear_status) {
         FL_CUDA_TRY(cudaMemsetAsync(s->scan_ticket, 0, fl_scan_scratch_bytes(s->scan_tiles), s->stream));
     k_scan<<<ntiles, kThreads, 0, s->stream>>>(s->cnt, s->off, s->scan_status, s->scan_ticket,
                                                ntiles, s->scan_epoch, /*inclusive=*/0,
-                                               s->dev_err);
+                                               s->dev_err, kSpinLimit, 0u);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fl_fail(FL_ERR_CUDA, "scan launch: %s", cudaGetErrorString(e));
+    return FL_OK;
+}
+
+// Test hook: the system scan with tile 0 withheld (ntiles - 1 CTAs take
+// tiles 1 .. ntiles - 1, so every index stays in bounds) and a short spin
+// limit, so tile 1's wait for tile 0's descriptor runs out: the kernel
+// records FL_DEV_SPIN_TIMEOUT and returns, and fl_sync reports it.
+extern "C" int fl_test_scan_timeout(fl_system *s, int spin_limit) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_test_scan_timeout: null system");
+    if (spin_limit < 1 || spin_limit > kSpinLimit)
+        return fl_fail(FL_ERR_ARG, "fl_test_scan_timeout: spin limit %d outside [1, %d]", spin_limit, kSpinLimit);
+    const int ntiles = (int)((s->gcells + kTile - 1) / kTile);
+    if (ntiles < 2) return fl_fail(FL_ERR_ARG, "fl_test_scan_timeout: needs at least two scan tiles");
+    FL_CUDA_TRY(cudaMemsetAsync(s->scan_ticket, 0, fl_scan_scratch_bytes(s->scan_tiles), s->stream));
+    k_scan<<<ntiles - 1, kThreads, 0, s->stream>>>(s->cnt, s->off, s->scan_status, s->scan_ticket, ntiles,
+                                                   s->scan_epoch, 0, s->dev_err, spin_limit, 1u);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fl_fail(FL_ERR_CUDA, "scan launch: %s", cudaGetErrorString(e));
+    fl_reset_progress(s);
     return FL_OK;
 }

@@ -74,12 +74,15 @@ SPH_PARAMS = dict(
 )
 
 
-def make_params(bound_min, bound_max, **overrides) -> FlParams:
-    p = default_params()
+def make_params(bound_min, bound_max, derive=None, **overrides) -> FlParams:
+    """The dam-break parameter set in the given box. `derive` (FlParams ->
+    FlParams) replaces the library's derivation; with it the inputs start
+    from zero instead of SetupDefaultParams (every input is set here)."""
+    p = default_params() if derive is None else FlParams()
     p.set(**SPH_PARAMS)
     p.set(bound_min=tuple(bound_min), bound_max=tuple(bound_max))
     p.set(**overrides)
-    return derive_params(p)
+    return derive_params(p) if derive is None else derive(p)
 
 
 def lattice_spacing() -> np.float32:
@@ -167,9 +170,10 @@ def shifted_target(sc: Scene, frac: float = 0.3, seed: int = 5) -> np.ndarray:
 
 
 def wave_tank(n: int = 4_000_000, seed: int = 2, steps: int = 1000,
-              wall_force: float = 0.3, wall_freq: float = 0.2) -> Scene:
+              wall_force: float = 0.3, wall_freq: float = 0.2, derive=None) -> Scene:
     """4M-point dam break with X- wall forcing: the block fills the low-x 40%
-    of a box scaled to hold it (86 x 216 lattice per layer, ~216 layers)."""
+    of a box scaled to hold it (86 x 216 lattice per layer, ~216 layers).
+    `derive`: see make_params."""
     s = lattice_spacing()
     cnt_x, cnt_z = 86, 216
     layers = -(-n // (cnt_x * cnt_z))
@@ -179,7 +183,7 @@ def wave_tank(n: int = 4_000_000, seed: int = 2, steps: int = 1000,
     lz = float(cnt_z * s) + 2 * margin
     ly = max(float(layers * s) + 2 * margin, lz)
     bmin, bmax = (0.0, 0.0, 0.0), (round(lx, 1), round(ly, 1), round(lz, 1))
-    params = make_params(bmin, bmax, bound_wall_force=wall_force, bound_wall_freq=wall_freq)
+    params = make_params(bmin, bmax, derive=derive, bound_wall_force=wall_force, bound_wall_freq=wall_freq)
     pos = lattice_block(n, (margin, margin, margin), cnt_x, cnt_z, s, seed)
     return _finish("wave_tank_4m" if n == 4_000_000 else f"wave_tank_{n}", params, pos, steps, bmin, bmax)
 

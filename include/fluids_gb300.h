@@ -409,20 +409,40 @@ int fl_tape_end(fl_system *s);
  * synchronise the device and stall its other streams: the cell prefix sum
  * of fl_prefix_sum_cells over caller-owned device buffers, without a
  * fl_system. d_counts[n] in, d_offsets[n] out (exclusive scan when
- * zero_offsets != 0, inclusive otherwise); d_status (nullable) gets
- * FL_DEV_SPIN_TIMEOUT OR-ed in if a look-back wait gave up. Work is queued
- * on `stream` (a cudaStream_t; NULL = default stream) and not waited for.
+ * zero_offsets != 0, inclusive otherwise); the two ranges must not overlap
+ * (the scan is not in place; overlapping ranges are rejected with
+ * FL_ERR_ARG). d_status (one device uint32, required: FL_ERR_ARG if NULL)
+ * gets FL_DEV_SPIN_TIMEOUT OR-ed in if a look-back wait gave up, in which
+ * case the offsets are wrong; it is the only report of that, since the
+ * call does not wait for its work. Work is queued on `stream` (a
+ * cudaStream_t; NULL = default stream).
  * The scan's scratch is a fixed ~8.5 KB device array inside the library,
  * held by every GPU that loads it until the process exits, so n is limited
  * to FL_NOALLOC_MAX_COUNTS (larger n is rejected with FL_ERR_ARG). The first
  * call on each device looks up that array's device address with the device
- * current; make that first call before any stream capture. All calls share
- * the one array: calls whose GPU work overlaps (other streams, other host
- * threads) race on it and must be ordered by the caller. Nothing is
- * allocated: no cudaMalloc, cudaFree or allocating library routine. */
+ * current; make that first call before any stream capture. Later calls look
+ * it up again unless their stream is capturing, so the array is found again
+ * after a cudaDeviceReset. All calls share the one array: calls whose GPU
+ * work overlaps (other streams, other host threads) race on it and must be
+ * ordered by the caller. Nothing is allocated: no cudaMalloc, cudaFree or
+ * allocating library routine. */
 #define FL_NOALLOC_MAX_COUNTS 4194304
 int fl_prefix_sum_noalloc(const uint32_t *d_counts, uint32_t *d_offsets, int n, int zero_offsets,
                           uint32_t *d_status, void *stream);
+
+/* ---- test hooks for the bounded look-back waits ----------------------------
+ * No counterpart in the reference. Each runs a scan with tile 0 withheld --
+ * one CTA fewer, the tile ticket starting at 1, so every index stays in
+ * bounds -- and a short spin limit (1 .. 2^20 polls): tile 1's wait for
+ * tile 0's descriptor runs out, the kernel records FL_DEV_SPIN_TIMEOUT and
+ * returns. fl_test_scan_timeout scans the system's cell counts (at least
+ * two 4096-entry tiles; fl_sync then returns FL_ERR_DEVICE), and
+ * fl_test_scan_noalloc_timeout runs fl_prefix_sum_noalloc's scan (n > 4096;
+ * the flag lands in d_status). The offsets they write are not a scan; they
+ * exist to test the error path. */
+int fl_test_scan_timeout(fl_system *s, int spin_limit);
+int fl_test_scan_noalloc_timeout(const uint32_t *d_counts, uint32_t *d_offsets, int n, uint32_t *d_status,
+                                 int spin_limit, void *stream);
 
 /* The CUDA stream (cudaStream_t) the system issues its work on. */
 void *fl_stream(fl_system *s);

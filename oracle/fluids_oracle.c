@@ -80,33 +80,46 @@ void orc_counting_sort(const fl_params *p, int n, const uint32_t *off,
     }
 }
 
-/* computePressure (fluids4.0/fluid_kernels.cu:112-149), FGRID = identity. */
+/* computePressure (fluids4.0/fluid_kernels.cu:112-149) for sorted point i,
+ * FGRID = identity. */
+static float density_point(const fl_params *p, int nadj, int i, const float *pos, const uint32_t *gcell,
+                           const uint32_t *off, const uint32_t *cnt) {
+    if (gcell[i] == UNDEF) return 0.0f;
+    const int base = (int)gcell[i] - nadj;
+    const float *xi = pos + 3 * i;
+    float sum = 0.0f;
+    for (int c = 0; c < p->gridAdjCnt; c++) {
+        const int cell = base + p->gridAdj[c];
+        const uint32_t j1 = off[cell] + cnt[cell];
+        for (uint32_t j = off[cell]; j < j1; j++) {
+            const float *xj = pos + 3 * j;
+            const float dx = xi[0] - xj[0], dy = xi[1] - xj[1], dz = xi[2] - xj[2];
+            float dsq = dx * dx + dy * dy + dz * dz;
+            if (dsq < p->rd2 && dsq > 0.0f) {
+                dsq = (p->rd2 - dsq) * p->d2;
+                sum += dsq * dsq * dsq;
+            }
+        }
+    }
+    sum = sum * p->pmass * p->poly6kern;
+    if (sum == 0.0f) sum = 1.0f;
+    return sum;
+}
+
 void orc_density(const fl_params *p, int n, const float *pos, const uint32_t *gcell,
                  const uint32_t *off, const uint32_t *cnt, float *press, int threads) {
     const int nadj = (1 * p->gridRes[2] + 1) * p->gridRes[0] + 1;
 #pragma omp parallel for schedule(dynamic, 1024) num_threads(threads) if (threads > 1)
-    for (int i = 0; i < n; i++) {
-        if (gcell[i] == UNDEF) { press[i] = 0.0f; continue; }
-        const int base = (int)gcell[i] - nadj;
-        const float *xi = pos + 3 * i;
-        float sum = 0.0f;
-        for (int c = 0; c < p->gridAdjCnt; c++) {
-            const int cell = base + p->gridAdj[c];
-            const uint32_t j1 = off[cell] + cnt[cell];
-            for (uint32_t j = off[cell]; j < j1; j++) {
-                const float *xj = pos + 3 * j;
-                const float dx = xi[0] - xj[0], dy = xi[1] - xj[1], dz = xi[2] - xj[2];
-                float dsq = dx * dx + dy * dy + dz * dz;
-                if (dsq < p->rd2 && dsq > 0.0f) {
-                    dsq = (p->rd2 - dsq) * p->d2;
-                    sum += dsq * dsq * dsq;
-                }
-            }
-        }
-        sum = sum * p->pmass * p->poly6kern;
-        if (sum == 0.0f) sum = 1.0f;
-        press[i] = sum;
-    }
+    for (int i = 0; i < n; i++) press[i] = density_point(p, nadj, i, pos, gcell, off, cnt);
+}
+
+/* The same at m chosen sorted slots: out[k] is slot idx[k]'s density (a
+ * sample of a large state; every other slot is still read as a neighbour). */
+void orc_density_at(const fl_params *p, int m, const uint32_t *idx, const float *pos, const uint32_t *gcell,
+                    const uint32_t *off, const uint32_t *cnt, float *out, int threads) {
+    const int nadj = (1 * p->gridRes[2] + 1) * p->gridRes[0] + 1;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads) if (threads > 1)
+    for (int k = 0; k < m; k++) out[k] = density_point(p, nadj, (int)idx[k], pos, gcell, off, cnt);
 }
 
 /* The pairs computePressure's loop accepts (0 < d^2 < rd2), per sorted
@@ -175,46 +188,59 @@ void orc_sample_volume(const fl_params *p, const float *pos, const uint32_t *off
             }
 }
 
-/* computeForce (fluids4.0/fluid_kernels.cu:180-217); the float3 operators
- * of cutil_math.h expand component-wise, and '/ s' is '* (1.0f / s)'. */
+/* computeForce (fluids4.0/fluid_kernels.cu:180-217) for sorted point i; the
+ * float3 operators of cutil_math.h expand component-wise, and '/ s' is
+ * '* (1.0f / s)'. */
+static void force_point(const fl_params *p, int nadj, int i, const float *pos, const float *veval,
+                        const float *press, const uint32_t *gcell, const uint32_t *off,
+                        const uint32_t *cnt, float *fo) {
+    if (gcell[i] == UNDEF) { fo[0] = fo[1] = fo[2] = 0.0f; return; }
+    const int base = (int)gcell[i] - nadj;
+    const float *xi = pos + 3 * i, *vi = veval + 3 * i;
+    const float di = press[i];
+    const float pi = (di - p->prest_dens) * p->pintstiff;
+    float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f;
+    for (int c = 0; c < p->gridAdjCnt; c++) {
+        const int cell = base + p->gridAdj[c];
+        const uint32_t j1 = off[cell] + cnt[cell];
+        for (uint32_t j = off[cell]; j < j1; j++) {
+            const float *xj = pos + 3 * j, *vj = veval + 3 * j;
+            const float dx = xi[0] - xj[0], dy = xi[1] - xj[1], dz = xi[2] - xj[2];
+            const float dsq = dx * dx + dy * dy + dz * dz;
+            if (dsq < p->rd2 && dsq > 0.0f) {
+                const float r = sqrtf(dsq * p->d2);
+                const float dj = press[j];
+                const float pj = (dj - p->prest_dens) * p->pintstiff;
+                const float cr = p->psmoothradius - r;
+                const float pterm = p->sim_scale * -0.5f * cr * p->spikykern * (pi + pj) / r;
+                const float sx = dx * pterm + (vj[0] - vi[0]) * p->vterm;
+                const float sy = dy * pterm + (vj[1] - vi[1]) * p->vterm;
+                const float sz = dz * pterm + (vj[2] - vi[2]) * p->vterm;
+                const float inv = 1.0f / (di * dj);
+                f0 += (sx * cr) * inv;
+                f1 += (sy * cr) * inv;
+                f2 += (sz * cr) * inv;
+            }
+        }
+    }
+    fo[0] = f0; fo[1] = f1; fo[2] = f2;
+}
+
 void orc_force(const fl_params *p, int n, const float *pos, const float *veval,
                const float *press, const uint32_t *gcell, const uint32_t *off,
                const uint32_t *cnt, float *force, int threads) {
     const int nadj = (1 * p->gridRes[2] + 1) * p->gridRes[0] + 1;
 #pragma omp parallel for schedule(dynamic, 1024) num_threads(threads) if (threads > 1)
-    for (int i = 0; i < n; i++) {
-        float *fo = force + 3 * i;
-        if (gcell[i] == UNDEF) { fo[0] = fo[1] = fo[2] = 0.0f; continue; }
-        const int base = (int)gcell[i] - nadj;
-        const float *xi = pos + 3 * i, *vi = veval + 3 * i;
-        const float di = press[i];
-        const float pi = (di - p->prest_dens) * p->pintstiff;
-        float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f;
-        for (int c = 0; c < p->gridAdjCnt; c++) {
-            const int cell = base + p->gridAdj[c];
-            const uint32_t j1 = off[cell] + cnt[cell];
-            for (uint32_t j = off[cell]; j < j1; j++) {
-                const float *xj = pos + 3 * j, *vj = veval + 3 * j;
-                const float dx = xi[0] - xj[0], dy = xi[1] - xj[1], dz = xi[2] - xj[2];
-                const float dsq = dx * dx + dy * dy + dz * dz;
-                if (dsq < p->rd2 && dsq > 0.0f) {
-                    const float r = sqrtf(dsq * p->d2);
-                    const float dj = press[j];
-                    const float pj = (dj - p->prest_dens) * p->pintstiff;
-                    const float cr = p->psmoothradius - r;
-                    const float pterm = p->sim_scale * -0.5f * cr * p->spikykern * (pi + pj) / r;
-                    const float sx = dx * pterm + (vj[0] - vi[0]) * p->vterm;
-                    const float sy = dy * pterm + (vj[1] - vi[1]) * p->vterm;
-                    const float sz = dz * pterm + (vj[2] - vi[2]) * p->vterm;
-                    const float inv = 1.0f / (di * dj);
-                    f0 += (sx * cr) * inv;
-                    f1 += (sy * cr) * inv;
-                    f2 += (sz * cr) * inv;
-                }
-            }
-        }
-        fo[0] = f0; fo[1] = f1; fo[2] = f2;
-    }
+    for (int i = 0; i < n; i++) force_point(p, nadj, i, pos, veval, press, gcell, off, cnt, force + 3 * i);
+}
+
+/* The same at m chosen sorted slots: out[3k..3k+2] is slot idx[k]'s force. */
+void orc_force_at(const fl_params *p, int m, const uint32_t *idx, const float *pos, const float *veval,
+                  const float *press, const uint32_t *gcell, const uint32_t *off, const uint32_t *cnt,
+                  float *out, int threads) {
+    const int nadj = (1 * p->gridRes[2] + 1) * p->gridRes[0] + 1;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads) if (threads > 1)
+    for (int k = 0; k < m; k++) force_point(p, nadj, (int)idx[k], pos, veval, press, gcell, off, cnt, out + 3 * k);
 }
 
 /* advanceParticles (fluids4.0/fluid_kernels.cu:332-420), in place. The
@@ -309,83 +335,108 @@ void orc_advance(const fl_params *p, int n, float time, float dt, float ss,
  * Same candidate cells, same formulas (poly6 density; spiky pressure plus
  * viscosity-Laplacian force), every operation in double. The force takes
  * the densities as input so that it checks the force pass alone. */
-void orc_density_f64(const fl_params *p, int n, const float *pos, const uint32_t *gcell,
-                     const uint32_t *off, const uint32_t *cnt, double *press, int threads) {
-    const int nadj = (1 * p->gridRes[2] + 1) * p->gridRes[0] + 1;
+static double density_point_f64(const fl_params *p, int nadj, int i, const float *pos, const uint32_t *gcell,
+                                const uint32_t *off, const uint32_t *cnt) {
     const double ss = p->sim_scale, h = p->psmoothradius;
     const double rd2 = (h * h) / (ss * ss), d2 = ss * ss;
     const double poly6 = 315.0 / (64.0 * M_PI * pow(h, 9.0));
-#pragma omp parallel for schedule(dynamic, 1024) num_threads(threads) if (threads > 1)
-    for (int i = 0; i < n; i++) {
-        if (gcell[i] == UNDEF) { press[i] = 0.0; continue; }
-        const int base = (int)gcell[i] - nadj;
-        double sum = 0.0;
-        for (int c = 0; c < p->gridAdjCnt; c++) {
-            const int cell = base + p->gridAdj[c];
-            const uint32_t j1 = off[cell] + cnt[cell];
-            for (uint32_t j = off[cell]; j < j1; j++) {
-                const double dx = (double)pos[3 * i] - pos[3 * j];
-                const double dy = (double)pos[3 * i + 1] - pos[3 * j + 1];
-                const double dz = (double)pos[3 * i + 2] - pos[3 * j + 2];
-                const double dsq = dx * dx + dy * dy + dz * dz;
-                if (dsq < rd2 && dsq > 0.0) {
-                    const double t = (rd2 - dsq) * d2;
-                    sum += t * t * t;
-                }
+    if (gcell[i] == UNDEF) return 0.0;
+    const int base = (int)gcell[i] - nadj;
+    double sum = 0.0;
+    for (int c = 0; c < p->gridAdjCnt; c++) {
+        const int cell = base + p->gridAdj[c];
+        const uint32_t j1 = off[cell] + cnt[cell];
+        for (uint32_t j = off[cell]; j < j1; j++) {
+            const double dx = (double)pos[3 * i] - pos[3 * j];
+            const double dy = (double)pos[3 * i + 1] - pos[3 * j + 1];
+            const double dz = (double)pos[3 * i + 2] - pos[3 * j + 2];
+            const double dsq = dx * dx + dy * dy + dz * dz;
+            if (dsq < rd2 && dsq > 0.0) {
+                const double t = (rd2 - dsq) * d2;
+                sum += t * t * t;
             }
         }
-        const double rho = sum * (double)p->pmass * poly6;
-        press[i] = (rho == 0.0) ? 1.0 : rho;
     }
+    const double rho = sum * (double)p->pmass * poly6;
+    return (rho == 0.0) ? 1.0 : rho;
+}
+
+void orc_density_f64(const fl_params *p, int n, const float *pos, const uint32_t *gcell,
+                     const uint32_t *off, const uint32_t *cnt, double *press, int threads) {
+    const int nadj = (1 * p->gridRes[2] + 1) * p->gridRes[0] + 1;
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(threads) if (threads > 1)
+    for (int i = 0; i < n; i++) press[i] = density_point_f64(p, nadj, i, pos, gcell, off, cnt);
+}
+
+void orc_density_f64_at(const fl_params *p, int m, const uint32_t *idx, const float *pos,
+                        const uint32_t *gcell, const uint32_t *off, const uint32_t *cnt, double *out,
+                        int threads) {
+    const int nadj = (1 * p->gridRes[2] + 1) * p->gridRes[0] + 1;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads) if (threads > 1)
+    for (int k = 0; k < m; k++) out[k] = density_point_f64(p, nadj, (int)idx[k], pos, gcell, off, cnt);
 }
 
 /* scale (nullable): per point, the sum of the magnitudes of its pair terms --
  * the bound that an FP32 evaluation's error is proportional to. */
-void orc_force_f64(const fl_params *p, int n, const float *pos, const float *veval,
-                   const float *press, const uint32_t *gcell, const uint32_t *off,
-                   const uint32_t *cnt, double *force, double *scale, int threads) {
-    const int nadj = (1 * p->gridRes[2] + 1) * p->gridRes[0] + 1;
+static void force_point_f64(const fl_params *p, int nadj, int i, const float *pos, const float *veval,
+                            const float *press, const uint32_t *gcell, const uint32_t *off,
+                            const uint32_t *cnt, double *fo, double *scale) {
     const double ss = p->sim_scale, h = p->psmoothradius;
     const double rd2 = (h * h) / (ss * ss), d2 = ss * ss;
     const double spiky = -45.0 / (M_PI * pow(h, 6.0));
     const double vterm = 45.0 / (M_PI * pow(h, 6.0)) * (double)p->pvisc;
     const double rest = p->prest_dens, stiff = p->pintstiff;
-#pragma omp parallel for schedule(dynamic, 1024) num_threads(threads) if (threads > 1)
-    for (int i = 0; i < n; i++) {
-        double *fo = force + 3 * i;
-        double sc = 0.0;
-        fo[0] = fo[1] = fo[2] = 0.0;
-        if (scale) scale[i] = 0.0;
-        if (gcell[i] == UNDEF) continue;
-        const int base = (int)gcell[i] - nadj;
-        const double di = press[i], pi = (di - rest) * stiff;
-        for (int c = 0; c < p->gridAdjCnt; c++) {
-            const int cell = base + p->gridAdj[c];
-            const uint32_t j1 = off[cell] + cnt[cell];
-            for (uint32_t j = off[cell]; j < j1; j++) {
-                double d[3], dsq = 0.0;
+    double sc = 0.0;
+    fo[0] = fo[1] = fo[2] = 0.0;
+    if (scale) *scale = 0.0;
+    if (gcell[i] == UNDEF) return;
+    const int base = (int)gcell[i] - nadj;
+    const double di = press[i], pi = (di - rest) * stiff;
+    for (int c = 0; c < p->gridAdjCnt; c++) {
+        const int cell = base + p->gridAdj[c];
+        const uint32_t j1 = off[cell] + cnt[cell];
+        for (uint32_t j = off[cell]; j < j1; j++) {
+            double d[3], dsq = 0.0;
+            for (int k = 0; k < 3; k++) {
+                d[k] = (double)pos[3 * i + k] - pos[3 * j + k];
+                dsq += d[k] * d[k];
+            }
+            if (dsq < rd2 && dsq > 0.0) {
+                const double r = sqrt(dsq * d2);
+                const double dj = press[j], pj = (dj - rest) * stiff;
+                const double cr = h - r;
+                const double pterm = -0.5 * ss * cr * spiky * (pi + pj) / r;
+                double t2 = 0.0;
                 for (int k = 0; k < 3; k++) {
-                    d[k] = (double)pos[3 * i + k] - pos[3 * j + k];
-                    dsq += d[k] * d[k];
+                    const double t = (d[k] * pterm + ((double)veval[3 * j + k] - veval[3 * i + k]) * vterm) *
+                                     cr / (di * dj);
+                    fo[k] += t;
+                    t2 += t * t;
                 }
-                if (dsq < rd2 && dsq > 0.0) {
-                    const double r = sqrt(dsq * d2);
-                    const double dj = press[j], pj = (dj - rest) * stiff;
-                    const double cr = h - r;
-                    const double pterm = -0.5 * ss * cr * spiky * (pi + pj) / r;
-                    double t2 = 0.0;
-                    for (int k = 0; k < 3; k++) {
-                        const double t = (d[k] * pterm + ((double)veval[3 * j + k] - veval[3 * i + k]) * vterm) *
-                                         cr / (di * dj);
-                        fo[k] += t;
-                        t2 += t * t;
-                    }
-                    sc += sqrt(t2);
-                }
+                sc += sqrt(t2);
             }
         }
-        if (scale) scale[i] = sc;
     }
+    if (scale) *scale = sc;
+}
+
+void orc_force_f64(const fl_params *p, int n, const float *pos, const float *veval,
+                   const float *press, const uint32_t *gcell, const uint32_t *off,
+                   const uint32_t *cnt, double *force, double *scale, int threads) {
+    const int nadj = (1 * p->gridRes[2] + 1) * p->gridRes[0] + 1;
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(threads) if (threads > 1)
+    for (int i = 0; i < n; i++)
+        force_point_f64(p, nadj, i, pos, veval, press, gcell, off, cnt, force + 3 * i, scale ? scale + i : NULL);
+}
+
+void orc_force_f64_at(const fl_params *p, int m, const uint32_t *idx, const float *pos, const float *veval,
+                      const float *press, const uint32_t *gcell, const uint32_t *off, const uint32_t *cnt,
+                      double *force, double *scale, int threads) {
+    const int nadj = (1 * p->gridRes[2] + 1) * p->gridRes[0] + 1;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads) if (threads > 1)
+    for (int k = 0; k < m; k++)
+        force_point_f64(p, nadj, (int)idx[k], pos, veval, press, gcell, off, cnt, force + 3 * k,
+                        scale ? scale + k : NULL);
 }
 
 /* ---- one full step -------------------------------------------------------

@@ -64,6 +64,10 @@ def orc():
         _orc.orc_density_f64.argtypes = [vp, i, vp, vp, vp, vp, vp, i]
         _orc.orc_force_f64.argtypes = [vp, i, vp, vp, vp, vp, vp, vp, vp, vp, i]
         _orc.orc_run.argtypes = [vp, i, i, C.POINTER(f), i] + [vp] * 18
+        _orc.orc_density_at.argtypes = [vp, i, vp, vp, vp, vp, vp, vp, i]
+        _orc.orc_force_at.argtypes = [vp, i, vp, vp, vp, vp, vp, vp, vp, vp, i]
+        _orc.orc_density_f64_at.argtypes = [vp, i, vp, vp, vp, vp, vp, vp, i]
+        _orc.orc_force_f64_at.argtypes = [vp, i, vp, vp, vp, vp, vp, vp, vp, vp, vp, i]
     return _orc
 
 
@@ -170,6 +174,47 @@ def force_f64(params, pos, veval, press, gcell, off, cnt, threads: int = 1):
     scale = np.zeros(pos.shape[0], np.float64)
     orc().orc_force_f64(C.byref(params), pos.shape[0], _p(pos), _p(veval), _p(press), _p(gcell),
                         _p(off), _p(cnt), _p(out), _p(scale), threads)
+    return out, scale
+
+
+def _idx(idx):
+    return np.ascontiguousarray(idx, np.uint32)
+
+
+def density_at(params, st: State, idx, threads: int = 1) -> np.ndarray:
+    """FP32 densities of the sorted slots `idx` of a sorted state (every slot
+    is still a neighbour): a sample of a state too large to evaluate whole."""
+    idx = _idx(idx)
+    out = np.zeros(idx.size, np.float32)
+    orc().orc_density_at(C.byref(params), idx.size, _p(idx), _p(st.pos), _p(st.gcell), _p(st.off), _p(st.cnt),
+                         _p(out), threads)
+    return out
+
+
+def force_at(params, pos, veval, press, gcell, off, cnt, idx, threads: int = 1) -> np.ndarray:
+    """FP32 forces of the sorted slots `idx` from the given densities."""
+    idx = _idx(idx)
+    out = np.zeros((idx.size, 3), np.float32)
+    orc().orc_force_at(C.byref(params), idx.size, _p(idx), _p(pos), _p(veval), _p(press), _p(gcell), _p(off),
+                       _p(cnt), _p(out), threads)
+    return out
+
+
+def density_f64_at(params, pos, gcell, off, cnt, idx, threads: int = 1) -> np.ndarray:
+    idx = _idx(idx)
+    out = np.zeros(idx.size, np.float64)
+    orc().orc_density_f64_at(C.byref(params), idx.size, _p(idx), _p(pos), _p(gcell), _p(off), _p(cnt), _p(out),
+                             threads)
+    return out
+
+
+def force_f64_at(params, pos, veval, press, gcell, off, cnt, idx, threads: int = 1):
+    """(force, scale) in FP64 at the sorted slots `idx`, from the given densities."""
+    idx = _idx(idx)
+    out = np.zeros((idx.size, 3), np.float64)
+    scale = np.zeros(idx.size, np.float64)
+    orc().orc_force_f64_at(C.byref(params), idx.size, _p(idx), _p(pos), _p(veval), _p(press), _p(gcell),
+                           _p(off), _p(cnt), _p(out), _p(scale), threads)
     return out, scale
 
 

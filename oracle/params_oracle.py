@@ -75,6 +75,25 @@ def derive(inp: dict) -> dict:
     return out
 
 
+def derive_flparams(p):
+    """A copy of the FlParams block `p` (inputs set) with every derived field
+    filled by derive() above -- fl_params_derive never runs, so a caller
+    that must stay independent of the product library (the reference arm of
+    the benchmark) gets its parameters from this restatement alone."""
+    out = p.copy()
+    inp = {k: (list(getattr(p, k)) if not isinstance(getattr(p, k), (int, float)) else getattr(p, k))
+           for k in ("sim_scale", "psmoothradius", "grid_density", "bound_min", "bound_max", "grav_dir",
+                     "grav_amt", "AL", "VL", "pvisc")}
+    for k, v in derive(inp).items():
+        if isinstance(v, list):
+            out.set(**{k: [int(x) if isinstance(x, int) else float(x) for x in v]})
+        else:
+            out.set(**{k: int(v) if isinstance(v, int) else float(v)})
+    # UpdateParamsCUDA's rest spacing (cpp:2300): powf(mass / rest density, 1/3)
+    out.pdist = float(powf(f32(f32(p.pmass) / f32(p.prest_dens)), f32(1.0) / f32(3.0)))
+    return out
+
+
 def compare(lib_params, tol_ulps: int = 0) -> list[str]:
     """Fields where fl_params_derive's result differs from this restatement.
     The powf-based kernels (poly6/spiky/lap) are compared within `tol_ulps`

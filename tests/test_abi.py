@@ -137,3 +137,28 @@ def test_product_has_no_cpu_fallback():
         assert "oracle" not in text.replace("oracle/", ""), f"{f} mentions the oracle"
     for f in (pkg / "csrc").iterdir():
         assert "fluids_oracle" not in f.read_text()
+
+
+def test_oracle_parameter_blocks_equal_the_library_ones():
+    """The benchmark's reference arm builds its parameters with the oracle's
+    restatement alone (no product code): the blocks must be byte-identical."""
+    for n in (60_000, 4_000_000):
+        a = scenes.wave_tank(n=n).params
+        b = scenes.wave_tank(n=n, derive=PO.derive_flparams).params
+        assert bytes(bytearray(a)) == bytes(bytearray(b)), f"wave tank {n}"
+
+
+def test_noalloc_scan_rejects_bad_arguments_before_any_gpu_work():
+    lib = _lib.lib()
+    status, counts, offsets = C.c_void_p(0x10000), C.c_void_p(0x20000), C.c_void_p(0x40000)
+    assert lib.fl_prefix_sum_noalloc(counts, offsets, 100, 1, None, None) == -1
+    assert b"d_status is required" in lib.fl_last_error()
+    # ranges [0x20000, 0x20000 + 4n) and [0x20100, ...) overlap for n = 100
+    assert lib.fl_prefix_sum_noalloc(counts, C.c_void_p(0x20100), 100, 1, status, None) == -1
+    assert b"overlap" in lib.fl_last_error()
+    assert lib.fl_prefix_sum_noalloc(counts, offsets, -1, 1, status, None) == -1
+    assert lib.fl_prefix_sum_noalloc(None, None, 0, 1, None, None) == 0
+    assert lib.fl_test_scan_noalloc_timeout(counts, offsets, 4096, status, 256, None) == -1
+    assert b"two tiles" in lib.fl_last_error()
+    assert lib.fl_test_scan_noalloc_timeout(counts, offsets, 8192, status, 0, None) == -1
+    assert lib.fl_test_scan_timeout(None, 256) == -1

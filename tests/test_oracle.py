@@ -216,3 +216,27 @@ def test_sample_volume_restatement_matches_reference_source():
         got = O.sample_volume(p, R.buf["pos"], off, cnt, res, lo, hi, 0.01)
         assert want.max() > 0
         assert_bit_equal(got, want, f"sample {res}")
+
+
+def test_sampled_evaluations_equal_the_full_ones():
+    """density_at / force_at (and their FP64 forms) evaluate chosen slots of a
+    large sorted state; they must give exactly the full pass's values there."""
+    sc = scenes.dam_break(n=20_000, seed=4)
+    p = sc.params
+    st = O.State.new(p, sc.pos, sc.vel, sc.veval, sc.clr)
+    O.run(p, st, 20, 0.0, threads=4)
+    O.insert(p, st)
+    O.prefix_sum(p, st)
+    O.counting_sort(p, st)
+    full = st.copy()
+    O.density(p, full, threads=4)
+    O.force(p, full, threads=4)
+    idx = np.random.default_rng(0).choice(st.n, 3000, replace=False)
+    assert_bit_equal(O.density_at(p, st, idx, threads=4), full.press[idx], "sampled density")
+    args = (full.pos, full.veval, full.press, full.gcell, full.off, full.cnt)
+    assert_bit_equal(O.force_at(p, *args, idx, threads=4), full.force[idx], "sampled force")
+    d64 = O.density_f64(p, full.pos, full.gcell, full.off, full.cnt, threads=4)
+    assert np.array_equal(O.density_f64_at(p, full.pos, full.gcell, full.off, full.cnt, idx, threads=4), d64[idx])
+    f64, s64 = O.force_f64(p, *args, threads=4)
+    fa, sa = O.force_f64_at(p, *args, idx, threads=4)
+    assert np.array_equal(fa, f64[idx]) and np.array_equal(sa, s64[idx])

@@ -64,3 +64,28 @@ def test_noalloc_scan_ragged_and_limit():
     # beyond the fixed scratch: rejected before any GPU work
     big = F.lib().fl_prefix_sum_noalloc(None, None, 4194305, 1, None, None)
     assert big == -1 and b"exceed" in F.lib().fl_last_error()
+
+
+def test_noalloc_scan_wait_runs_out_and_is_reported():
+    """The scan's bounded look-back wait, made to run out on purpose: the
+    test hook withholds tile 0 (one CTA fewer, every index in bounds) with a
+    256-poll limit. The call returns, FL_DEV_SPIN_TIMEOUT lands in d_status,
+    and the next ordinary call (which clears the shared scratch) scans
+    correctly again."""
+    torch = pytest.importorskip("torch")
+    n = 3 * 4096 + 5
+    cnt = np.random.default_rng(8).integers(0, 40, size=n, dtype=np.uint32)
+    d_cnt = torch.from_numpy(cnt.view(np.int32)).cuda()
+    d_off = torch.empty(n, dtype=torch.int32, device="cuda")
+    d_status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    lib = _lib.lib()
+    assert lib.fl_test_scan_noalloc_timeout(d_cnt.data_ptr(), d_off.data_ptr(), n, d_status.data_ptr(), 256,
+                                            None) == 0, lib.fl_last_error()
+    torch.cuda.synchronize()
+    assert int(d_status.item()) & 0x1
+    d_status.zero_()
+    assert _scan(d_cnt, d_off, n, 1, d_status) == 0
+    torch.cuda.synchronize()
+    want = (np.cumsum(cnt, dtype=np.uint64) - cnt).astype(np.uint32)
+    assert_bit_equal(d_off.cpu().numpy().view(np.uint32), want, "scan after the timed-out one")
+    assert int(d_status.item()) == 0
