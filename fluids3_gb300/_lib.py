@@ -68,6 +68,8 @@ SIGNATURES = [
     ("fl_add_particles", C.c_int, [vp, C.c_int, vp, vp, vp, vp]),
     ("fl_autotune", C.c_int, [vp, C.c_int, vp]),
     ("fl_launch_shapes", C.c_int, [vp, vp]),
+    ("fl_set_neighbour_passes", C.c_int, [vp, C.c_int]),
+    ("fl_neighbour_passes", C.c_int, [vp]),
     ("fl_set_launch_shapes", C.c_int, [vp, vp]),
     ("fl_conservation", C.c_int, [vp, vp]),
     ("fl_pts_write", C.c_int, [C.c_char_p, C.c_int, vp, vp, vp, vp]),
@@ -81,6 +83,7 @@ SIGNATURES = [
     ("fl_tape_steps", C.c_int, [vp]),
     ("fl_tape_order", C.c_int, [vp, vp]),
     ("fl_backward", C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp]),
+    ("fl_backward_scaled", C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     ("fl_tape_end", C.c_int, [vp]),
     ("fl_stream", vp, [vp]),
     ("fl_last_error", C.c_char_p, []),

@@ -881,7 +881,7 @@ k_param_partial(const float4 *__restrict__ pc, const int *__restrict__ sbase, co
 }
 
 __global__ void k_param_final(int nscenes, int nchunks, const double *__restrict__ partial,
-                              double *__restrict__ acc) {
+                              const int *__restrict__ gexp, double *__restrict__ acc) {
     // one warp per scene: lane l takes chunks l, l+32, ...; fixed shuffle tree
     const int scene = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (scene >= nscenes) return;
@@ -890,8 +890,94 @@ __global__ void k_param_final(int nscenes, int nchunks, const double *__restrict
         double t = 0.0;
         for (int c = (int)lane; c < nchunks; c += 32) t += partial[((size_t)scene * nchunks + c) * 3 + j];
         for (int d = 16; d > 0; d >>= 1) t += __shfl_xor_sync(0xffffffffu, t, d);
-        if (lane == 0) acc[scene * 3 + j] += t;
+        // the partials carry the cotangent's current scale 2^-gexp
+        if (lane == 0) acc[scene * 3 + j] += gexp ? ldexp(t, gexp[scene]) : t;
     }
+}
+
+// ---- cotangent renormalisation ----------------------------------------------
+// The exact gradient of a long rollout grows about 1.4x per step (nearby
+// trajectories diverge), so over a few hundred steps the cotangents leave
+// the FP32 range. After each reverse step the cotangents of a scene whose
+// largest component exceeds 2^40 are scaled by 2^-k (k its binary
+// exponent) and k is added to the scene's exponent. Power-of-two scaling
+// is exact and every reverse operation is linear in the cotangent, so the
+// mantissas round exactly as the unscaled values would.
+constexpr float kRescaleAbove = 1099511627776.0f;   // 2^40
+
+__device__ __forceinline__ float abs_max4(float4 v, float m) {
+    return fmaxf(m, fmaxf(fabsf(v.x), fmaxf(fabsf(v.y), fabsf(v.z))));
+}
+
+// Per-scene largest |component| of (dL/dX, dL/dV, dL/dE) as float bits
+// (non-negative floats order like their bit patterns); NaN is kept as the
+// largest value so that no scaling hides it.
+__global__ void __launch_bounds__(kThreads)
+k_adj_gmax(int n, const uint16_t *__restrict__ point_scene, const float4 *__restrict__ gx,
+           const float4 *__restrict__ gv, const float4 *__restrict__ ge, uint32_t *__restrict__ gmax) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < n;
+    float m = 0.0f;
+    bool nan = false;
+    uint32_t scene = 0;
+    if (valid) {
+        const float4 a = gx[i], b = gv[i], c = ge[i];
+        m = abs_max4(c, abs_max4(b, abs_max4(a, 0.0f)));
+        nan = isnan(a.x + a.y + a.z + b.x + b.y + b.z + c.x + c.y + c.z);
+        scene = point_scene ? point_scene[i] : 0u;
+    }
+    uint32_t bits = nan ? 0x7fffffffu : __float_as_uint(m);
+    const uint32_t s0 = __shfl_sync(0xffffffffu, scene, 0);
+    if (__all_sync(0xffffffffu, !valid || scene == s0)) {
+        bits = __reduce_max_sync(0xffffffffu, bits);
+        if ((threadIdx.x & 31u) == 0 && bits) atomicMax(&gmax[s0], bits);
+    } else if (valid && bits) {
+        atomicMax(&gmax[scene], bits);
+    }
+}
+
+__device__ __forceinline__ int rescale_exponent(uint32_t bits) {
+    const float m = __uint_as_float(bits);
+    // at most 126, so that 2^-k stays a normal float
+    return (bits < 0x7f800000u && m > kRescaleAbove) ? min(ilogbf(m), 126) : 0;
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_adj_rescale(int n, const uint16_t *__restrict__ point_scene, float4 *__restrict__ gx, float4 *__restrict__ gv,
+              float4 *__restrict__ ge, const uint32_t *__restrict__ gmax) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int k = rescale_exponent(gmax[point_scene ? point_scene[i] : 0u]);
+    if (!k) return;
+    const float f = __int_as_float((127 - k) << 23);   // 2^-k, k in 40..126
+    float4 a = gx[i], b = gv[i], c = ge[i];
+    a.x *= f; a.y *= f; a.z *= f;
+    b.x *= f; b.y *= f; b.z *= f;
+    c.x *= f; c.y *= f; c.z *= f;
+    gx[i] = a; gv[i] = b; ge[i] = c;
+}
+
+// The gradient itself from its mantissa: times 2^gexp (float; infinite
+// where it overflows).
+__global__ void __launch_bounds__(kThreads)
+k_adj_apply_exponent(int n, const uint16_t *__restrict__ point_scene, float4 *__restrict__ gx,
+                     float4 *__restrict__ gv, float4 *__restrict__ ge, const int *__restrict__ gexp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int k = gexp[point_scene ? point_scene[i] : 0u];
+    if (!k) return;
+    float4 a = gx[i], b = gv[i], c = ge[i];
+    a.x = ldexpf(a.x, k); a.y = ldexpf(a.y, k); a.z = ldexpf(a.z, k);
+    b.x = ldexpf(b.x, k); b.y = ldexpf(b.y, k); b.z = ldexpf(b.z, k);
+    c.x = ldexpf(c.x, k); c.y = ldexpf(c.y, k); c.z = ldexpf(c.z, k);
+    gx[i] = a; gv[i] = b; ge[i] = c;
+}
+
+__global__ void k_adj_bump(int nscenes, uint32_t *__restrict__ gmax, int *__restrict__ gexp) {
+    const int sc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sc >= nscenes) return;
+    gexp[sc] += rescale_exponent(gmax[sc]);
+    gmax[sc] = 0u;
 }
 
 // Identity tracking across recorded steps: out[s] = in[src[s]] (in null:
@@ -997,13 +1083,33 @@ int fl_param_chunks(int max_scene_points) {
 }
 
 int fl_launch_param_reduce(fl_system *s, const float4 *pc, const int *sbase, const int *sn, int nchunks,
-                           double *partial, double *acc) {
+                           double *partial, const int *gexp, double *acc) {
     if (s->n == 0) return FL_OK;
     dim3 grid((unsigned)nchunks, (unsigned)s->nscenes);
     k_param_partial<<<grid, kReduceThreads, 0, s->stream>>>(pc, sbase, sn, nchunks, partial);
     FL_LAUNCH_CHECK("param_partial");
-    k_param_final<<<blocks_for(s->nscenes, 4), 128, 0, s->stream>>>(s->nscenes, nchunks, partial, acc);
+    k_param_final<<<blocks_for(s->nscenes, 4), 128, 0, s->stream>>>(s->nscenes, nchunks, partial, gexp, acc);
     FL_LAUNCH_CHECK("param_final");
+    return FL_OK;
+}
+
+int fl_launch_adj_apply_exponent(fl_system *s, float4 *gx, float4 *gv, float4 *ge, const int *gexp) {
+    if (s->n == 0) return FL_OK;
+    const uint16_t *ps = s->batched ? s->point_scene : nullptr;
+    k_adj_apply_exponent<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(s->n, ps, gx, gv, ge, gexp);
+    FL_LAUNCH_CHECK("adj_apply_exponent");
+    return FL_OK;
+}
+
+int fl_launch_adj_rescale(fl_system *s, float4 *gx, float4 *gv, float4 *ge, uint32_t *gmax, int *gexp) {
+    if (s->n == 0) return FL_OK;
+    const uint16_t *ps = s->batched ? s->point_scene : nullptr;
+    k_adj_gmax<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(s->n, ps, gx, gv, ge, gmax);
+    FL_LAUNCH_CHECK("adj_gmax");
+    k_adj_rescale<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(s->n, ps, gx, gv, ge, gmax);
+    FL_LAUNCH_CHECK("adj_rescale");
+    k_adj_bump<<<blocks_for(s->nscenes, 128), 128, 0, s->stream>>>(s->nscenes, gmax, gexp);
+    FL_LAUNCH_CHECK("adj_bump");
     return FL_OK;
 }
 

@@ -101,9 +101,13 @@ int fl_dalloc(void **p, size_t bytes) {
 static void free_grid(fl_system *s) {
     cudaFree(s->cnt);
     cudaFree(s->off);
+    cudaFree(s->tasks);
     s->codes_valid = 0;
     s->cnt = s->off = nullptr;
+    s->tasks = nullptr;
+    s->task_cap = 0;
     s->scan_ticket = nullptr;
+    s->task_counters = nullptr;
     s->scan_status = nullptr;
 }
 
@@ -118,12 +122,17 @@ static int alloc_grid(fl_system *s) {
     const size_t entries = (size_t)s->gcells;
     s->scan_tiles = (int)((entries + tile - 1) / tile);
     s->grid_pad = (size_t)s->scan_tiles * tile;
-    void *blk = nullptr, *off = nullptr;
+    void *blk = nullptr, *off = nullptr, *tasks = nullptr;
     FL_TRY(fl_dalloc(&blk, grid_block_bytes(s)));
     int r = fl_dalloc(&off, s->grid_pad * sizeof(uint32_t));
     if (r != FL_OK) { cudaFree(blk); return r; }
+    s->task_cap = fl_task_cap(s->max_points, s->gcells);
+    r = fl_dalloc(&tasks, s->task_cap * sizeof(uint2));
+    if (r != FL_OK) { cudaFree(blk); cudaFree(off); return r; }
+    s->tasks = (uint2 *)tasks;
     s->cnt = (uint32_t *)blk;
     s->scan_ticket = (uint32_t *)((char *)blk + s->grid_pad * sizeof(uint32_t));
+    s->task_counters = s->scan_ticket + 1;   // same 256-byte slot as the ticket
     s->scan_status = (uint64_t *)((char *)s->scan_ticket + 256);
     s->off = (uint32_t *)off;
     s->scan_epoch = 1;
@@ -181,6 +190,7 @@ extern "C" int fl_create(const fl_params *p, int max_points, fl_system **out) {
     FL_TRY(check_derived(p));
     fl_system *s = (fl_system *)calloc(1, sizeof(fl_system));
     if (!s) return fl_fail(FL_ERR_NOMEM, "fl_create: host allocation failed");
+    s->cell_passes = 1;
     int r = FL_OK;
     do {
         if (cudaGetDevice(&s->device) != cudaSuccess) {
@@ -222,6 +232,7 @@ extern "C" int fl_create(const fl_params *p, int max_points, fl_system **out) {
             break;
         }
         if ((r = fl_kernels_init(s)) != FL_OK) break;
+        if ((r = fl_cells_init(s)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&s->dev_err, 256)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&s->time_dev, 256)) != FL_OK) break;
         if ((r = alloc_grid(s)) != FL_OK) break;
@@ -290,6 +301,7 @@ extern "C" int fl_batch_create(const fl_params *params, const int *counts, int n
         s->P = params[0];
         s->batched = 1;
         s->nscenes = nscenes;
+        if ((r = fl_cells_init(s)) != FL_OK) break;
         free_grid(s);
         s->ncells = (int)ncell;
         s->gcells = (int)gcell;
@@ -839,6 +851,13 @@ static int record(fl_system *s, TimingState *t, int k) {
     return FL_OK;
 }
 
+// The cell-task passes (fl_cells.cu) need the pruned search (gridSrch 2 in
+// every scene) with band codes from this step's sort; a recording tape keeps
+// the per-point passes, whose pair lists its reverse steps read.
+static bool use_cell_passes(const fl_system *s, bool taped) {
+    return s->cell_passes && s->D.prune && s->codes_valid && !taped && s->n > 0;
+}
+
 static int run_step(fl_system *s, TimingState *t) {
     // InsertParticles, PrefixSumCells, CountingSortFull, ComputePressure,
     // ComputeForce + Advance (cpp:507-515) as eight launches (the sort is a
@@ -855,10 +874,12 @@ static int run_step(fl_system *s, TimingState *t) {
     FL_TRY(record(s, t, 3));
     FL_TRY(fl_launch_sort_cells(s, 1));
     flip(s, F_POS); flip(s, F_VEL); flip(s, F_VEVAL); flip(s, F_CLR); flip(s, F_GCELL); flip(s, F_GNDX);
+    const bool cells = use_cell_passes(s, taped);
+    if (cells) FL_TRY(fl_launch_make_tasks(s));
     FL_TRY(record(s, t, 4));
-    FL_TRY(fl_launch_density(s));
+    FL_TRY(cells ? fl_launch_density_cells(s) : fl_launch_density(s));
     FL_TRY(record(s, t, 5));
-    FL_TRY(fl_launch_force_advance(s, s->P.dt));
+    FL_TRY(cells ? fl_launch_force_cells(s, s->P.dt, nullptr) : fl_launch_force_advance(s, s->P.dt));
     flip(s, F_POS); flip(s, F_VEVAL);
     s->codes_valid = 0;
     s->lists_valid = 0;
@@ -935,10 +956,16 @@ static int run_step_late(fl_system *s, const float *vel3, const float *veval3, c
     FL_TRY(fl_launch_scatter_index(s));
     FL_TRY(fl_launch_sort_cells(s, 1, true));
     flip(s, F_POS); flip(s, F_VEL); flip(s, F_VEVAL); flip(s, F_CLR); flip(s, F_GCELL); flip(s, F_GNDX);
-    FL_TRY(fl_launch_density(s));
+    const bool cells = use_cell_passes(s, false);
+    if (cells) FL_TRY(fl_launch_make_tasks(s));
+    FL_TRY(cells ? fl_launch_density_cells(s) : fl_launch_density(s));
     FL_CUDA_TRY(cudaStreamWaitEvent(s->stream, s->ev_late, 0));
     FL_TRY(fl_launch_gather_late(s, vel3, veval3, clr));
-    if (!pos_out) {
+    if (cells) {
+        // the force pass also writes the new positions into the caller's
+        // page-locked array as it goes (no separate readback)
+        FL_TRY(fl_launch_force_cells(s, s->P.dt, pos_out ? (float *)mapped_device_ptr(pos_out) : nullptr));
+    } else if (!pos_out) {
         FL_TRY(fl_launch_force_advance(s, s->P.dt));
     } else {
         // the force pass in up to four slot ranges of whole blocks; as each
@@ -1222,6 +1249,22 @@ extern "C" int fl_set_launch_shapes(fl_system *s, const int *shapes) {
     s->sort_cells = c;
     destroy_graph(s);   // the captured step holds the old shapes
     return FL_OK;
+}
+
+extern "C" int fl_set_neighbour_passes(fl_system *s, int mode) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_set_neighbour_passes: null system");
+    if (mode != FL_PASSES_PER_POINT && mode != FL_PASSES_CELL_TASKS)
+        return fl_fail(FL_ERR_ARG, "fl_set_neighbour_passes: mode %d is neither %d nor %d", mode,
+                       FL_PASSES_PER_POINT, FL_PASSES_CELL_TASKS);
+    FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->cell_passes = mode == FL_PASSES_CELL_TASKS;
+    destroy_graph(s);   // the captured step holds the other passes
+    return FL_OK;
+}
+
+extern "C" int fl_neighbour_passes(const fl_system *s) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_neighbour_passes: null system");
+    return s->cell_passes ? FL_PASSES_CELL_TASKS : FL_PASSES_PER_POINT;
 }
 
 extern "C" int fl_launch_shapes(fl_system *s, int *shapes) {

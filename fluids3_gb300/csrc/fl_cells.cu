@@ -1,0 +1,477 @@
+// Cell-task neighbour passes of the fused step (gridSrch 2, band codes set).
+//
+// computePressure and computeForce (fluids4.0/fluid_kernels.cu:112-149,
+// 180-217) walk, for every point, the 2x2x2 search block c-1..c of its cell
+// c. Every point of a cell shares that block, so here the unit of work is a
+// task: up to 64 sorted slots of one cell, taken by one warp (two points per
+// lane: slot s0 + lane and s0 + 32 + lane). The warp walks the block once
+// for all of its points, in lockstep:
+//
+//  * the walk visits the adjacency entries in the reference's order, each
+//    entry only if some point of the task lies within the band of every
+//    lower face that entry reaches across (the same pruning as the
+//    per-thread walk: lower-band bits in pos.w), and within an entry the
+//    members whose upper-band flags cover those faces, in ascending slot
+//    order -- the "union" sequence of the task;
+//  * each 32-slot flag word is staged with one coalesced load per lane into
+//    a per-warp ring in shared memory, and every staged candidate is then
+//    tested by all lanes at once (a broadcast read), 32 at a time;
+//  * a pair that some other point of the task needed but this point's own
+//    pruning would have skipped has |d| >= band > h, so it fails the test
+//    0 < d^2 < rd2: each point's sum still sees exactly the reference's
+//    terms in the reference's order, and densities and forces stay
+//    bit-identical to the per-point walk.
+//
+// The density pass evaluates two points per lane with packed f32x2
+// arithmetic (add/sub/mul.rn.f32x2: IEEE round-to-nearest per element, the
+// same results as scalar operations) when a task has more than 32 points.
+// The force pass stages each candidate's 32-byte pair record (position and
+// density, evaluated velocity; written by the density pass), tests the 32
+// candidates of a group for every lane, and then each lane adds its own
+// hits in order with the reference's pair arithmetic (add_pair_terms),
+// followed by the advance of its points.
+//
+// Tasks are listed once per step by k_make_tasks (one entry per 64 slots of
+// a cell, out-of-range bins included, in any order: no result depends on
+// it). Both passes run a grid sized to the resident warps, each warp taking
+// tasks from a ticket.
+#include <algorithm>
+
+#include "fl_internal.h"
+
+namespace {
+
+#include "fl_device.cuh"
+#include "fl_step.cuh"
+
+constexpr int kTaskPoints = 64;    // slots per task: two per lane
+constexpr int kCellThreads = 128;  // threads per block of both passes (4 warps, one task each at a time)
+constexpr uint32_t kRing = 64;     // staged candidates per warp (at most 63 are pending)
+
+// ---- packed f32x2 arithmetic (round-to-nearest per element) ---------------
+__device__ __forceinline__ uint64_t pk2(float a, float b) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void up2(uint64_t v, float &a, float &b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+    uint64_t r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
+    uint64_t r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+    uint64_t r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+// ---- tasks ------------------------------------------------------------------
+// counters (in the grid block, cleared with the counts every step):
+// [0] tasks listed, [1] density pass ticket, [2] force pass ticket.
+// One task per kTaskPoints slots of every non-empty cell entry (an entry's
+// tasks are its slots off + 64 k); a task is (first slot, cell entry).
+__global__ void __launch_bounds__(256)
+k_make_tasks(int gcells, const uint32_t *__restrict__ off, const uint32_t *__restrict__ cnt,
+             uint2 *__restrict__ tasks, uint32_t cap, uint32_t *counters, uint32_t *err) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned lane = lane_id();
+    const uint32_t m = (c < gcells) ? cnt[c] : 0u;
+    const uint32_t k = (m + kTaskPoints - 1) / kTaskPoints;
+    uint32_t incl = k;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= (unsigned)d) incl += y;
+    }
+    uint32_t base = 0;
+    if (lane == 31 && incl) base = atomicAdd(&counters[0], incl);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    if (!k) return;
+    const uint32_t o = off[c];
+    uint32_t t = base + incl - k;
+    for (uint32_t q = 0; q < k; q++, t++) {
+        if (t < cap) tasks[t] = make_uint2(o + q * kTaskPoints, (uint32_t)c);
+        else atomicOr(err, FL_DEV_BAD_CELL);
+    }
+}
+
+// The adjacency entries (bit k) the task's points reach: entry k is needed
+// when some point lies within the band of every lower face the entry
+// crosses (lower-band bits 3-5 of its code).
+__device__ __forceinline__ uint32_t needed_entries(bool va, uint32_t ca, bool vb, uint32_t cb) {
+    const uint32_t la = (ca >> 3) & 7u, lb = (cb >> 3) & 7u;
+    uint32_t need = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const uint32_t U = lower_axes(k);
+        if (__any_sync(0xffffffffu, (va && (la & U) == U) || (vb && (lb & U) == U))) need |= 1u << k;
+    }
+    return need;
+}
+
+// The union walk of a task in cell c: for each needed adjacency entry in
+// order, the members of that neighbour cell whose upper-band flags cover the
+// faces the entry crosses, in ascending slot order. stage(r, j) (called by
+// the lanes that hold candidate j) puts slot j's data into ring slot r;
+// group(g, count) evaluates the `count` candidates staged from union index
+// g (g a multiple of 32; count 32 except for the last group). All lanes
+// call this with the same arguments.
+template <class Stage, class Group>
+__device__ __forceinline__ void walk_union(const DevParams &P, int c, uint32_t need,
+                                           const uint32_t *__restrict__ off, const uint32_t *__restrict__ cnt,
+                                           const uint32_t *__restrict__ upbits, Stage stage, Group group) {
+    const unsigned lane = lane_id();
+    const unsigned below = (1u << lane) - 1u;
+    const int base = c - P.nadj;
+    uint32_t staged = 0, head = 0;
+    for (int k = 0; k < 8; k++) {
+        if (!((need >> k) & 1u)) continue;
+        const int cn = base + P.adj[k];
+        const uint32_t mn = cnt[cn];
+        if (mn == 0) continue;
+        const uint32_t lo = off[cn], hi = lo + mn;
+        const uint32_t U = lower_axes(k);
+        const uint32_t w_lo = lo >> 5, w_hi = (hi - 1) >> 5;
+        for (uint32_t wd = w_lo; wd <= w_hi; wd++) {
+            uint32_t bits = 0xffffffffu;
+            if (U & 1u) bits &= upbits[wd];
+            if (U & 2u) bits &= upbits[(size_t)P.upwords + wd];
+            if (U & 4u) bits &= upbits[2 * (size_t)P.upwords + wd];
+            if (wd == w_lo) bits &= 0xffffffffu << (lo & 31u);
+            if (wd == w_hi && (hi & 31u)) bits &= 0xffffffffu >> (32u - (hi & 31u));
+            if (!bits) continue;
+            if ((bits >> lane) & 1u) stage((staged + __popc(bits & below)) & (kRing - 1u), (wd << 5) + lane);
+            staged += __popc(bits);
+            if (staged - head >= 32u) {
+                __syncwarp();
+                group(head, 32u);
+                __syncwarp();
+                head += 32u;
+            }
+        }
+    }
+    if (staged > head) {
+        __syncwarp();
+        group(head, staged - head);
+        __syncwarp();
+    }
+}
+
+// ---- density ----------------------------------------------------------------
+// Candidates of one group against one point per lane (a), in order. A
+// candidate that fails the test adds +0, which leaves the (non-negative)
+// sum unchanged.
+__device__ __forceinline__ void density_group1(const DevParams &P, const float4 *ring, uint32_t g, uint32_t count,
+                                               float4 pa, float &sa) {
+#pragma unroll 4
+    for (uint32_t u = 0; u < count; u++) {
+        const float4 q = ring[(g + u) & (kRing - 1u)];
+        const float dx = pa.x - q.x, dy = pa.y - q.y, dz = pa.z - q.z;
+        const float dsq = dx * dx + dy * dy + dz * dz;
+        const float t = (P.rd2 - dsq) * P.d2;
+        const float t3 = t * t * t;
+        sa += (dsq < P.rd2 && dsq > 0.0f) ? t3 : 0.0f;
+    }
+}
+
+// The same for two points per lane (a, b), in packed f32x2 arithmetic.
+__device__ __forceinline__ void density_group2(const DevParams &P, const float4 *ring, uint32_t g, uint32_t count,
+                                               uint64_t px, uint64_t py, uint64_t pz, uint64_t &sab) {
+    const uint64_t rd2 = pk2(P.rd2, P.rd2), d2 = pk2(P.d2, P.d2);
+#pragma unroll 4
+    for (uint32_t u = 0; u < count; u++) {
+        const float4 q = ring[(g + u) & (kRing - 1u)];
+        const uint64_t dx = sub2(px, pk2(q.x, q.x));
+        const uint64_t dy = sub2(py, pk2(q.y, q.y));
+        const uint64_t dz = sub2(pz, pk2(q.z, q.z));
+        const uint64_t dsq = add2(add2(mul2(dx, dx), mul2(dy, dy)), mul2(dz, dz));
+        const uint64_t t = mul2(sub2(rd2, dsq), d2);
+        const uint64_t t3 = mul2(mul2(t, t), t);
+        float da, db, ta, tb;
+        up2(dsq, da, db);
+        up2(t3, ta, tb);
+        ta = (da < P.rd2 && da > 0.0f) ? ta : 0.0f;
+        tb = (db < P.rd2 && db > 0.0f) ? tb : 0.0f;
+        sab = add2(sab, pk2(ta, tb));
+    }
+}
+
+template <bool BATCH>
+__global__ void __launch_bounds__(kCellThreads)
+k_density_cells(const __grid_constant__ DevParams P0, const SceneTab T, const uint2 *__restrict__ tasks,
+                uint32_t cap, uint32_t *counters, const float4 *__restrict__ pos, const uint32_t *__restrict__ off,
+                const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
+                const float4 *__restrict__ veval, float *__restrict__ press, float4 *__restrict__ pairdata) {
+    __shared__ float4 s_ring[kCellThreads / 32][kRing];
+    const unsigned lane = lane_id();
+    float4 *ring = s_ring[threadIdx.x >> 5];
+    const uint32_t ntasks = min(counters[0], cap);   // k_make_tasks flags an overflow
+    for (;;) {
+        uint32_t t = 0;
+        if (lane == 0) t = atomicAdd(&counters[1], 1u);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= ntasks) return;
+        const uint2 task = tasks[t];
+        const int c = (int)task.y;
+        const DevParams &P = BATCH ? T.params[T.cell_scene[c]] : P0;
+        const uint32_t mt = min((uint32_t)kTaskPoints, off[c] + cnt[c] - task.x);
+        const uint32_t ia = task.x + lane, ib = ia + 32u;
+        const bool va = lane < mt, vb = lane + 32u < mt;
+        if (c - P.cell_base == P.ncells) {   // the out-of-range bin: density 0
+            if (va) press[ia] = 0.0f;
+            if (vb) press[ib] = 0.0f;
+            continue;
+        }
+        const float4 pa = va ? pos[ia] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 pb = vb ? pos[ib] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const uint32_t need = needed_entries(va, __float_as_uint(pa.w), vb, __float_as_uint(pb.w));
+        auto stage = [&](uint32_t r, uint32_t j) { ring[r] = pos[j]; };
+        float sa = 0.0f, sb = 0.0f;
+        if (mt > 32u) {   // two points per lane
+            const uint64_t px = pk2(pa.x, pb.x), py = pk2(pa.y, pb.y), pz = pk2(pa.z, pb.z);
+            uint64_t sab = pk2(0.0f, 0.0f);
+            walk_union(P, c, need, off, cnt, upbits, stage,
+                       [&](uint32_t g, uint32_t count) { density_group2(P, ring, g, count, px, py, pz, sab); });
+            up2(sab, sa, sb);
+        } else {
+            walk_union(P, c, need, off, cnt, upbits, stage,
+                       [&](uint32_t g, uint32_t count) { density_group1(P, ring, g, count, pa, sa); });
+        }
+        // fluid_kernels.cu:146-148, and the pair records the force pass reads
+        if (va) {
+            sa = sa * P.pmass * P.poly6kern;
+            if (sa == 0.0f) sa = 1.0f;
+            press[ia] = sa;
+            const float4 e = veval[ia];
+            pairdata[2 * (size_t)ia] = make_float4(pa.x, pa.y, pa.z, sa);
+            pairdata[2 * (size_t)ia + 1] = make_float4(e.x, e.y, e.z, 0.0f);
+        }
+        if (vb) {
+            sb = sb * P.pmass * P.poly6kern;
+            if (sb == 0.0f) sb = 1.0f;
+            press[ib] = sb;
+            const float4 e = veval[ib];
+            pairdata[2 * (size_t)ib] = make_float4(pb.x, pb.y, pb.z, sb);
+            pairdata[2 * (size_t)ib + 1] = make_float4(e.x, e.y, e.z, 0.0f);
+        }
+    }
+}
+
+// ---- force + advance ----------------------------------------------------------
+// The hits of one lane's point among the group's candidates: bit u set when
+// candidate g + u passes 0 < d^2 < rd2 (the density pass's test, same
+// positions, same rounding).
+__device__ __forceinline__ uint32_t hit_bits(const DevParams &P, const float4 (*ring)[2], uint32_t g, uint32_t count,
+                                             float4 p) {
+    uint32_t h = 0;
+#pragma unroll 4
+    for (uint32_t u = 0; u < count; u++) {
+        const float4 q = ring[(g + u) & (kRing - 1u)][0];
+        const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+        const float dsq = dx * dx + dy * dy + dz * dz;
+        h |= (dsq < P.rd2 && dsq > 0.0f) ? (1u << u) : 0u;
+    }
+    return h;
+}
+
+__device__ __forceinline__ void add_hits(const DevParams &P, const float4 (*ring)[2], uint32_t g, uint32_t h,
+                                         ForcePoint &fp) {
+    while (h) {
+        const uint32_t u = (uint32_t)(__ffs(h) - 1);
+        h &= h - 1u;
+        const float4 *rec = ring[(g + u) & (kRing - 1u)];
+        const float4 q = rec[0];
+        add_pair_terms(P, fp, q, rec[1], q.w);
+    }
+}
+
+__device__ __forceinline__ void load_point(const DevParams &P, ForcePoint &fp, bool valid, uint32_t i,
+                                           const float4 *__restrict__ pos, const float4 *__restrict__ veval,
+                                           const float *__restrict__ press) {
+    fp.f = make_float3(0.0f, 0.0f, 0.0f);
+    if (valid) {
+        fp.p = pos[i];
+        fp.vi = veval[i];
+        fp.di = press[i];
+    } else {
+        fp.p = make_float4(0.f, 0.f, 0.f, 0.f);
+        fp.vi = fp.p;
+        fp.di = 1.0f;
+    }
+    fp.pi = (fp.di - P.prest_dens) * P.pintstiff;
+}
+
+struct ForceOut {
+    float4 *vel, *force, *pos_out, *veval_out;
+    float *host_pos;      // optional page-locked host copy of the new positions (float x3)
+    uint32_t *err;
+};
+
+// The advance of one in-range point from its force (fluid_kernels.cu:332-420);
+// returns the new position.
+__device__ __forceinline__ float3 finish_point(const DevParams &P, float time, float dt, uint32_t i,
+                                               const ForcePoint &fp, const ForceOut &o) {
+    o.force[i] = f4(fp.f);
+    float3 po, vo, eo;
+    advance_point(P, time, dt, P.sim_scale, fp.f, xyz(fp.p), xyz(o.vel[i]), xyz(fp.vi), po, vo, eo);
+    if (!(isfinite(po.x) && isfinite(po.y) && isfinite(po.z))) atomicOr(o.err, FL_DEV_NONFINITE);
+    o.pos_out[i] = f4(po);
+    o.vel[i] = f4(vo);
+    o.veval_out[i] = f4(eo);
+    return po;
+}
+
+// An out-of-range point: no force, parked at (-1000, -1000, -1000) with zero
+// velocity (advanceParticles, cu:339-342).
+__device__ __forceinline__ float3 park_point(uint32_t i, const float4 *__restrict__ veval, const ForceOut &o) {
+    o.force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    o.pos_out[i] = make_float4(-1000.f, -1000.f, -1000.f, 0.f);
+    o.vel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    o.veval_out[i] = veval[i];
+    return make_float3(-1000.f, -1000.f, -1000.f);
+}
+
+// The new positions of `count` (<= 32) consecutive slots from s, packed
+// float x3 into page-locked host memory: staged in shared memory so that
+// each store instruction of the warp writes 128 contiguous bytes.
+__device__ __forceinline__ void host_store(float *host, uint32_t s, uint32_t count, float3 v, float *stage) {
+    const unsigned lane = lane_id();
+    __syncwarp();
+    stage[3 * lane] = v.x; stage[3 * lane + 1] = v.y; stage[3 * lane + 2] = v.z;
+    __syncwarp();
+    for (uint32_t e = lane; e < 3u * count; e += 32u) host[3 * (size_t)s + e] = stage[e];
+    __syncwarp();
+}
+
+template <bool BATCH>
+__global__ void __launch_bounds__(kCellThreads)
+k_force_cells(const __grid_constant__ DevParams P0, const SceneTab T, const uint2 *__restrict__ tasks,
+              uint32_t cap, uint32_t *counters, float *time_dev, int slot, float dt, const float4 *__restrict__ pos_in,
+              const float4 *__restrict__ veval_in, const float *__restrict__ press,
+              const uint32_t *__restrict__ off, const uint32_t *__restrict__ cnt,
+              const uint32_t *__restrict__ upbits, const float4 *__restrict__ pairdata,
+              const __grid_constant__ ForceOut o) {
+    __shared__ float4 s_ring[kCellThreads / 32][kRing][2];
+    const unsigned lane = lane_id();
+    float4 (*ring)[2] = s_ring[threadIdx.x >> 5];
+    const float time = time_dev[slot];
+    if (blockIdx.x == 0 && threadIdx.x == 0) time_dev[slot ^ 1] = time + dt;
+    const uint32_t ntasks = min(counters[0], cap);   // k_make_tasks flags an overflow
+    for (;;) {
+        uint32_t t = 0;
+        if (lane == 0) t = atomicAdd(&counters[2], 1u);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= ntasks) return;
+        const uint2 task = tasks[t];
+        const int c = (int)task.y;
+        const DevParams &P = BATCH ? T.params[T.cell_scene[c]] : P0;
+        const uint32_t mt = min((uint32_t)kTaskPoints, off[c] + cnt[c] - task.x);
+        const uint32_t ia = task.x + lane, ib = ia + 32u;
+        const bool va = lane < mt, vb = lane + 32u < mt;
+        float3 na = make_float3(0.f, 0.f, 0.f), nb = na;
+        if (c - P.cell_base == P.ncells) {   // the out-of-range bin
+            if (va) na = park_point(ia, veval_in, o);
+            if (vb) nb = park_point(ib, veval_in, o);
+        } else {
+            ForcePoint fa, fb;
+            load_point(P, fa, va, ia, pos_in, veval_in, press);
+            load_point(P, fb, vb, ib, pos_in, veval_in, press);
+            const uint32_t need = needed_entries(va, __float_as_uint(fa.p.w), vb, __float_as_uint(fb.p.w));
+            const bool dual = mt > 32u;
+            auto stage = [&](uint32_t r, uint32_t j) {
+                ring[r][0] = pairdata[2 * (size_t)j];
+                ring[r][1] = pairdata[2 * (size_t)j + 1];
+            };
+            walk_union(P, c, need, off, cnt, upbits, stage, [&](uint32_t g, uint32_t count) {
+                const uint32_t ha = va ? hit_bits(P, ring, g, count, fa.p) : 0u;
+                const uint32_t hb = (dual && vb) ? hit_bits(P, ring, g, count, fb.p) : 0u;
+                add_hits(P, ring, g, ha, fa);
+                add_hits(P, ring, g, hb, fb);
+            });
+            if (va) na = finish_point(P, time, dt, ia, fa, o);
+            if (vb) nb = finish_point(P, time, dt, ib, fb, o);
+        }
+        if (o.host_pos) {
+            float *st = reinterpret_cast<float *>(ring);   // the ring is free once the walk is done
+            host_store(o.host_pos, task.x, min(mt, 32u), na, st);
+            if (mt > 32u) host_store(o.host_pos, ib - lane, mt - 32u, nb, st);
+        }
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Launch wrappers.
+
+size_t fl_task_cap(int max_points, int gcells) {
+    const size_t n = (size_t)(max_points > 0 ? max_points : 1);
+    return n / kTaskPoints + std::min(n, (size_t)gcells) + 32;
+}
+
+static int resident_blocks(const void *kern) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCellThreads, 0) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    return per_sm;
+}
+
+// Grids of the two passes: every block resident at once (queried once, at
+// system creation, outside any stream capture).
+int fl_cells_init(fl_system *s) {
+    const int d = s->batched ? resident_blocks((const void *)k_density_cells<true>)
+                             : resident_blocks((const void *)k_density_cells<false>);
+    const int f = s->batched ? resident_blocks((const void *)k_force_cells<true>)
+                             : resident_blocks((const void *)k_force_cells<false>);
+    s->cells_grid[0] = d * s->num_sms;
+    s->cells_grid[1] = f * s->num_sms;
+    return FL_OK;
+}
+
+int fl_launch_make_tasks(fl_system *s) {
+    k_make_tasks<<<blocks_for((long long)s->gcells, 256), 256, 0, s->stream>>>(
+        s->gcells, s->off, s->cnt, s->tasks, (uint32_t)s->task_cap, s->task_counters, s->dev_err);
+    FL_LAUNCH_CHECK("make_tasks");
+    return FL_OK;
+}
+
+int fl_launch_density_cells(fl_system *s) {
+    if (s->n == 0) return FL_OK;
+    auto kern = s->batched ? k_density_cells<true> : k_density_cells<false>;
+    const int grid = s->cells_grid[0];
+    kern<<<grid, kCellThreads, 0, s->stream>>>(s->D, fl_scene_tab(s), s->tasks, (uint32_t)s->task_cap,
+                                                s->task_counters, s->f[F_POS].cur<float4>(), s->off, s->cnt, s->upbits,
+                                                s->f[F_VEVAL].cur<float4>(), s->f[F_PRESS].cur<float>(),
+                                                s->pairdata);
+    FL_LAUNCH_CHECK("density_cells");
+    return FL_OK;
+}
+
+int fl_launch_force_cells(fl_system *s, float dt, float *host_pos) {
+    auto kern = s->batched ? k_force_cells<true> : k_force_cells<false>;
+    const int grid = s->cells_grid[1];
+    ForceOut o;
+    o.vel = s->f[F_VEL].cur<float4>();
+    o.force = s->f[F_FORCE].cur<float4>();
+    o.pos_out = s->f[F_POS].nxt<float4>();
+    o.veval_out = s->f[F_VEVAL].nxt<float4>();
+    o.host_pos = host_pos;
+    o.err = s->dev_err;
+    kern<<<grid, kCellThreads, 0, s->stream>>>(s->D, fl_scene_tab(s), s->tasks, (uint32_t)s->task_cap,
+                                                s->task_counters, s->time_dev,
+                                                s->time_slot, dt, s->f[F_POS].cur<float4>(),
+                                                s->f[F_VEVAL].cur<float4>(), s->f[F_PRESS].cur<float>(), s->off,
+                                                s->cnt, s->upbits, s->pairdata, o);
+    FL_LAUNCH_CHECK("force_cells");
+    return FL_OK;
+}

@@ -127,6 +127,15 @@ struct fl_system {
     uint32_t *big_count;   // [0] their number, [1] k_sort_big's sign-off count (256 B slot, zeroed at creation)
     int num_sms;
 
+    // cell tasks of the fused step (fl_cells.cu): (first slot, cell entry)
+    // per 64 slots of a cell, listed every step; counters in the scan
+    // ticket's slot (cleared with the counts)
+    uint2 *tasks;
+    size_t task_cap;
+    uint32_t *task_counters;
+    int cell_passes;       // 1: the fused step uses the cell-task passes where it can
+    int cells_grid[2];     // blocks of the density and force cell passes (all resident)
+
     uint32_t *hitlist;     // ceil(N/32) * hcap * 32 entries
     uint32_t *hitcnt;      // per point
     // per slot, written with the lists: (pos.xyz, density), (veval.xyz, 0),
@@ -233,8 +242,13 @@ int fl_launch_adj_force(fl_system *s, const float2 *rr, const float4 *fb, float4
 int fl_launch_adj_density(fl_system *s, const uint32_t *revlist, const uint32_t *revcnt, const float *rb,
                           const float4 *xa, float4 *x_out, uint32_t *crowd, uint32_t *crowd_count);
 int fl_param_chunks(int max_scene_points);
+// acc += partial sums x 2^gexp (gexp null: x 1)
 int fl_launch_param_reduce(fl_system *s, const float4 *pc, const int *sbase, const int *sn, int nchunks,
-                           double *partial, double *acc);
+                           double *partial, const int *gexp, double *acc);
+// per scene: cotangents above 2^40 scaled by 2^-k, gexp += k (gmax zero on entry, left zero)
+int fl_launch_adj_rescale(fl_system *s, float4 *gx, float4 *gv, float4 *ge, uint32_t *gmax, int *gexp);
+// the cotangents times 2^gexp of their scene
+int fl_launch_adj_apply_exponent(fl_system *s, float4 *gx, float4 *gv, float4 *ge, const int *gexp);
 int fl_launch_compose(fl_system *s, int n, const uint32_t *src, const uint32_t *in, uint32_t *out);
 // dst[k][0..n) = src[k][0..n) for k < count (<= 3), one kernel pass
 int fl_launch_copy3(fl_system *s, int n, int count, const float4 *const *src, float4 *const *dst);
@@ -278,6 +292,14 @@ int fl_conservation_chunks(int max_scene_points);
 int fl_launch_conservation(fl_system *s, const int *sbase, const int *sn, int nchunks, double *partial);
 int fl_launch_sample_volume(fl_system *s, const int res[3], const float bmin[3], const float bmax[3],
                             float scalar, float gausskern, float h2, float *out);
+// cell-task passes of the fused step (fl_cells.cu)
+size_t fl_task_cap(int max_points, int gcells);
+int fl_cells_init(fl_system *s);   // after num_sms and batched are set
+int fl_launch_make_tasks(fl_system *s);
+int fl_launch_density_cells(fl_system *s);
+// force + advance over the tasks; host_pos (device-usable pointer to
+// page-locked host memory, or null) also receives the new positions as float x3
+int fl_launch_force_cells(fl_system *s, float dt, float *host_pos);
 size_t fl_scan_tile();
 size_t fl_upbits_bytes(const fl_system *s);
 size_t fl_scan_scratch_bytes(int ntiles);

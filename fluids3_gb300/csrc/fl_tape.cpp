@@ -19,6 +19,9 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <math.h>
+#include <vector>
+
 #include "fl_internal.h"
 
 struct fl_tape {
@@ -40,6 +43,8 @@ struct fl_tape {
     uint32_t *crowd, *crowd_count; // points whose pair lists overflowed (count cleared per reverse step)
     int nchunks;
     double *partial, *acc;  // per-scene parameter gradients (visc, rest density, IntStiff)
+    uint32_t *gmax;         // per scene: largest cotangent component of the last reverse step (float bits)
+    int *gexp;              // per scene: the cotangents are the gradient times 2^-gexp
     int *sbase, *sn;
     void *save[F_COUNT];    // the live state when fl_backward starts, restored at its end
     float *save_time;
@@ -64,6 +69,7 @@ static void tape_release(fl_tape *t) {
     cudaFree(t->revlist); cudaFree(t->revcnt); cudaFree(t->rr);
     cudaFree(t->crowd); cudaFree(t->crowd_count);
     cudaFree(t->partial); cudaFree(t->acc); cudaFree(t->sbase); cudaFree(t->sn);
+    cudaFree(t->gmax); cudaFree(t->gexp);
     for (int k = 0; k < F_COUNT; k++) cudaFree(t->save[k]);
     cudaFree(t->save_time);
     cudaFree(t->seg_list); cudaFree(t->seg_cnt); cudaFree(t->seg_rho);
@@ -174,6 +180,8 @@ extern "C" int fl_tape_begin_ex(fl_system *s, int max_steps, int every, int flag
         if ((r = fl_dalloc((void **)&t->acc, 24 * (size_t)s->nscenes)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&t->sbase, 4 * (size_t)s->nscenes)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&t->sn, 4 * (size_t)s->nscenes)) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&t->gmax, 4 * (size_t)s->nscenes)) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&t->gexp, 4 * (size_t)s->nscenes)) != FL_OK) break;
         for (int k = 0; k < F_COUNT && r == FL_OK; k++) r = fl_dalloc(&t->save[k], s->f[k].esz * cap);
         if (r != FL_OK) break;
         if ((r = fl_dalloc((void **)&t->save_time, 256)) != FL_OK) break;
@@ -312,7 +320,8 @@ static int backward_step(fl_system *s, fl_tape *t, const float4 *state, const fl
                                    t->revcnt, t->crowd, t->crowd_count));
         FL_TRY(fl_launch_adj_density(s, t->revlist, t->revcnt, t->rb, t->xa, t->g[x][0], t->crowd,
                                      t->crowd_count));
-        FL_TRY(fl_launch_param_reduce(s, t->pc, t->sbase, t->sn, t->nchunks, t->partial, t->acc));
+        FL_TRY(fl_launch_param_reduce(s, t->pc, t->sbase, t->sn, t->nchunks, t->partial, t->gexp, t->acc));
+        FL_TRY(fl_launch_adj_rescale(s, t->g[x][0], t->g[x][1], t->g[x][2], t->gmax, t->gexp));
         return FL_OK;
     }();
     s->hitlist = own_list;
@@ -342,13 +351,16 @@ static int run_reverse(fl_system *s, fl_tape *t) {
             FL_CUDA_TRY(cudaMemcpyAsync(s->time_dev + s->time_slot, t->time + k, sizeof(float),
                                         cudaMemcpyDeviceToDevice, s->stream));
             uint32_t *own_list = s->hitlist, *own_cnt = s->hitcnt;
-            if (t->keep_lists) {   // the step's density pass writes its lists into the slot
+            const int own_passes = s->cell_passes;
+            if (t->keep_lists) {   // the step's (per-point) density pass writes its lists into the slot
                 s->hitlist = t->seg_list + (size_t)(k - t0) * t->list_words;
                 s->hitcnt = t->seg_cnt + (size_t)(k - t0) * t->cap;
+                s->cell_passes = 0;
             }
             const int r = fl_step_fused(s);
             s->hitlist = own_list;
             s->hitcnt = own_cnt;
+            s->cell_passes = own_passes;
             FL_TRY(r);
             FL_TRY(save_force(s, t->force + (size_t)(k - t0) * t->cap));
             if (t->keep_lists && s->n)
@@ -362,8 +374,12 @@ static int run_reverse(fl_system *s, fl_tape *t) {
     return FL_OK;
 }
 
-extern "C" int fl_backward(fl_system *s, const float *dpos, const float *dvel, const float *dveval,
-                           float *gpos, float *gvel, float *gveval, double *gparams) {
+// The reverse pass; the state gradients come back as mantissas with a
+// per-scene binary exponent in `exps` (host, nscenes entries).
+// With apply_exponent the mantissas are multiplied by 2^exponent on the
+// device first (in float: infinite where the gradient overflows it).
+static int backward_impl(fl_system *s, const float *dpos, const float *dvel, const float *dveval, float *gpos,
+                         float *gvel, float *gveval, double *gparams, int *exps, bool apply_exponent) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_backward: null system");
     fl_tape *t = s->tape;
     if (!t) return fl_fail(FL_ERR_STATE, "fl_backward: no tape (fl_tape_begin)");
@@ -401,6 +417,8 @@ extern "C" int fl_backward(fl_system *s, const float *dpos, const float *dvel, c
                            cudaGetErrorString(e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3)));
     }
     FL_CUDA_TRY(cudaMemsetAsync(t->acc, 0, 24 * (size_t)s->nscenes, s->stream));
+    FL_CUDA_TRY(cudaMemsetAsync(t->gmax, 0, 4 * (size_t)s->nscenes, s->stream));
+    FL_CUDA_TRY(cudaMemsetAsync(t->gexp, 0, 4 * (size_t)s->nscenes, s->stream));
     t->gcur = 0;
     FL_TRY(upload_vec3(s, dpos, t->g[0][0]));
     FL_TRY(upload_vec3(s, dvel, t->g[0][1]));
@@ -425,11 +443,27 @@ extern "C" int fl_backward(fl_system *s, const float *dpos, const float *dvel, c
     s->codes_valid = s->lists_valid = 0;
     if (r != FL_OK) return r;
 
+    if (apply_exponent)
+        FL_TRY(fl_launch_adj_apply_exponent(s, t->g[t->gcur][0], t->g[t->gcur][1], t->g[t->gcur][2], t->gexp));
     FL_TRY(download_vec3(s, t->g[t->gcur][0], gpos));
     FL_TRY(download_vec3(s, t->g[t->gcur][1], gvel));
     FL_TRY(download_vec3(s, t->g[t->gcur][2], gveval));
     if (gparams)
         FL_CUDA_TRY(cudaMemcpyAsync(gparams, t->acc, 24 * (size_t)s->nscenes, cudaMemcpyDeviceToHost, s->stream));
+    FL_CUDA_TRY(cudaMemcpyAsync(exps, t->gexp, 4 * (size_t)s->nscenes, cudaMemcpyDeviceToHost, s->stream));
     FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
     return FL_OK;
+}
+
+extern "C" int fl_backward_scaled(fl_system *s, const float *dpos, const float *dvel, const float *dveval,
+                                  float *gpos, float *gvel, float *gveval, double *gparams, int *exponents) {
+    if (!s || !exponents) return fl_fail(FL_ERR_ARG, "fl_backward_scaled: null system or exponents");
+    return backward_impl(s, dpos, dvel, dveval, gpos, gvel, gveval, gparams, exponents, false);
+}
+
+extern "C" int fl_backward(fl_system *s, const float *dpos, const float *dvel, const float *dveval,
+                           float *gpos, float *gvel, float *gveval, double *gparams) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_backward: null system");
+    std::vector<int> e((size_t)(s->nscenes > 0 ? s->nscenes : 1), 0);
+    return backward_impl(s, dpos, dvel, dveval, gpos, gvel, gveval, gparams, e.data(), true);
 }

@@ -329,6 +329,19 @@ class FluidSystem:
             call("fl_tape_order", self._h, _ptr(out))
         return out
 
+    def BackwardScaled(self, dpos=None, dvel=None, dveval=None):
+        """Backward for long rollouts (fl_backward_scaled): returns (gpos,
+        gvel, gveval, gparams, exponents) with the state gradients as
+        mantissas; the gradient of scene k is mantissa * 2**exponents[k]."""
+        n = self.NumPoints()
+        keep = [None if a is None else np.ascontiguousarray(a, dtype=np.float32).reshape(n, 3)
+                for a in (dpos, dvel, dveval)]
+        outs = [np.empty((n, 3), np.float32) for _ in range(3)]
+        gp = np.zeros((self.NumScenes(), 3), np.float64)
+        ex = np.zeros(self.NumScenes(), np.int32)
+        call("fl_backward_scaled", self._h, *[_ptr(a) for a in keep], *[_ptr(o) for o in outs], _ptr(gp), _ptr(ex))
+        return outs[0], outs[1], outs[2], gp, ex
+
     def Backward(self, dpos=None, dvel=None, dveval=None, want_state: bool = True):
         """Reverse pass over the recorded steps. ``d*``: dL/d(final pos, vel,
         veval) as (N,3) arrays in the current slot order (None = zero), or device
@@ -379,6 +392,15 @@ class FluidSystem:
         after an Autotune in an earlier run."""
         shapes = (C.c_int * 4)(int(density), int(force), int(sort), int(sort_cells))
         call("fl_set_launch_shapes", self._h, shapes)
+
+    def SetNeighbourPasses(self, mode: str) -> None:
+        """"cells" (default): one warp per 64 points of a cell walks their shared
+        search block in lockstep; "points": one thread per point (the
+        reference's loop structure). Results are bit-identical."""
+        call("fl_set_neighbour_passes", self._h, {"points": 0, "cells": 1}[mode])
+
+    def NeighbourPasses(self) -> str:
+        return ("points", "cells")[call("fl_neighbour_passes", self._h)]
 
     # -- timing ---------------------------------------------------------------
     def SetTiming(self, enable: bool) -> None:

@@ -333,6 +333,21 @@ int fl_launch_shapes(fl_system *s, int *shapes);
  * identical for every shape. */
 int fl_set_launch_shapes(fl_system *s, const int *shapes);
 
+/* Which neighbour passes the fused step (fl_run, fl_run_steps,
+ * fl_run_from_host) uses; both give bit-identical results.
+ * FL_PASSES_CELL_TASKS (the default): one warp per 64 points of a cell walks
+ * their shared search block once, in lockstep, staged in shared memory;
+ * used where the pruned search applies (gridSrch 2 in every scene) and no
+ * tape is recording. FL_PASSES_PER_POINT: one thread per point walks its
+ * own search block (fluids4.0/fluid_kernels.cu:112-149, 180-217 as
+ * written), recording pair lists for the force pass; always used by the
+ * phase entry points, recording tapes and gridSrch > 2. No counterpart in
+ * the reference (which has only the per-point walk). */
+#define FL_PASSES_PER_POINT  0
+#define FL_PASSES_CELL_TASKS 1
+int fl_set_neighbour_passes(fl_system *s, int mode);
+int fl_neighbour_passes(const fl_system *s);
+
 /* Wait for the system stream; returns FL_ERR_DEVICE if a kernel raised the
  * device error word since the last fl_sync (bits in *dev_flags if non-NULL). */
 int fl_sync(fl_system *s);
@@ -398,6 +413,18 @@ int fl_tape_begin(fl_system *s, int max_steps, int every);
 int fl_tape_begin_ex(fl_system *s, int max_steps, int every, int flags);
 int fl_tape_steps(const fl_system *s);
 int fl_tape_order(fl_system *s, uint32_t *order);
+/* fl_backward_scaled: fl_backward for long rollouts, whose exact gradient
+ * grows about 1.4x per step (nearby trajectories diverge) and leaves the
+ * FP32 range after a few hundred steps. The reverse pass scales each
+ * scene's cotangents by a power of two whenever their largest component
+ * passes 2^40 (exact: every reverse operation is linear in them), so
+ * nothing overflows; gpos/gvel/gveval receive the mantissas and
+ * exponents[scene] (nscenes ints, host) the binary exponent: the gradient
+ * is mantissa * 2^exponent. gparams are the full FP64 values. fl_backward
+ * itself returns mantissa * 2^exponent in float (infinite where that
+ * overflows); both give identical bits wherever no scaling happened. */
+int fl_backward_scaled(fl_system *s, const float *dpos, const float *dvel, const float *dveval,
+                       float *gpos, float *gvel, float *gveval, double *gparams, int *exponents);
 int fl_backward(fl_system *s, const float *dpos, const float *dvel, const float *dveval,
                 float *gpos, float *gvel, float *gveval, double *gparams);
 int fl_tape_end(fl_system *s);

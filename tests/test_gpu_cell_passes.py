@@ -1,0 +1,156 @@
+"""The cell-task neighbour passes (fl_cells.cu) against the per-point passes.
+
+The fused step walks each cell's shared search block once per 64 of its
+points, in lockstep, instead of once per point. Every point's sum must keep
+the reference's terms and order, so both passes give bit-identical states:
+checked over many steps on the wave tank, on crowded cells (tasks of one
+cell split over many warps, unions of thousands of candidates), on cells of
+1..64 points (one and two points per lane), on batches, through graph
+replay and through fl_run_from_host (whose force pass also writes the new
+positions into the caller's page-locked array), and against the oracle
+step by step.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import fluids3_gb300 as F
+from fluids3_gb300 import scenes
+from oracle import oracle as O
+
+from helpers import FIELDS, assert_bit_equal
+
+pytestmark = pytest.mark.gpu
+UNDEF = 0xFFFFFFFF
+
+
+def run_both(params, pos, vel, veval, clr, steps, graph=True):
+    out = {}
+    for mode in ("points", "cells"):
+        with F.FluidSystem(params, pos.shape[0]) as s:
+            s.SetParticles(pos, vel, veval, clr=clr)
+            s.SetNeighbourPasses(mode)
+            assert s.NeighbourPasses() == mode
+            if graph:
+                s.RunSteps(steps)
+            else:
+                for _ in range(steps):
+                    s.Run()
+            s.Sync()
+            assert s.IntegrityCheck() == 0
+            out[mode] = s.state()
+    return out["points"], out["cells"]
+
+
+def assert_states_equal(a, b, what):
+    for k in FIELDS + ("gridcnt", "gridoff"):
+        assert_bit_equal(b[k], a[k], f"{what}: {k}")
+
+
+def test_cells_equal_points_on_the_wave_tank():
+    sc = scenes.wave_tank(n=300_000)
+    a, b = run_both(sc.params, sc.pos, sc.vel, sc.veval, sc.clr, 40)
+    assert_states_equal(a, b, "wave tank, 40 steps")
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_cells_equal_points_on_the_dam_break(graph):
+    sc = scenes.dam_break()
+    a, b = run_both(sc.params, sc.pos, sc.vel, sc.veval, sc.clr, 30, graph=graph)
+    assert_states_equal(a, b, "dam break, 30 steps")
+
+
+@pytest.mark.parametrize("m", [1, 31, 32, 33, 63, 64, 65, 129, 700, 3000])
+def test_cells_equal_points_with_a_crowded_cell(m):
+    """m points packed into one cell among a dam break: tasks of 1..64
+    points, a cell split into several tasks, unions of thousands."""
+    sc = scenes.dam_break(n=6000, seed=31)
+    p = sc.params
+    rng = np.random.default_rng(100 + m)
+    pos = sc.pos.copy()
+    pick = rng.choice(pos.shape[0], size=m, replace=False)
+    c = np.array([p.gridMin[0] + 7.5 * 5.0, p.gridMin[1] + 5.5 * 5.0, p.gridMin[2] + 6.5 * 5.0], np.float32)
+    pos[pick] = c + rng.uniform(-2.4, 2.4, size=(m, 3)).astype(np.float32)
+    a, b = run_both(p, pos, sc.vel, sc.veval, sc.clr, 4)
+    assert_states_equal(a, b, f"crowded cell of {m}")
+
+
+def test_cells_match_the_oracle_step_by_step():
+    sc = scenes.dam_break(n=20_000, seed=4)
+    p = sc.params
+    with F.FluidSystem(p, sc.n) as s:
+        s.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
+        assert s.NeighbourPasses() == "cells"
+        s.RunSteps(40)
+        s.Sync()
+        for _ in range(3):
+            st0 = s.state()
+            ref = O.State.new(p, st0["pos"], st0["vel"], st0["veval"], st0["clr"])
+            O.step(p, ref, s.time, threads=8)
+            s.Run()
+            s.Sync()
+            st = s.state()
+            for k in FIELDS:
+                assert_bit_equal(st[k], getattr(ref, k), k)
+
+
+def test_cells_equal_points_on_a_batch():
+    scs = scenes.batch_scenes(nscenes=12, seed=23, nmin=500, nmax=20000)
+    cat = scenes.concat(scs)
+    out = {}
+    for mode in ("points", "cells"):
+        with F.FluidSystem.batch([sc.params for sc in scs], [sc.n for sc in scs]) as b:
+            b.SetParticles(cat["pos"], cat["vel"], cat["veval"], clr=cat["clr"])
+            b.SetNeighbourPasses(mode)
+            b.RunSteps(25)
+            b.Sync()
+            out[mode] = b.state()
+    assert_states_equal(out["points"], out["cells"], "batch of 12, 25 steps")
+
+
+def test_cells_with_escaped_points_and_nan():
+    sc = scenes.dam_break(n=3000, seed=12)
+    pos = sc.pos.copy()
+    pos[:4] = [(-500.0, 1.0, 1.0), (1.0, -300.0, 1.0), (np.nan, 0.0, 0.0), (1e30, 1e30, 1e30)]
+    a, b = run_both(sc.params, pos, sc.vel, sc.veval, sc.clr, 3)
+    assert_states_equal(a, b, "escapes")
+    assert (b["gcell"] == UNDEF).sum() >= 4
+
+
+def test_run_from_host_with_cells_writes_positions_back():
+    """fl_run_from_host's force pass writes the new positions into the
+    caller's page-locked array as it goes: equal to the device state and to
+    the per-point path's step."""
+    import ctypes as C
+    sc = scenes.wave_tank(n=150_000)
+    n = sc.n
+    pins = {k: F.PinnedArray((n, 3), np.float32) for k in ("pos", "vel", "veval", "out")}
+    clr = F.PinnedArray((n,), np.uint32)
+    pins["pos"].array[:] = sc.pos
+    pins["vel"].array[:] = sc.vel
+    pins["veval"].array[:] = sc.veval
+    clr.array[:] = sc.clr
+    lib = F.lib()
+    vp = lambda a: a.ctypes.data_as(C.c_void_p)
+    try:
+        with F.FluidSystem(sc.params, n) as s:
+            assert s.NeighbourPasses() == "cells"
+            pins["out"].array[:] = np.nan
+            F._lib.check("fl_run_from_host", lib.fl_run_from_host(
+                s.handle, n, vp(pins["pos"].array), vp(pins["vel"].array), vp(pins["veval"].array),
+                vp(clr.array), vp(pins["out"].array)))
+            got_host = pins["out"].array.copy()
+            got = s.state()
+        assert_bit_equal(got_host, got["pos"], "host copy of the new positions")
+        with F.FluidSystem(sc.params, n) as s:
+            s.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
+            s.SetNeighbourPasses("points")
+            s.Run()
+            s.Sync()
+            want = s.state()
+        for k in FIELDS:
+            assert_bit_equal(got[k], want[k], f"run_from_host vs per-point step: {k}")
+    finally:
+        for a in list(pins.values()) + [clr]:
+            a.free()

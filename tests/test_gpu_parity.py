@@ -685,9 +685,11 @@ def test_run_from_host_equals_set_particles_then_run(case):
             p.free()
 
 
-def test_run_from_host_reads_back_in_slot_ranges():
-    """Above 2^21 points the force pass of fl_run_from_host runs in slot
-    ranges whose positions go back while the next range computes: the
+@pytest.mark.parametrize("passes", ["points", "cells"])
+def test_run_from_host_reads_back_in_slot_ranges(passes):
+    """Above 2^21 points the per-point force pass of fl_run_from_host runs
+    in slot ranges whose positions go back while the next range computes
+    (the cell-task force pass writes them to host memory as it goes): the
     positions read back and the state still equal SetParticles + Run +
     GetBuffer."""
     sc = scenes.wave_tank(n=2_200_000)
@@ -699,7 +701,9 @@ def test_run_from_host_reads_back_in_slot_ranges():
             pins[k].array[:] = a
         with F.FluidSystem(sc.params, n) as a, F.FluidSystem(sc.params, n) as b:
             a.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
+            a.SetNeighbourPasses("points")
             a.Run()
+            b.SetNeighbourPasses(passes)
             b.RunFromHost(pins["pos"].array, pins["vel"].array, pins["veval"].array, clr=pins["clr"].array,
                           pos_out=pins["out"].array)
             sa, sb = gpu_state(a), gpu_state(b)
