@@ -23,8 +23,9 @@
 //    bit-identical to the per-point walk.
 //
 // The density pass evaluates two points per lane with packed f32x2
-// arithmetic (add/sub/mul.rn.f32x2: IEEE round-to-nearest per element, the
-// same results as scalar operations) when a task has more than 32 points.
+// arithmetic (sub/mul.rn.f32x2: IEEE round-to-nearest per element, the same
+// results as scalar operations) when a task has more than 32 points; no
+// packed add ever takes two packed products (see density_group2).
 // The force pass stages each candidate's 32-byte pair record (position and
 // density, evaluated velocity; written by the density pass), tests the 32
 // candidates of a group for every lane, and then each lane adds its own
@@ -192,11 +193,18 @@ __device__ __forceinline__ void density_group2(const DevParams &P, const float4 
         const uint64_t dx = sub2(px, pk2(q.x, q.x));
         const uint64_t dy = sub2(py, pk2(q.y, q.y));
         const uint64_t dz = sub2(pz, pk2(q.z, q.z));
-        const uint64_t dsq = add2(add2(mul2(dx, dx), mul2(dy, dy)), mul2(dz, dz));
-        const uint64_t t = mul2(sub2(rd2, dsq), d2);
+        // The squares are summed in scalar: ptxas contracts a packed add of
+        // two packed products into a packed fused multiply-add (one rounding
+        // fewer), explicit .rn notwithstanding; the scalar adds of the
+        // unpacked squares round exactly as the reference's expression.
+        float xa, xb, ya, yb, za, zb;
+        up2(mul2(dx, dx), xa, xb);
+        up2(mul2(dy, dy), ya, yb);
+        up2(mul2(dz, dz), za, zb);
+        const float da = xa + ya + za, db = xb + yb + zb;
+        const uint64_t t = mul2(sub2(rd2, pk2(da, db)), d2);
         const uint64_t t3 = mul2(mul2(t, t), t);
-        float da, db, ta, tb;
-        up2(dsq, da, db);
+        float ta, tb;
         up2(t3, ta, tb);
         ta = (da < P.rd2 && da > 0.0f) ? ta : 0.0f;
         tb = (db < P.rd2 && db > 0.0f) ? tb : 0.0f;
