@@ -84,7 +84,7 @@ def parse():
     ap.add_argument("--n", type=int, default=4_000_000, help="points in the wave tank")
     ap.add_argument("--segment", type=int, default=50,
                     help="timed steps run as rollouts of at most this many steps from the warm state")
-    ap.add_argument("--long-steps", type=int, default=0,
+    ap.add_argument("--long-steps", type=int, default=300,
                     help="also time this many continuous steps from the warm state, per 100-step run")
     ap.add_argument("--e2e-steps", type=int, default=None, help="steps in the e2e region (default: min(K, 20))")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
@@ -99,6 +99,11 @@ def parse():
                     help="steps of the differentiated 65,536-point rollout (0 skips the adjoint section)")
     ap.add_argument("--adjoint-every", type=int, default=20, help="checkpoint interval of that rollout")
     ap.add_argument("--no-autotune", action="store_true", help="keep the compiled block shapes")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling run for ncu: the wave tank of --n points, --warmup eager steps, then "
+                         "--steps eager steps (one launch per kernel per step), no timing, no JSON line")
+    ap.add_argument("--passes", choices=["cells", "points"], default="cells",
+                    help="neighbour passes of the fused step (bit-identical results)")
     ap.add_argument("--fit-iters", type=int, default=40,
                     help="iterations of the 64-scene batched parameter fit (0 skips it)")
     return ap.parse_args()
@@ -672,6 +677,7 @@ def config_of(scene, args):
             "n_points": scene.n, "cells": p.gridTotal, "grid": list(p.gridRes),
             "l2": "inputs larger than L2 (state ~1 GB in HBM), no flush needed",
             "segment_steps": args.segment,
+            "neighbour_passes": getattr(args, "passes", "cells"),
             "step": "insert, scan, index scatter, canonical sort+gather, density, force+advance"}
 
 
@@ -706,6 +712,7 @@ def our_arm(args, rank, world, local_rank):
     p = scene.params
     s = F.FluidSystem(p, scene.n)
     s.SetParticles(scene.pos, scene.vel, scene.veval, clr=scene.clr)
+    s.SetNeighbourPasses(args.passes)
 
     # warm-up (untimed): graph capture + W steps; keep the state so the
     # per-kernel region below replays exactly the timed steps
@@ -884,9 +891,28 @@ def our_arm(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+def profile_run(args):
+    """Launches for a profiler: every step eager, so kernel k of step j is
+    launch j of that kernel (skip --warmup of them with ncu -s)."""
+    import fluids3_gb300 as F
+    from fluids3_gb300 import scenes
+    scene = scenes.wave_tank(n=args.n)
+    with F.FluidSystem(scene.params, scene.n) as s:
+        s.SetParticles(scene.pos, scene.vel, scene.veval, clr=scene.clr)
+        s.SetNeighbourPasses(args.passes)
+        for _ in range(args.warmup + args.steps):
+            s.Run()
+        s.Sync()
+        print(f"profile run: {scene.n:,} points, {args.warmup} + {args.steps} eager steps ({args.passes} passes), "
+              f"device status {s.DeviceStatus()}", flush=True)
+
+
 def main():
     args = parse()
     rank, world, local_rank = dist_env()
+    if args.profile:
+        profile_run(args)
+        return
     if args.impl == "reference":
         reference_arm(args, rank, world)
         return

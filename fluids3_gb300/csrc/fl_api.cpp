@@ -905,6 +905,12 @@ int fl_rebuild_grid(fl_system *s) {
 
 int fl_recompute_step(fl_system *s) {
     FL_TRY(fl_rebuild_grid(s));
+    if (use_cell_passes(s, false)) {   // the cell-task density, writing per-point pair lists
+        FL_TRY(fl_launch_make_tasks(s));
+        FL_TRY(fl_launch_density_cells(s, true));
+        s->lists_valid = 1;
+        return FL_OK;
+    }
     FL_TRY(fl_launch_density(s));
     return FL_OK;
 }

@@ -170,8 +170,10 @@ __device__ __forceinline__ void walk_union(const DevParams &P, int c, uint32_t n
 // Candidates of one group against one point per lane (a), in order. A
 // candidate that fails the test adds +0, which leaves the (non-negative)
 // sum unchanged.
-__device__ __forceinline__ void density_group1(const DevParams &P, const float4 *ring, uint32_t g, uint32_t count,
-                                               float4 pa, float &sa) {
+// Returns the group's hit mask (bit u: candidate g + u passed the test).
+__device__ __forceinline__ uint32_t density_group1(const DevParams &P, const float4 *ring, uint32_t g,
+                                                   uint32_t count, float4 pa, float &sa) {
+    uint32_t ma = 0;
 #pragma unroll 4
     for (uint32_t u = 0; u < count; u++) {
         const float4 q = ring[(g + u) & (kRing - 1u)];
@@ -179,13 +181,18 @@ __device__ __forceinline__ void density_group1(const DevParams &P, const float4 
         const float dsq = dx * dx + dy * dy + dz * dz;
         const float t = (P.rd2 - dsq) * P.d2;
         const float t3 = t * t * t;
-        sa += (dsq < P.rd2 && dsq > 0.0f) ? t3 : 0.0f;
+        const bool hit = dsq < P.rd2 && dsq > 0.0f;
+        sa += hit ? t3 : 0.0f;
+        ma |= (hit ? 1u : 0u) << u;
     }
+    return ma;
 }
 
 // The same for two points per lane (a, b), in packed f32x2 arithmetic.
 __device__ __forceinline__ void density_group2(const DevParams &P, const float4 *ring, uint32_t g, uint32_t count,
-                                               uint64_t px, uint64_t py, uint64_t pz, uint64_t &sab) {
+                                               uint64_t px, uint64_t py, uint64_t pz, uint64_t &sab,
+                                               uint32_t &ma, uint32_t &mb) {
+    ma = mb = 0;
     const uint64_t rd2 = pk2(P.rd2, P.rd2), d2 = pk2(P.d2, P.d2);
 #pragma unroll 4
     for (uint32_t u = 0; u < count; u++) {
@@ -206,18 +213,38 @@ __device__ __forceinline__ void density_group2(const DevParams &P, const float4 
         const uint64_t t3 = mul2(mul2(t, t), t);
         float ta, tb;
         up2(t3, ta, tb);
-        ta = (da < P.rd2 && da > 0.0f) ? ta : 0.0f;
-        tb = (db < P.rd2 && db > 0.0f) ? tb : 0.0f;
+        const bool ha = da < P.rd2 && da > 0.0f, hb = db < P.rd2 && db > 0.0f;
+        ta = ha ? ta : 0.0f;
+        tb = hb ? tb : 0.0f;
         sab = add2(sab, pk2(ta, tb));
+        ma |= (ha ? 1u : 0u) << u;
+        mb |= (hb ? 1u : 0u) << u;
     }
 }
 
-template <bool BATCH>
+// Pair lists in the per-point passes' layout (list_at: the first hcap hits
+// of a point in visiting order; hitcnt: the count of all of them) from one
+// group's hit mask. The slot of each staged candidate rides in its .w.
+__device__ __forceinline__ void list_hits(const DevParams &P, const float4 *ring, uint32_t g, uint32_t h, uint32_t i,
+                                          uint32_t &nh, uint32_t *__restrict__ hitlist) {
+    while (h) {
+        const uint32_t u = (uint32_t)(__ffs(h) - 1);
+        h &= h - 1u;
+        if (nh < (uint32_t)P.hcap) hitlist[list_at(P, (int)i, nh)] = __float_as_uint(ring[(g + u) & (kRing - 1u)].w);
+        nh++;
+    }
+}
+
+// LIST: the adjoint's rebuilt steps, whose reverse kernels read per-point
+// pair lists and counts (hitlist, hitcnt): the same lists the per-point
+// density pass writes.
+template <bool BATCH, bool LIST>
 __global__ void __launch_bounds__(kCellThreads)
 k_density_cells(const __grid_constant__ DevParams P0, const SceneTab T, const uint2 *__restrict__ tasks,
                 uint32_t cap, uint32_t *counters, const float4 *__restrict__ pos, const uint32_t *__restrict__ off,
                 const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
-                const float4 *__restrict__ veval, float *__restrict__ press, float4 *__restrict__ pairdata) {
+                const float4 *__restrict__ veval, float *__restrict__ press, float4 *__restrict__ pairdata,
+                uint32_t *__restrict__ hitlist, uint32_t *__restrict__ hitcnt) {
     __shared__ float4 s_ring[kCellThreads / 32][kRing];
     const unsigned lane = lane_id();
     float4 *ring = s_ring[threadIdx.x >> 5];
@@ -236,22 +263,37 @@ k_density_cells(const __grid_constant__ DevParams P0, const SceneTab T, const ui
         if (c - P.cell_base == P.ncells) {   // the out-of-range bin: density 0
             if (va) press[ia] = 0.0f;
             if (vb) press[ib] = 0.0f;
+            if (LIST && va) hitcnt[ia] = 0;
+            if (LIST && vb) hitcnt[ib] = 0;
             continue;
         }
         const float4 pa = va ? pos[ia] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float4 pb = vb ? pos[ib] : make_float4(0.f, 0.f, 0.f, 0.f);
         const uint32_t need = needed_entries(va, __float_as_uint(pa.w), vb, __float_as_uint(pb.w));
-        auto stage = [&](uint32_t r, uint32_t j) { ring[r] = pos[j]; };
+        auto stage = [&](uint32_t r, uint32_t j) {
+            float4 q = pos[j];
+            q.w = __uint_as_float(j);   // the slot (band codes are not needed here)
+            ring[r] = q;
+        };
         float sa = 0.0f, sb = 0.0f;
+        uint32_t na = 0, nb = 0;
         if (mt > 32u) {   // two points per lane
             const uint64_t px = pk2(pa.x, pb.x), py = pk2(pa.y, pb.y), pz = pk2(pa.z, pb.z);
             uint64_t sab = pk2(0.0f, 0.0f);
-            walk_union(P, c, need, off, cnt, upbits, stage,
-                       [&](uint32_t g, uint32_t count) { density_group2(P, ring, g, count, px, py, pz, sab); });
+            walk_union(P, c, need, off, cnt, upbits, stage, [&](uint32_t g, uint32_t count) {
+                uint32_t ma, mb;
+                density_group2(P, ring, g, count, px, py, pz, sab, ma, mb);
+                if (LIST) {
+                    if (va) list_hits(P, ring, g, ma, ia, na, hitlist);
+                    if (vb) list_hits(P, ring, g, mb, ib, nb, hitlist);
+                }
+            });
             up2(sab, sa, sb);
         } else {
-            walk_union(P, c, need, off, cnt, upbits, stage,
-                       [&](uint32_t g, uint32_t count) { density_group1(P, ring, g, count, pa, sa); });
+            walk_union(P, c, need, off, cnt, upbits, stage, [&](uint32_t g, uint32_t count) {
+                const uint32_t ma = density_group1(P, ring, g, count, pa, sa);
+                if (LIST && va) list_hits(P, ring, g, ma, ia, na, hitlist);
+            });
         }
         // fluid_kernels.cu:146-148, and the pair records the force pass reads
         if (va) {
@@ -261,6 +303,7 @@ k_density_cells(const __grid_constant__ DevParams P0, const SceneTab T, const ui
             const float4 e = veval[ia];
             pairdata[2 * (size_t)ia] = make_float4(pa.x, pa.y, pa.z, sa);
             pairdata[2 * (size_t)ia + 1] = make_float4(e.x, e.y, e.z, 0.0f);
+            if (LIST) hitcnt[ia] = na;
         }
         if (vb) {
             sb = sb * P.pmass * P.poly6kern;
@@ -269,6 +312,7 @@ k_density_cells(const __grid_constant__ DevParams P0, const SceneTab T, const ui
             const float4 e = veval[ib];
             pairdata[2 * (size_t)ib] = make_float4(pb.x, pb.y, pb.z, sb);
             pairdata[2 * (size_t)ib + 1] = make_float4(e.x, e.y, e.z, 0.0f);
+            if (LIST) hitcnt[ib] = nb;
         }
     }
 }
@@ -437,8 +481,8 @@ static int resident_blocks(const void *kern) {
 // Grids of the two passes: every block resident at once (queried once, at
 // system creation, outside any stream capture).
 int fl_cells_init(fl_system *s) {
-    const int d = s->batched ? resident_blocks((const void *)k_density_cells<true>)
-                             : resident_blocks((const void *)k_density_cells<false>);
+    const int d = s->batched ? resident_blocks((const void *)k_density_cells<true, false>)
+                             : resident_blocks((const void *)k_density_cells<false, false>);
     const int f = s->batched ? resident_blocks((const void *)k_force_cells<true>)
                              : resident_blocks((const void *)k_force_cells<false>);
     s->cells_grid[0] = d * s->num_sms;
@@ -453,14 +497,15 @@ int fl_launch_make_tasks(fl_system *s) {
     return FL_OK;
 }
 
-int fl_launch_density_cells(fl_system *s) {
+int fl_launch_density_cells(fl_system *s, bool lists) {
     if (s->n == 0) return FL_OK;
-    auto kern = s->batched ? k_density_cells<true> : k_density_cells<false>;
+    auto kern = lists ? (s->batched ? k_density_cells<true, true> : k_density_cells<false, true>)
+                      : (s->batched ? k_density_cells<true, false> : k_density_cells<false, false>);
     const int grid = s->cells_grid[0];
     kern<<<grid, kCellThreads, 0, s->stream>>>(s->D, fl_scene_tab(s), s->tasks, (uint32_t)s->task_cap,
                                                 s->task_counters, s->f[F_POS].cur<float4>(), s->off, s->cnt, s->upbits,
                                                 s->f[F_VEVAL].cur<float4>(), s->f[F_PRESS].cur<float>(),
-                                                s->pairdata);
+                                                s->pairdata, s->hitlist, s->hitcnt);
     FL_LAUNCH_CHECK("density_cells");
     return FL_OK;
 }

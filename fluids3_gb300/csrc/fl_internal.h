@@ -296,7 +296,9 @@ int fl_launch_sample_volume(fl_system *s, const int res[3], const float bmin[3],
 size_t fl_task_cap(int max_points, int gcells);
 int fl_cells_init(fl_system *s);   // after num_sms and batched are set
 int fl_launch_make_tasks(fl_system *s);
-int fl_launch_density_cells(fl_system *s);
+// lists: also write per-point pair lists and counts (the per-point passes'
+// layout, read by the adjoint's reverse kernels)
+int fl_launch_density_cells(fl_system *s, bool lists = false);
 // force + advance over the tasks; host_pos (device-usable pointer to
 // page-locked host memory, or null) also receives the new positions as float x3
 int fl_launch_force_cells(fl_system *s, float dt, float *host_pos);
