@@ -102,7 +102,7 @@ def parse():
     ap.add_argument("--profile", action="store_true",
                     help="profiling run for ncu: the wave tank of --n points, --warmup eager steps, then "
                          "--steps eager steps (one launch per kernel per step), no timing, no JSON line")
-    ap.add_argument("--passes", choices=["cells", "points"], default="cells",
+    ap.add_argument("--passes", choices=["cells", "points"], default="points",
                     help="neighbour passes of the fused step (bit-identical results)")
     ap.add_argument("--fit-iters", type=int, default=40,
                     help="iterations of the 64-scene batched parameter fit (0 skips it)")
@@ -677,7 +677,7 @@ def config_of(scene, args):
             "n_points": scene.n, "cells": p.gridTotal, "grid": list(p.gridRes),
             "l2": "inputs larger than L2 (state ~1 GB in HBM), no flush needed",
             "segment_steps": args.segment,
-            "neighbour_passes": getattr(args, "passes", "cells"),
+            "neighbour_passes": getattr(args, "passes", "points"),
             "step": "insert, scan, index scatter, canonical sort+gather, density, force+advance"}
 
 

@@ -190,7 +190,7 @@ extern "C" int fl_create(const fl_params *p, int max_points, fl_system **out) {
     FL_TRY(check_derived(p));
     fl_system *s = (fl_system *)calloc(1, sizeof(fl_system));
     if (!s) return fl_fail(FL_ERR_NOMEM, "fl_create: host allocation failed");
-    s->cell_passes = 1;
+    s->cell_passes = 0;   // the per-point passes: the faster step (fl_set_neighbour_passes)
     int r = FL_OK;
     do {
         if (cudaGetDevice(&s->device) != cudaSuccess) {
@@ -852,8 +852,8 @@ static int record(fl_system *s, TimingState *t, int k) {
 }
 
 // The cell-task passes (fl_cells.cu) need the pruned search (gridSrch 2 in
-// every scene) with band codes from this step's sort; a recording tape keeps
-// the per-point passes, whose pair lists its reverse steps read.
+// every scene) with band codes from this step's sort. A recording tape keeps
+// the per-point passes (its hooks keep each step's pair lists).
 static bool use_cell_passes(const fl_system *s, bool taped) {
     return s->cell_passes && s->D.prune && s->codes_valid && !taped && s->n > 0;
 }
@@ -905,10 +905,9 @@ int fl_rebuild_grid(fl_system *s) {
 
 int fl_recompute_step(fl_system *s) {
     FL_TRY(fl_rebuild_grid(s));
-    if (use_cell_passes(s, false)) {   // the cell-task density, writing per-point pair lists
+    if (use_cell_passes(s, false)) {   // the cell-task density, writing the same pair lists
         FL_TRY(fl_launch_make_tasks(s));
         FL_TRY(fl_launch_density_cells(s, true));
-        s->lists_valid = 1;
         return FL_OK;
     }
     FL_TRY(fl_launch_density(s));

@@ -1,4 +1,6 @@
-// Cell-task neighbour passes of the fused step (gridSrch 2, band codes set).
+// Cell-task neighbour passes of the fused step (FL_PASSES_CELL_TASKS;
+// gridSrch 2, band codes set), and the cell-task density of the adjoint's
+// rebuilt steps.
 //
 // computePressure and computeForce (fluids4.0/fluid_kernels.cu:112-149,
 // 180-217) walk, for every point, the 2x2x2 search block c-1..c of its cell
@@ -18,19 +20,16 @@
 //    tested by all lanes at once (a broadcast read), 32 at a time;
 //  * a pair that some other point of the task needed but this point's own
 //    pruning would have skipped has |d| >= band > h, so it fails the test
-//    0 < d^2 < rd2: each point's sum still sees exactly the reference's
+//    0 < d^2 < rd2: each point's sums still see exactly the reference's
 //    terms in the reference's order, and densities and forces stay
 //    bit-identical to the per-point walk.
 //
-// The density pass evaluates two points per lane with packed f32x2
+// The density pass evaluates two points per lane in packed f32x2
 // arithmetic (sub/mul.rn.f32x2: IEEE round-to-nearest per element, the same
 // results as scalar operations) when a task has more than 32 points; no
-// packed add ever takes two packed products (see density_group2).
-// The force pass stages each candidate's 32-byte pair record (position and
-// density, evaluated velocity; written by the density pass), tests the 32
-// candidates of a group for every lane, and then each lane adds its own
-// hits in order with the reference's pair arithmetic (add_pair_terms),
-// followed by the advance of its points.
+// packed add ever takes two packed products (see density_group2). It
+// records hit masks for the force pass, or pair lists for the adjoint. The
+// force pass is described above k_force_cells.
 //
 // Tasks are listed once per step by k_make_tasks (one entry per 64 slots of
 // a cell, out-of-range bins included, in any order: no result depends on
@@ -48,6 +47,8 @@ namespace {
 constexpr int kTaskPoints = 64;    // slots per task: two per lane
 constexpr int kCellThreads = 128;  // threads per block of both passes (4 warps, one task each at a time)
 constexpr uint32_t kRing = 64;     // staged candidates per warp (at most 63 are pending)
+constexpr uint32_t kMaskWords = 16; // hit-mask words kept per point: unions of up to 512 candidates
+constexpr uint32_t kPairCap = 512; // hit pairs of one group evaluated pair-parallel (else per lane)
 
 // ---- packed f32x2 arithmetic (round-to-nearest per element) ---------------
 __device__ __forceinline__ uint64_t pk2(float a, float b) {
@@ -235,16 +236,20 @@ __device__ __forceinline__ void list_hits(const DevParams &P, const float4 *ring
     }
 }
 
-// LIST: the adjoint's rebuilt steps, whose reverse kernels read per-point
-// pair lists and counts (hitlist, hitcnt): the same lists the per-point
-// density pass writes.
+// Besides the densities and the pair records, LIST = false (the fused step)
+// writes each point's hit masks for the force pass: word w of point i, at
+// masks[w * mstride + i], holds bit u set when union candidate 32 w + u
+// passed the test (the first kMaskWords words). LIST = true (the adjoint's
+// rebuilt steps) writes each point's pair list and count (hitlist,
+// hitcnt) exactly as the per-point density pass does, for the reverse
+// kernels, which drain those lists. Both share the pair-list buffer.
 template <bool BATCH, bool LIST>
 __global__ void __launch_bounds__(kCellThreads)
 k_density_cells(const __grid_constant__ DevParams P0, const SceneTab T, const uint2 *__restrict__ tasks,
                 uint32_t cap, uint32_t *counters, const float4 *__restrict__ pos, const uint32_t *__restrict__ off,
                 const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
                 const float4 *__restrict__ veval, float *__restrict__ press, float4 *__restrict__ pairdata,
-                uint32_t *__restrict__ hitlist, uint32_t *__restrict__ hitcnt) {
+                uint32_t *__restrict__ hitlist, uint32_t *__restrict__ hitcnt, size_t mstride) {
     __shared__ float4 s_ring[kCellThreads / 32][kRing];
     const unsigned lane = lane_id();
     float4 *ring = s_ring[threadIdx.x >> 5];
@@ -286,13 +291,21 @@ k_density_cells(const __grid_constant__ DevParams P0, const SceneTab T, const ui
                 if (LIST) {
                     if (va) list_hits(P, ring, g, ma, ia, na, hitlist);
                     if (vb) list_hits(P, ring, g, mb, ib, nb, hitlist);
+                } else if ((g >> 5) < kMaskWords) {
+                    uint32_t *row = hitlist + (size_t)(g >> 5) * mstride;
+                    if (va) row[ia] = ma;
+                    if (vb) row[ib] = mb;
                 }
             });
             up2(sab, sa, sb);
         } else {
             walk_union(P, c, need, off, cnt, upbits, stage, [&](uint32_t g, uint32_t count) {
                 const uint32_t ma = density_group1(P, ring, g, count, pa, sa);
-                if (LIST && va) list_hits(P, ring, g, ma, ia, na, hitlist);
+                if (LIST) {
+                    if (va) list_hits(P, ring, g, ma, ia, na, hitlist);
+                } else if ((g >> 5) < kMaskWords && va) {
+                    hitlist[(size_t)(g >> 5) * mstride + ia] = ma;
+                }
             });
         }
         // fluid_kernels.cu:146-148, and the pair records the force pass reads
@@ -317,10 +330,33 @@ k_density_cells(const __grid_constant__ DevParams P0, const SceneTab T, const ui
     }
 }
 
+
 // ---- force + advance ----------------------------------------------------------
-// The hits of one lane's point among the group's candidates: bit u set when
-// candidate g + u passes 0 < d^2 < rd2 (the density pass's test, same
-// positions, same rounding).
+// The force pass walks the same union as the density pass (same codes,
+// flags and counts, so the same sequence), staging each candidate's 32-byte
+// pair record (position and density; evaluated velocity). For each group of
+// 32 candidates the hits of the task's points come from the density pass's
+// masks (past kMaskWords words the test is repeated). The hits of a group
+// are then evaluated pair-parallel: they are listed point by point, in
+// candidate order, in shared memory; 32 lanes compute 32 pair terms at a
+// time (pair_term, the reference's arithmetic); and each lane adds its own
+// points' terms in list order -- the reference's pair order -- so every
+// force is the same sum, bit for bit. Groups with more than kPairCap hits
+// (crowded cells) are drained per lane instead, each lane adding its hits
+// as it finds them.
+struct ForceOut {
+    float4 *vel, *force, *pos_out, *veval_out;
+    float *host_pos;      // optional page-locked host copy of the new positions (float x3)
+    uint32_t *err;
+};
+
+struct ForceShared {
+    float4 ring[kRing][2];        // staged pair records
+    float4 pts[kTaskPoints][2];   // the task's points: (p.xyz, pressure term), (veval.xyz, density)
+    float4 terms[32];             // one batch of pair terms
+    uint16_t pairs[kPairCap];     // the group's hits: point << 5 | candidate
+};
+
 __device__ __forceinline__ uint32_t hit_bits(const DevParams &P, const float4 (*ring)[2], uint32_t g, uint32_t count,
                                              float4 p) {
     uint32_t h = 0;
@@ -334,46 +370,33 @@ __device__ __forceinline__ uint32_t hit_bits(const DevParams &P, const float4 (*
     return h;
 }
 
-__device__ __forceinline__ void add_hits(const DevParams &P, const float4 (*ring)[2], uint32_t g, uint32_t h,
-                                         ForcePoint &fp) {
+// One point's hits of a group, added in candidate order (the per-lane drain).
+__device__ __forceinline__ void drain_hits(const DevParams &P, const ForceShared &sh, uint32_t g, uint32_t h,
+                                           const float4 pt[2], float3 &f) {
     while (h) {
         const uint32_t u = (uint32_t)(__ffs(h) - 1);
         h &= h - 1u;
-        const float4 *rec = ring[(g + u) & (kRing - 1u)];
-        const float4 q = rec[0];
-        add_pair_terms(P, fp, q, rec[1], q.w);
+        const float4 *rec = sh.ring[(g + u) & (kRing - 1u)];
+        const float3 t = pair_term(P, pt[0], pt[0].w, pt[1], pt[1].w, rec[0], rec[1], rec[0].w);
+        f.x += t.x; f.y += t.y; f.z += t.z;
     }
 }
 
-__device__ __forceinline__ void load_point(const DevParams &P, ForcePoint &fp, bool valid, uint32_t i,
-                                           const float4 *__restrict__ pos, const float4 *__restrict__ veval,
-                                           const float *__restrict__ press) {
-    fp.f = make_float3(0.0f, 0.0f, 0.0f);
-    if (valid) {
-        fp.p = pos[i];
-        fp.vi = veval[i];
-        fp.di = press[i];
-    } else {
-        fp.p = make_float4(0.f, 0.f, 0.f, 0.f);
-        fp.vi = fp.p;
-        fp.di = 1.0f;
+// Adds the terms of list entries [lo, hi) that fall in the batch [bs, bs + 32).
+__device__ __forceinline__ void take_terms(const ForceShared &sh, uint32_t lo, uint32_t hi, uint32_t bs, float3 &f) {
+    const uint32_t a = max(lo, bs), b = min(hi, bs + 32u);
+    for (uint32_t e = a; e < b; e++) {
+        const float4 t = sh.terms[e - bs];
+        f.x += t.x; f.y += t.y; f.z += t.z;
     }
-    fp.pi = (fp.di - P.prest_dens) * P.pintstiff;
 }
 
-struct ForceOut {
-    float4 *vel, *force, *pos_out, *veval_out;
-    float *host_pos;      // optional page-locked host copy of the new positions (float x3)
-    uint32_t *err;
-};
-
-// The advance of one in-range point from its force (fluid_kernels.cu:332-420);
-// returns the new position.
-__device__ __forceinline__ float3 finish_point(const DevParams &P, float time, float dt, uint32_t i,
-                                               const ForcePoint &fp, const ForceOut &o) {
-    o.force[i] = f4(fp.f);
+// The advance of one in-range point from its force (fluid_kernels.cu:332-420).
+__device__ __forceinline__ float3 finish_point(const DevParams &P, float time, float dt, uint32_t i, float4 p,
+                                               float4 vi, float3 f, const ForceOut &o) {
+    o.force[i] = f4(f);
     float3 po, vo, eo;
-    advance_point(P, time, dt, P.sim_scale, fp.f, xyz(fp.p), xyz(o.vel[i]), xyz(fp.vi), po, vo, eo);
+    advance_point(P, time, dt, P.sim_scale, f, xyz(p), xyz(o.vel[i]), xyz(vi), po, vo, eo);
     if (!(isfinite(po.x) && isfinite(po.y) && isfinite(po.z))) atomicOr(o.err, FL_DEV_NONFINITE);
     o.pos_out[i] = f4(po);
     o.vel[i] = f4(vo);
@@ -392,7 +415,7 @@ __device__ __forceinline__ float3 park_point(uint32_t i, const float4 *__restric
 }
 
 // The new positions of `count` (<= 32) consecutive slots from s, packed
-// float x3 into page-locked host memory: staged in shared memory so that
+// float x3 into page-locked host memory, staged in shared memory so that
 // each store instruction of the warp writes 128 contiguous bytes.
 __device__ __forceinline__ void host_store(float *host, uint32_t s, uint32_t count, float3 v, float *stage) {
     const unsigned lane = lane_id();
@@ -410,10 +433,10 @@ k_force_cells(const __grid_constant__ DevParams P0, const SceneTab T, const uint
               const float4 *__restrict__ veval_in, const float *__restrict__ press,
               const uint32_t *__restrict__ off, const uint32_t *__restrict__ cnt,
               const uint32_t *__restrict__ upbits, const float4 *__restrict__ pairdata,
-              const __grid_constant__ ForceOut o) {
-    __shared__ float4 s_ring[kCellThreads / 32][kRing][2];
+              const uint32_t *__restrict__ masks, size_t mstride, const __grid_constant__ ForceOut o) {
+    __shared__ ForceShared s_sh[kCellThreads / 32];
     const unsigned lane = lane_id();
-    float4 (*ring)[2] = s_ring[threadIdx.x >> 5];
+    ForceShared &sh = s_sh[threadIdx.x >> 5];
     const float time = time_dev[slot];
     if (blockIdx.x == 0 && threadIdx.x == 0) time_dev[slot ^ 1] = time + dt;
     const uint32_t ntasks = min(counters[0], cap);   // k_make_tasks flags an overflow
@@ -433,28 +456,89 @@ k_force_cells(const __grid_constant__ DevParams P0, const SceneTab T, const uint
             if (va) na = park_point(ia, veval_in, o);
             if (vb) nb = park_point(ib, veval_in, o);
         } else {
-            ForcePoint fa, fb;
-            load_point(P, fa, va, ia, pos_in, veval_in, press);
-            load_point(P, fb, vb, ib, pos_in, veval_in, press);
-            const uint32_t need = needed_entries(va, __float_as_uint(fa.p.w), vb, __float_as_uint(fb.p.w));
+            // the task's points: (position, pressure term), (veval, density)
+            float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = make_float4(0.f, 0.f, 0.f, 1.f), b0 = a0, b1 = a1;
+            uint32_t code_a = 0, code_b = 0;
+            if (va) {
+                const float4 p = pos_in[ia], e = veval_in[ia];
+                const float d = press[ia];
+                code_a = __float_as_uint(p.w);
+                a0 = make_float4(p.x, p.y, p.z, (d - P.prest_dens) * P.pintstiff);
+                a1 = make_float4(e.x, e.y, e.z, d);
+            }
+            if (vb) {
+                const float4 p = pos_in[ib], e = veval_in[ib];
+                const float d = press[ib];
+                code_b = __float_as_uint(p.w);
+                b0 = make_float4(p.x, p.y, p.z, (d - P.prest_dens) * P.pintstiff);
+                b1 = make_float4(e.x, e.y, e.z, d);
+            }
+            __syncwarp();
+            sh.pts[lane][0] = a0; sh.pts[lane][1] = a1;
+            sh.pts[32 + lane][0] = b0; sh.pts[32 + lane][1] = b1;
+            const float4 pa[2] = {a0, a1}, pb[2] = {b0, b1};
+            const uint32_t need = needed_entries(va, code_a, vb, code_b);
             const bool dual = mt > 32u;
+            float3 fa = make_float3(0.f, 0.f, 0.f), fb = fa;
             auto stage = [&](uint32_t r, uint32_t j) {
-                ring[r][0] = pairdata[2 * (size_t)j];
-                ring[r][1] = pairdata[2 * (size_t)j + 1];
+                sh.ring[r][0] = pairdata[2 * (size_t)j];
+                sh.ring[r][1] = pairdata[2 * (size_t)j + 1];
             };
             walk_union(P, c, need, off, cnt, upbits, stage, [&](uint32_t g, uint32_t count) {
-                const uint32_t ha = va ? hit_bits(P, ring, g, count, fa.p) : 0u;
-                const uint32_t hb = (dual && vb) ? hit_bits(P, ring, g, count, fb.p) : 0u;
-                add_hits(P, ring, g, ha, fa);
-                add_hits(P, ring, g, hb, fb);
+                uint32_t ha = 0, hb = 0;
+                if ((g >> 5) < kMaskWords) {   // the density pass's record of this group
+                    const uint32_t *row = masks + (size_t)(g >> 5) * mstride;
+                    if (va) ha = row[ia];
+                    if (dual && vb) hb = row[ib];
+                } else {                       // beyond it: the same test again
+                    if (va) ha = hit_bits(P, sh.ring, g, count, a0);
+                    if (dual && vb) hb = hit_bits(P, sh.ring, g, count, b0);
+                }
+                // list offsets: point a of lane l, then point b of lane l
+                const uint32_t ca = __popc(ha), cb = __popc(hb);
+                uint32_t xa = ca, xb = cb;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const uint32_t ya = __shfl_up_sync(0xffffffffu, xa, d);
+                    const uint32_t yb = __shfl_up_sync(0xffffffffu, xb, d);
+                    if (lane >= (unsigned)d) { xa += ya; xb += yb; }
+                }
+                const uint32_t total_a = __shfl_sync(0xffffffffu, xa, 31);
+                const uint32_t total = total_a + __shfl_sync(0xffffffffu, xb, 31);
+                if (total == 0) return;
+                if (total > kPairCap) {   // crowded: each lane drains its own hits
+                    drain_hits(P, sh, g, ha, pa, fa);
+                    drain_hits(P, sh, g, hb, pb, fb);
+                    return;
+                }
+                const uint32_t lo_a = xa - ca, lo_b = total_a + xb - cb;
+                for (uint32_t h = ha, e = lo_a; h; h &= h - 1u, e++)
+                    sh.pairs[e] = (uint16_t)((lane << 5) | (uint32_t)(__ffs(h) - 1));
+                for (uint32_t h = hb, e = lo_b; h; h &= h - 1u, e++)
+                    sh.pairs[e] = (uint16_t)(((32u + lane) << 5) | (uint32_t)(__ffs(h) - 1));
+                __syncwarp();
+                for (uint32_t bs = 0; bs < total; bs += 32u) {
+                    const uint32_t e = bs + lane;
+                    if (e < total) {
+                        const uint32_t pr = sh.pairs[e];
+                        const float4 *pt = sh.pts[pr >> 5];
+                        const float4 *rec = sh.ring[(g + (pr & 31u)) & (kRing - 1u)];
+                        const float3 tm = pair_term(P, pt[0], pt[0].w, pt[1], pt[1].w, rec[0], rec[1], rec[0].w);
+                        sh.terms[lane] = make_float4(tm.x, tm.y, tm.z, 0.f);
+                    }
+                    __syncwarp();
+                    take_terms(sh, lo_a, lo_a + ca, bs, fa);
+                    take_terms(sh, lo_b, lo_b + cb, bs, fb);
+                    __syncwarp();
+                }
             });
-            if (va) na = finish_point(P, time, dt, ia, fa, o);
-            if (vb) nb = finish_point(P, time, dt, ib, fb, o);
+            if (va) na = finish_point(P, time, dt, ia, a0, a1, fa, o);
+            if (vb) nb = finish_point(P, time, dt, ib, b0, b1, fb, o);
         }
         if (o.host_pos) {
-            float *st = reinterpret_cast<float *>(ring);   // the ring is free once the walk is done
+            float *st = reinterpret_cast<float *>(sh.ring);   // free once the walk is done
             host_store(o.host_pos, task.x, min(mt, 32u), na, st);
-            if (mt > 32u) host_store(o.host_pos, ib - lane, mt - 32u, nb, st);
+            if (mt > 32u) host_store(o.host_pos, task.x + 32u, mt - 32u, nb, st);
         }
     }
 }
@@ -478,8 +562,8 @@ static int resident_blocks(const void *kern) {
     return per_sm;
 }
 
-// Grids of the two passes: every block resident at once (queried once, at
-// system creation, outside any stream capture).
+// Grid of the pass: every block resident at once (queried once, at system
+// creation, outside any stream capture).
 int fl_cells_init(fl_system *s) {
     const int d = s->batched ? resident_blocks((const void *)k_density_cells<true, false>)
                              : resident_blocks((const void *)k_density_cells<false, false>);
@@ -489,6 +573,13 @@ int fl_cells_init(fl_system *s) {
     s->cells_grid[1] = f * s->num_sms;
     return FL_OK;
 }
+
+// The hit masks share the per-point pass's pair-list buffer (128 words per
+// point; the masks take at most kMaskWords): row w holds word w of every slot.
+static size_t mask_stride(const fl_system *s) {
+    return ((size_t)(s->max_points > 0 ? s->max_points : 1) + 31) & ~(size_t)31;
+}
+static_assert(kMaskWords <= 128, "the hit masks must fit in the pair-list buffer");
 
 int fl_launch_make_tasks(fl_system *s) {
     k_make_tasks<<<blocks_for((long long)s->gcells, 256), 256, 0, s->stream>>>(
@@ -505,14 +596,14 @@ int fl_launch_density_cells(fl_system *s, bool lists) {
     kern<<<grid, kCellThreads, 0, s->stream>>>(s->D, fl_scene_tab(s), s->tasks, (uint32_t)s->task_cap,
                                                 s->task_counters, s->f[F_POS].cur<float4>(), s->off, s->cnt, s->upbits,
                                                 s->f[F_VEVAL].cur<float4>(), s->f[F_PRESS].cur<float>(),
-                                                s->pairdata, s->hitlist, s->hitcnt);
+                                                s->pairdata, s->hitlist, s->hitcnt, mask_stride(s));
     FL_LAUNCH_CHECK("density_cells");
+    s->lists_valid = lists ? 1 : 0;   // without lists the buffer holds the force pass's hit masks
     return FL_OK;
 }
 
 int fl_launch_force_cells(fl_system *s, float dt, float *host_pos) {
     auto kern = s->batched ? k_force_cells<true> : k_force_cells<false>;
-    const int grid = s->cells_grid[1];
     ForceOut o;
     o.vel = s->f[F_VEL].cur<float4>();
     o.force = s->f[F_FORCE].cur<float4>();
@@ -520,11 +611,10 @@ int fl_launch_force_cells(fl_system *s, float dt, float *host_pos) {
     o.veval_out = s->f[F_VEVAL].nxt<float4>();
     o.host_pos = host_pos;
     o.err = s->dev_err;
-    kern<<<grid, kCellThreads, 0, s->stream>>>(s->D, fl_scene_tab(s), s->tasks, (uint32_t)s->task_cap,
-                                                s->task_counters, s->time_dev,
-                                                s->time_slot, dt, s->f[F_POS].cur<float4>(),
-                                                s->f[F_VEVAL].cur<float4>(), s->f[F_PRESS].cur<float>(), s->off,
-                                                s->cnt, s->upbits, s->pairdata, o);
+    kern<<<s->cells_grid[1], kCellThreads, 0, s->stream>>>(
+        s->D, fl_scene_tab(s), s->tasks, (uint32_t)s->task_cap, s->task_counters, s->time_dev, s->time_slot, dt,
+        s->f[F_POS].cur<float4>(), s->f[F_VEVAL].cur<float4>(), s->f[F_PRESS].cur<float>(), s->off, s->cnt,
+        s->upbits, s->pairdata, s->hitlist, mask_stride(s), o);
     FL_LAUNCH_CHECK("force_cells");
     return FL_OK;
 }

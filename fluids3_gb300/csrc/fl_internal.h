@@ -127,14 +127,14 @@ struct fl_system {
     uint32_t *big_count;   // [0] their number, [1] k_sort_big's sign-off count (256 B slot, zeroed at creation)
     int num_sms;
 
-    // cell tasks of the fused step (fl_cells.cu): (first slot, cell entry)
+    // cell tasks of the fused step's neighbour passes (fl_cells.cu): (first slot, cell entry)
     // per 64 slots of a cell, listed every step; counters in the scan
     // ticket's slot (cleared with the counts)
     uint2 *tasks;
     size_t task_cap;
     uint32_t *task_counters;
     int cell_passes;       // 1: the fused step uses the cell-task passes where it can
-    int cells_grid[2];     // blocks of the density and force cell passes (all resident)
+    int cells_grid[2];     // blocks of the cell-task density and force passes (all resident)
 
     uint32_t *hitlist;     // ceil(N/32) * hcap * 32 entries
     uint32_t *hitcnt;      // per point
@@ -296,11 +296,12 @@ int fl_launch_sample_volume(fl_system *s, const int res[3], const float bmin[3],
 size_t fl_task_cap(int max_points, int gcells);
 int fl_cells_init(fl_system *s);   // after num_sms and batched are set
 int fl_launch_make_tasks(fl_system *s);
-// lists: also write per-point pair lists and counts (the per-point passes'
-// layout, read by the adjoint's reverse kernels)
+// densities and pair records, plus the force pass's hit masks or (lists) the
+// per-point pair lists and counts in the per-point pass's layout
 int fl_launch_density_cells(fl_system *s, bool lists = false);
-// force + advance over the tasks; host_pos (device-usable pointer to
-// page-locked host memory, or null) also receives the new positions as float x3
+// force + advance over the tasks from the hit masks; host_pos (a
+// device-usable pointer to page-locked host memory, or null) also receives
+// the new positions as float x3
 int fl_launch_force_cells(fl_system *s, float dt, float *host_pos);
 size_t fl_scan_tile();
 size_t fl_upbits_bytes(const fl_system *s);

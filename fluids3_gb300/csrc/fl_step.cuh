@@ -11,24 +11,33 @@ struct ForcePoint {
     float3 f;
 };
 
-// One pair's term from the neighbour's position q, evaluated velocity vj and
-// density dj, added in the reference's operation order
-// (fluid_kernels.cu:203-210); the pair is known to pass 0 < d^2 < rd2.
-__device__ __forceinline__ void add_pair_terms(const DevParams &P, ForcePoint &fp, float4 q, float4 vj,
-                                               float dj) {
-    const float dx = fp.p.x - q.x, dy = fp.p.y - q.y, dz = fp.p.z - q.z;
+// One pair's force term on a point at p (pressure term pi, evaluated
+// velocity vi, density di) from the neighbour's position q, evaluated
+// velocity vj and density dj, in the reference's operation order
+// (fluid_kernels.cu:203-210); the pair is known to pass 0 < d^2 < rd2. The
+// point's force is the sum of its terms, added component-wise in the
+// reference's pair order.
+__device__ __forceinline__ float3 pair_term(const DevParams &P, float4 p, float pi, float4 vi, float di, float4 q,
+                                            float4 vj, float dj) {
+    const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
     const float dsq = dx * dx + dy * dy + dz * dz;
     const float r = sqrtf(dsq * P.d2);
     const float pj = (dj - P.prest_dens) * P.pintstiff;
     const float cr = P.psmoothradius - r;
-    const float pterm = P.sim_scale * -0.5f * cr * P.spikykern * (fp.pi + pj) / r;
-    const float sx = dx * pterm + (vj.x - fp.vi.x) * P.vterm;
-    const float sy = dy * pterm + (vj.y - fp.vi.y) * P.vterm;
-    const float sz = dz * pterm + (vj.z - fp.vi.z) * P.vterm;
-    const float inv = 1.0f / (fp.di * dj);
-    fp.f.x += (sx * cr) * inv;
-    fp.f.y += (sy * cr) * inv;
-    fp.f.z += (sz * cr) * inv;
+    const float pterm = P.sim_scale * -0.5f * cr * P.spikykern * (pi + pj) / r;
+    const float sx = dx * pterm + (vj.x - vi.x) * P.vterm;
+    const float sy = dy * pterm + (vj.y - vi.y) * P.vterm;
+    const float sz = dz * pterm + (vj.z - vi.z) * P.vterm;
+    const float inv = 1.0f / (di * dj);
+    return make_float3((sx * cr) * inv, (sy * cr) * inv, (sz * cr) * inv);
+}
+
+__device__ __forceinline__ void add_pair_terms(const DevParams &P, ForcePoint &fp, float4 q, float4 vj,
+                                               float dj) {
+    const float3 t = pair_term(P, fp.p, fp.pi, fp.vi, fp.di, q, vj, dj);
+    fp.f.x += t.x;
+    fp.f.y += t.y;
+    fp.f.z += t.z;
 }
 
 // advanceParticles body (fluids4.0/fluid_kernels.cu:343-419) for an

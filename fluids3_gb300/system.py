@@ -394,9 +394,10 @@ class FluidSystem:
         call("fl_set_launch_shapes", self._h, shapes)
 
     def SetNeighbourPasses(self, mode: str) -> None:
-        """"cells" (default): one warp per 64 points of a cell walks their shared
-        search block in lockstep; "points": one thread per point (the
-        reference's loop structure). Results are bit-identical."""
+        """Neighbour passes of the fused step: "points" (default, the faster
+        step), one thread per point (the reference's loop structure);
+        "cells", one warp per 64 points of a cell walks their shared search
+        block in lockstep. Results are bit-identical."""
         call("fl_set_neighbour_passes", self._h, {"points": 0, "cells": 1}[mode])
 
     def NeighbourPasses(self) -> str:

@@ -334,15 +334,17 @@ int fl_launch_shapes(fl_system *s, int *shapes);
 int fl_set_launch_shapes(fl_system *s, const int *shapes);
 
 /* Which neighbour passes the fused step (fl_run, fl_run_steps,
- * fl_run_from_host) uses; both give bit-identical results.
- * FL_PASSES_CELL_TASKS (the default): one warp per 64 points of a cell walks
- * their shared search block once, in lockstep, staged in shared memory;
- * used where the pruned search applies (gridSrch 2 in every scene) and no
- * tape is recording. FL_PASSES_PER_POINT: one thread per point walks its
- * own search block (fluids4.0/fluid_kernels.cu:112-149, 180-217 as
- * written), recording pair lists for the force pass; always used by the
- * phase entry points, recording tapes and gridSrch > 2. No counterpart in
- * the reference (which has only the per-point walk). */
+ * fl_run_from_host) uses; both give bit-identical densities, forces and
+ * states. FL_PASSES_PER_POINT (the default, the faster step): one thread
+ * per point walks its own search block (fluids4.0/fluid_kernels.cu:112-149
+ * as written) and records its pair list, which the force pass drains.
+ * FL_PASSES_CELL_TASKS: one warp per 64 points of a cell walks their shared
+ * search block once, in lockstep, staged in shared memory, recording hit
+ * masks; the force pass walks the block again and evaluates the hits
+ * pair-parallel. Used where the pruned search applies (gridSrch 2 in every
+ * scene) and no tape is recording; the phase entry points and recording
+ * tapes always use the per-point passes. No counterpart in the reference
+ * (which has only the per-point walk). */
 #define FL_PASSES_PER_POINT  0
 #define FL_PASSES_CELL_TASKS 1
 int fl_set_neighbour_passes(fl_system *s, int mode);

@@ -1,14 +1,16 @@
 """The cell-task neighbour passes (fl_cells.cu) against the per-point passes.
 
-The fused step walks each cell's shared search block once per 64 of its
-points, in lockstep, instead of once per point. Every point's sum must keep
-the reference's terms and order, so both passes give bit-identical states:
-checked over many steps on the wave tank, on crowded cells (tasks of one
-cell split over many warps, unions of thousands of candidates), on cells of
+With FL_PASSES_CELL_TASKS the fused step walks each cell's shared search
+block once per 64 of its points, in lockstep, and evaluates the hits
+pair-parallel; the adjoint's rebuilt steps take their pair lists from the
+cell-task density. Every point's sums keep the reference's terms and order,
+so both give bit-identical states: checked over many steps on the wave
+tank, on crowded cells (tasks of one cell split over many warps, unions of
+thousands of candidates, groups past the pair-parallel cap), on cells of
 1..64 points (one and two points per lane), on batches, through graph
-replay and through fl_run_from_host (whose force pass also writes the new
-positions into the caller's page-locked array), and against the oracle
-step by step.
+replay and fl_run_from_host (whose cell-task force pass writes the new
+positions into the caller's page-locked array), against the oracle step by
+step, and through the adjoint.
 """
 from __future__ import annotations
 
@@ -81,7 +83,8 @@ def test_cells_match_the_oracle_step_by_step():
     p = sc.params
     with F.FluidSystem(p, sc.n) as s:
         s.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
-        assert s.NeighbourPasses() == "cells"
+        assert s.NeighbourPasses() == "points"   # the default
+        s.SetNeighbourPasses("cells")
         s.RunSteps(40)
         s.Sync()
         for _ in range(3):
@@ -119,9 +122,9 @@ def test_cells_with_escaped_points_and_nan():
 
 
 def test_run_from_host_with_cells_writes_positions_back():
-    """fl_run_from_host's force pass writes the new positions into the
-    caller's page-locked array as it goes: equal to the device state and to
-    the per-point path's step."""
+    """fl_run_from_host with the cell-task passes: the force pass writes the
+    new positions into the caller's page-locked array as it goes; they
+    equal the device state and the per-point path's step."""
     import ctypes as C
     sc = scenes.wave_tank(n=150_000)
     n = sc.n
@@ -135,7 +138,7 @@ def test_run_from_host_with_cells_writes_positions_back():
     vp = lambda a: a.ctypes.data_as(C.c_void_p)
     try:
         with F.FluidSystem(sc.params, n) as s:
-            assert s.NeighbourPasses() == "cells"
+            s.SetNeighbourPasses("cells")
             pins["out"].array[:] = np.nan
             F._lib.check("fl_run_from_host", lib.fl_run_from_host(
                 s.handle, n, vp(pins["pos"].array), vp(pins["vel"].array), vp(pins["veval"].array),
@@ -159,8 +162,8 @@ def test_run_from_host_with_cells_writes_positions_back():
 @pytest.mark.parametrize("every", [1, 3])
 def test_adjoint_identical_with_either_passes(every):
     """The adjoint's rebuilt steps take their pair lists from the cell-task
-    density (list-writing variant) and its segment replays run the cell-task
-    step: gradients must equal those of the per-point passes bit for bit."""
+    density and its segment replays run the cell-task step: gradients must
+    equal those of the per-point pass bit for bit."""
     sc = scenes.dam_break(n=6000, seed=41)
     w = np.random.default_rng(42).standard_normal((3, sc.n, 3)).astype(np.float32)
     got = {}

@@ -687,11 +687,10 @@ def test_run_from_host_equals_set_particles_then_run(case):
 
 @pytest.mark.parametrize("passes", ["points", "cells"])
 def test_run_from_host_reads_back_in_slot_ranges(passes):
-    """Above 2^21 points the per-point force pass of fl_run_from_host runs
-    in slot ranges whose positions go back while the next range computes
-    (the cell-task force pass writes them to host memory as it goes): the
-    positions read back and the state still equal SetParticles + Run +
-    GetBuffer."""
+    """Above 2^21 points the force pass of fl_run_from_host runs in slot
+    ranges whose positions go back while the next range computes (after
+    either density pass): the positions read back and the state still equal
+    SetParticles + Run + GetBuffer."""
     sc = scenes.wave_tank(n=2_200_000)
     n = sc.n
     pins = {k: F.PinnedArray((n, 3), np.float32) for k in ("pos", "vel", "veval", "out")}
