@@ -501,22 +501,36 @@ def _device_free():
         return None
 
 
-def _time_backward(s, dpos):
-    """Wall time of one fl_backward with the cotangent and the gradients in
-    device memory (fl_backward returns after its stream is done)."""
+def _time_backward(s, dpos, scaled: bool = False):
+    """Wall time of one fl_backward (or fl_backward_scaled) with the
+    cotangent and the gradients in device memory (the call returns after its
+    stream is done). Returns (ms, parameter gradients, state gradients,
+    per-scene binary exponents of the state gradients (zeros unscaled))."""
     import torch
     from fluids3_gb300 import _lib
     d = torch.from_numpy(np.ascontiguousarray(dpos, np.float32)).cuda()
     outs = [torch.empty_like(d) for _ in range(3)]
     gp = np.zeros((s.NumScenes(), 3), np.float64)
+    ex = np.zeros(s.NumScenes(), np.int32)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    _lib.check("fl_backward", _lib.lib().fl_backward(s.handle, d.data_ptr(), None, None, outs[0].data_ptr(),
-                                                   outs[1].data_ptr(), outs[2].data_ptr(),
-                                                   gp.ctypes.data_as(ctypes.c_void_p)))
+    if scaled:
+        _lib.check("fl_backward_scaled", _lib.lib().fl_backward_scaled(
+            s.handle, d.data_ptr(), None, None, outs[0].data_ptr(), outs[1].data_ptr(), outs[2].data_ptr(),
+            gp.ctypes.data_as(ctypes.c_void_p), ex.ctypes.data_as(ctypes.c_void_p)))
+    else:
+        _lib.check("fl_backward", _lib.lib().fl_backward(s.handle, d.data_ptr(), None, None, outs[0].data_ptr(),
+                                                       outs[1].data_ptr(), outs[2].data_ptr(),
+                                                       gp.ctypes.data_as(ctypes.c_void_p)))
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    return (t1 - t0) * 1e3, gp, outs
+    return (t1 - t0) * 1e3, gp, outs, ex
+
+
+def _rms_scaled(mantissa, exponent: int) -> float:
+    """RMS of mantissa * 2^exponent, formed in float64."""
+    m = mantissa.double()
+    return float(m.pow(2).mean().sqrt()) * 2.0 ** int(exponent)
 
 
 def adjoint_measurements(args):
@@ -563,17 +577,16 @@ def adjoint_measurements(args):
         s.Sync()
         t1 = time.perf_counter()
         loss, dpos, counted = position_loss(s, target)
-        ms_b, gp, outs = _time_backward(s, dpos)
-        gvel = outs[1].cpu().numpy()
+        ms_b, gp, outs, ex = _time_backward(s, dpos, scaled=True)
         s.TapeEnd()
-        gv = float(np.sqrt((gvel.astype(np.float64) ** 2).mean()))
+        gv = _rms_scaled(outs[1], ex[0])
         runs[(every, keep)] = {"every": every, "keep_lists": keep, "tape_bytes": (f0 - f1) if f0 is not None else None,
                        "taped_forward_ms_per_step": (t1 - t0) * 1e3 / T,
                        "backward_ms_per_step": ms_b / T, "ratio": ms_b / T / ms_fwd,
                        "loss": loss, "points_in_loss": counted,
                        "grad_finite": bool(np.isfinite(gp).all() and np.isfinite(gv)),
                        "grad_params": dict(zip(("pvisc", "prest_dens", "pintstiff"), _finite(gp[0].tolist()))),
-                       "grad_vel_rms": _finite(gv)}
+                       "grad_vel_rms": _finite(gv), "grad_state_exponent": int(ex[0])}
     # the exact gradient grows ~1.3-1.5x per step (trajectories diverge):
     # its size against the horizon, each from the same start
     growth = []
@@ -584,10 +597,9 @@ def adjoint_measurements(args):
         s.TapeBegin(h, 1)
         s.RunSteps(h)
         loss, dpos, _ = position_loss(s, target)
-        _, gp, outs = _time_backward(s, dpos)
+        _, gp, outs, ex = _time_backward(s, dpos, scaled=True)
         s.TapeEnd()
-        g = outs[1].double()
-        growth.append({"steps": h, "grad_vel_rms": _finite(float(g.pow(2).mean().sqrt())),
+        growth.append({"steps": h, "grad_vel_rms": _finite(_rms_scaled(outs[1], ex[0])),
                        "grad_pvisc": _finite(float(gp[0, 0]))})
     s.close()
     out["rollout_65k"] = {
@@ -601,8 +613,9 @@ def adjoint_measurements(args):
         "adjoint_forward_ratio": runs[(every_k, False)]["ratio"],
         "adjoint_forward_ratio_kept_lists": runs[(every_k, True)]["ratio"],
         "gradient_vs_horizon": growth,
-        "note": "gradients are exact (FP64-checked over 8 steps); over long horizons they overflow FP32 "
-                "because trajectories diverge exponentially (null = non-finite)"}
+        "note": "exact gradients (FP64-checked over 8 and 300 steps); they grow ~1.4x per step because "
+                "trajectories diverge, so the state gradients come back as FP32 mantissas with a per-scene "
+                "binary exponent (fl_backward_scaled); RMS values here are formed in float64"}
 
     scene = scenes.wave_tank(n=args.n)
     s = F.FluidSystem(scene.params, scene.n)
@@ -622,7 +635,7 @@ def adjoint_measurements(args):
         s.Sync()
         t1 = time.perf_counter()
         _time_backward(s, w)                       # first call: staging buffers
-        ms_b, _, _ = _time_backward(s, w)
+        ms_b, _, _, _ = _time_backward(s, w)
         s.TapeEnd()
         rows.append({"every": every, "keep_lists": keep, "taped_forward_ms_per_step": (t1 - t0) * 1e3 / T4,
                      "backward_ms_per_step": ms_b / T4, "ratio": ms_b / T4 / ms_fwd})
@@ -844,7 +857,7 @@ def our_arm(args, rank, world, local_rank):
                 "fp32_fma_pipe_pct_ncu": rec.get("fp32_fma_pipe_pct"),
                 "issue_roofline_note": "warp instructions / (time x 152 SMs x 4 schedulers x SM clock), "
                                        "from the committed ncu capture: the roof this kernel meets",
-                "profile": "profiles/ncu_wave_tank_4m.md"}
+                "profile": "profiles/ncu_step_wave_tank.md"}
     step_bytes = sum(ALGO_BYTES.values()) * n_in + 12 * (p.gridTotal + 1)
     cpu = None
     if not args.no_cpu_baseline:
