@@ -439,6 +439,7 @@ def batched_comparison(args):
     cat = scenes.concat(scs)
     b = F.FluidSystem.batch([sc.params for sc in scs], [sc.n for sc in scs])
     b.SetParticles(cat["pos"], cat["vel"], cat["veval"], clr=cat["clr"])
+    b.SetNeighbourPasses(args.passes)
     b.RunSteps(warm)
     if not args.no_autotune:
         b.Autotune(3)
@@ -457,6 +458,7 @@ def batched_comparison(args):
     for q, sc in enumerate(scs):
         s = F.FluidSystem(sc.params, sc.n)
         s.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
+        s.SetNeighbourPasses(args.passes)
         s.RunSteps(warm)
         s.SetLaunchShapes(**shapes)
         s.SaveCheckpoint(0)
@@ -480,6 +482,7 @@ def batched_comparison(args):
             "one_at_a_time_value": vs, "speedup": vb / vs, "ms_per_step": ms_b / k,
             "one_at_a_time_ms_per_step": ms_seq / k, "scenes_bit_identical": same,
             "launch_shapes_both": shapes, "largest_cell_at_end": largest_cell,
+            "neighbour_passes": args.passes,
             "protocol": f"{k} continuous graph-replayed steps after {warm} warm-up steps, both arms with the "
                         "batch's autotuned launch shapes; final pos/vel/veval/gcell compared per scene",
             "workload": "scenes log-uniform 2,048..65,536 points, fill U[0.2,0.6] of own box, "
