@@ -7,6 +7,7 @@ import ctypes as C
 import json
 import re
 import subprocess
+import sys
 from pathlib import Path
 
 import numpy as np
@@ -162,3 +163,20 @@ def test_noalloc_scan_rejects_bad_arguments_before_any_gpu_work():
     assert b"two tiles" in lib.fl_last_error()
     assert lib.fl_test_scan_noalloc_timeout(counts, offsets, 8192, status, 0, None) == -1
     assert lib.fl_test_scan_timeout(None, 256) == -1
+
+
+def test_reference_arm_loads_no_product_library():
+    """bench.py --impl reference times the reference's CPU path; its scene
+    parameters come from the oracle's own derivation, so the product library
+    is never loaded in that process (checked in a fresh one)."""
+    code = (
+        "import sys, runpy\n"
+        "sys.argv = ['bench.py', '--impl', 'reference', '--n', '12000', '--steps', '1', '--warmup', '0']\n"
+        "runpy.run_path('bench.py', run_name='__main__')\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print('PRODUCT_LOADED' if 'libfluids_gb300' in maps else 'PRODUCT_NOT_LOADED')\n")
+    out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads([l for l in out.stdout.splitlines() if l.startswith("{")][-1])
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert "PRODUCT_NOT_LOADED" in out.stdout

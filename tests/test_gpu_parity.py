@@ -103,6 +103,30 @@ def test_dam_break_32k_digests(golden_dir):
             assert digest(gpu_state(s)) == rec[key], f"32k dam break diverged from the reference by step {m}"
 
 
+def test_dam_break_32k_all_100_steps_bit_exact_against_the_oracle():
+    """configs[0] over its full 100 steps. Past step 60 a point escapes the
+    grid (step 66) and the reference's own sort leaves stale tail slots, so
+    the reference digests stop there; the oracle restatement places
+    escaped points behind the in-range ones as this library does, so the
+    whole trajectory is compared with it bit for bit."""
+    sc = scenes.dam_break()
+    p = sc.params
+    ref = O.State.new(p, sc.pos, sc.vel, sc.veval, sc.clr)
+    t = 0.0
+    with make_system(p, sc.pos, sc.vel, sc.veval, sc.clr) as s:
+        done = 0
+        for m in (60, 66, 67, 80, 100):
+            s.RunSteps(m - done)
+            t = O.run(p, ref, m - done, t, threads=8)
+            done = m
+            s.Sync()
+            st = gpu_state(s)
+            for k in FIELDS:
+                assert_bit_equal(st[k], getattr(ref, k), f"step {m}: {k}")
+            assert np.float32(s.time) == np.float32(t)
+        assert (st["gcell"] == UNDEF).sum() >= 1   # the escape happened
+
+
 def test_graph_and_eager_agree_with_odd_counts():
     sc = scenes.dam_break(n=5000, seed=9)
     with make_system(sc.params, sc.pos, sc.vel, sc.veval, sc.clr) as a, \
