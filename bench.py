@@ -609,7 +609,7 @@ def adjoint_measurements(args):
         "workload": f"{sc.name}: 65,536-point dam break, box scaled x1.26 (same density as the 32,768-point "
                     f"scene), {T} steps; loss vs the initial block shifted 0.3 box widths in +x",
         "steps": T, "forward_ms_per_step": ms_fwd,
-        "reference_gpu_forward_ms_per_step": reference_gpu_rollout_ms(sc, T),
+        "reference_gpu_forward_ms_per_step": None if args.no_ref_gpu else reference_gpu_rollout_ms(sc, T),
         "system_bytes": (free_before - free_sys) if free_before is not None else None,
         "checkpointed": runs[(every_k, False)], "checkpointed_kept_lists": runs[(every_k, True)],
         "every_step": runs[(1, False)] if (1, False) in runs else runs[(every_k, False)],
