@@ -280,29 +280,49 @@ __device__ __forceinline__ float apply_cotangent(const DevParams &P, AdjAcc &a, 
 }
 
 // One entry of s's pair list (own, reverse, or both).
-__device__ __forceinline__ void adj_pair(const DevParams &P, AdjAcc &a, float3 X, float3 Ev, float rs, float3 fs,
-                                         float irs, uint32_t entry, const float4 *__restrict__ pos,
-                                         const float4 *__restrict__ veval, const float2 *__restrict__ rr,
-                                         const float4 *__restrict__ fb) {
+// The neighbour data one pair's adjoint reads: position, evaluated
+// velocity, density and its reciprocal, and (for a pair the neighbour owns)
+// the neighbour's force cotangent.
+struct PairData {
+    float4 qp, qe, fq;
+    float2 rq2;
+};
+
+__device__ __forceinline__ PairData load_pair(uint32_t entry, const float4 *__restrict__ pos,
+                                              const float4 *__restrict__ veval, const float2 *__restrict__ rr,
+                                              const float4 *__restrict__ fb) {
+    const uint32_t q = entry & kSlotMask;
+    PairData d;
+    d.qp = pos[q];
+    d.qe = veval[q];
+    d.rq2 = rr[q];
+    d.fq = (entry & (kRevFlag | kBothFlag)) ? fb[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+    return d;
+}
+
+__device__ __forceinline__ void apply_pair(const DevParams &P, AdjAcc &a, float3 X, float3 Ev, float rs, float3 fs,
+                                           float irs, uint32_t entry, const PairData &d) {
     const bool rev_only = (entry & kRevFlag) != 0u;
     const bool both = (entry & kBothFlag) != 0u;
-    const uint32_t q = entry & kSlotMask;
-    const float4 qp = pos[q];
-    const float3 D = make_float3(X.x - qp.x, X.y - qp.y, X.z - qp.z);
+    const float3 D = make_float3(X.x - d.qp.x, X.y - d.qp.y, X.z - d.qp.z);
     const float dsq = D.x * D.x + D.y * D.y + D.z * D.z;
-    const float4 qe = veval[q];
-    const float3 dE = make_float3(qe.x - Ev.x, qe.y - Ev.y, qe.z - Ev.z);
-    const float2 rq2 = rr[q];
-    const PairGeo g = pair_geometry(P, D, dE, dsq, rs, rq2.x, irs * rq2.y);
-    float3 fq = make_float3(0.f, 0.f, 0.f);
-    if (rev_only || both) fq = xyz(fb[q]);
+    const float3 dE = make_float3(d.qe.x - Ev.x, d.qe.y - Ev.y, d.qe.z - Ev.z);
+    const PairGeo g = pair_geometry(P, D, dE, dsq, rs, d.rq2.x, irs * d.rq2.y);
+    const float3 fq = xyz(d.fq);
     const float DF = apply_cotangent(P, a, g, rev_only ? fq : fs, rev_only ? -1.0f : 1.0f, irs);
     if (!rev_only) {
         a.gv += P.lapkern * dot3(dE, fs) * g.B;
         a.gr += g.B * DF * g.AcR * (-2.0f * P.pintstiff);
-        a.gk += g.B * DF * g.AcR * ((rs - P.prest_dens) + (rq2.x - P.prest_dens));
+        a.gk += g.B * DF * g.AcR * ((rs - P.prest_dens) + (d.rq2.x - P.prest_dens));
     }
     if (both) apply_cotangent(P, a, g, fq, -1.0f, irs);
+}
+
+__device__ __forceinline__ void adj_pair(const DevParams &P, AdjAcc &a, float3 X, float3 Ev, float rs, float3 fs,
+                                         float irs, uint32_t entry, const float4 *__restrict__ pos,
+                                         const float4 *__restrict__ veval, const float2 *__restrict__ rr,
+                                         const float4 *__restrict__ fb) {
+    apply_pair(P, a, X, Ev, rs, fs, irs, entry, load_pair(entry, pos, veval, rr, fb));
 }
 
 // The reverse search block of a point in local cell lc: entry k of the
