@@ -102,7 +102,7 @@ def parse():
     ap.add_argument("--profile", action="store_true",
                     help="profiling run for ncu: the wave tank of --n points, --warmup eager steps, then "
                          "--steps eager steps (one launch per kernel per step), no timing, no JSON line")
-    ap.add_argument("--passes", choices=["cells", "points"], default="points",
+    ap.add_argument("--passes", choices=["cells", "points", "pairs"], default="points",
                     help="neighbour passes of the fused step (bit-identical results)")
     ap.add_argument("--fit-iters", type=int, default=40,
                     help="iterations of the 64-scene batched parameter fit (0 skips it)")

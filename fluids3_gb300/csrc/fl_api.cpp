@@ -190,7 +190,7 @@ extern "C" int fl_create(const fl_params *p, int max_points, fl_system **out) {
     FL_TRY(check_derived(p));
     fl_system *s = (fl_system *)calloc(1, sizeof(fl_system));
     if (!s) return fl_fail(FL_ERR_NOMEM, "fl_create: host allocation failed");
-    s->cell_passes = 0;   // the per-point passes: the faster step (fl_set_neighbour_passes)
+    s->passes = FL_PASSES_PER_POINT;   // the faster step (fl_set_neighbour_passes)
     int r = FL_OK;
     do {
         if (cudaGetDevice(&s->device) != cudaSuccess) {
@@ -233,6 +233,7 @@ extern "C" int fl_create(const fl_params *p, int max_points, fl_system **out) {
         }
         if ((r = fl_kernels_init(s)) != FL_OK) break;
         if ((r = fl_cells_init(s)) != FL_OK) break;
+        if ((r = fl_pairs_init()) != FL_OK) break;
         if ((r = fl_dalloc((void **)&s->dev_err, 256)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&s->time_dev, 256)) != FL_OK) break;
         if ((r = alloc_grid(s)) != FL_OK) break;
@@ -302,6 +303,7 @@ extern "C" int fl_batch_create(const fl_params *params, const int *counts, int n
         s->batched = 1;
         s->nscenes = nscenes;
         if ((r = fl_cells_init(s)) != FL_OK) break;
+        if ((r = fl_pairs_init()) != FL_OK) break;
         free_grid(s);
         s->ncells = (int)ncell;
         s->gcells = (int)gcell;
@@ -855,7 +857,7 @@ static int record(fl_system *s, TimingState *t, int k) {
 // every scene) with band codes from this step's sort. A recording tape keeps
 // the per-point passes (its hooks keep each step's pair lists).
 static bool use_cell_passes(const fl_system *s, bool taped) {
-    return s->cell_passes && s->D.prune && s->codes_valid && !taped && s->n > 0;
+    return s->passes == FL_PASSES_CELL_TASKS && s->D.prune && s->codes_valid && !taped && s->n > 0;
 }
 
 static int run_step(fl_system *s, TimingState *t) {
@@ -1258,18 +1260,18 @@ extern "C" int fl_set_launch_shapes(fl_system *s, const int *shapes) {
 
 extern "C" int fl_set_neighbour_passes(fl_system *s, int mode) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_set_neighbour_passes: null system");
-    if (mode != FL_PASSES_PER_POINT && mode != FL_PASSES_CELL_TASKS)
-        return fl_fail(FL_ERR_ARG, "fl_set_neighbour_passes: mode %d is neither %d nor %d", mode,
-                       FL_PASSES_PER_POINT, FL_PASSES_CELL_TASKS);
+    if (mode != FL_PASSES_PER_POINT && mode != FL_PASSES_CELL_TASKS && mode != FL_PASSES_POINT_PAIRS)
+        return fl_fail(FL_ERR_ARG, "fl_set_neighbour_passes: mode %d is none of %d, %d, %d", mode,
+                       FL_PASSES_PER_POINT, FL_PASSES_CELL_TASKS, FL_PASSES_POINT_PAIRS);
     FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
-    s->cell_passes = mode == FL_PASSES_CELL_TASKS;
+    s->passes = mode;
     destroy_graph(s);   // the captured step holds the other passes
     return FL_OK;
 }
 
 extern "C" int fl_neighbour_passes(const fl_system *s) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_neighbour_passes: null system");
-    return s->cell_passes ? FL_PASSES_CELL_TASKS : FL_PASSES_PER_POINT;
+    return s->passes;
 }
 
 extern "C" int fl_launch_shapes(fl_system *s, int *shapes) {

@@ -50,31 +50,6 @@ constexpr uint32_t kRing = 64;     // staged candidates per warp (at most 63 are
 constexpr uint32_t kMaskWords = 16; // hit-mask words kept per point: unions of up to 512 candidates
 constexpr uint32_t kPairCap = 512; // hit pairs of one group evaluated pair-parallel (else per lane)
 
-// ---- packed f32x2 arithmetic (round-to-nearest per element) ---------------
-__device__ __forceinline__ uint64_t pk2(float a, float b) {
-    uint64_t r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ void up2(uint64_t v, float &a, float &b) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-}
-__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
-    uint64_t r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
-    uint64_t r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
-    uint64_t r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-
 // ---- tasks ------------------------------------------------------------------
 // counters (in the grid block, cleared with the counts every step):
 // [0] tasks listed, [1] density pass ticket, [2] force pass ticket.

@@ -133,7 +133,7 @@ struct fl_system {
     uint2 *tasks;
     size_t task_cap;
     uint32_t *task_counters;
-    int cell_passes;       // 1: the fused step uses the cell-task passes where it can
+    int passes;            // FL_PASSES_*: the neighbour passes of the fused step
     int cells_grid[2];     // blocks of the cell-task density and force passes (all resident)
 
     uint32_t *hitlist;     // ceil(N/32) * hcap * 32 entries
@@ -299,6 +299,8 @@ int fl_launch_make_tasks(fl_system *s);
 // densities and pair records, plus the force pass's hit masks or (lists) the
 // per-point pair lists and counts in the per-point pass's layout
 int fl_launch_density_cells(fl_system *s, bool lists = false);
+int fl_launch_density_pairs(fl_system *s);
+int fl_pairs_init();   // once per process is enough; outside any stream capture
 // force + advance over the tasks from the hit masks; host_pos (a
 // device-usable pointer to page-locked host memory, or null) also receives
 // the new positions as float x3

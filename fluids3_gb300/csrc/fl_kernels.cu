@@ -1037,6 +1037,7 @@ static auto density_kernel(bool prune) {
 
 int fl_launch_density(fl_system *s) {
     if (s->n == 0) return FL_OK;
+    if (s->passes == FL_PASSES_POINT_PAIRS && use_prune(s)) return fl_launch_density_pairs(s);
     auto kern = s->batched ? density_kernel<true>(use_prune(s)) : density_kernel<false>(use_prune(s));
     const int bs = s->blk_density ? s->blk_density : kThreads;
     kern<<<blocks_for(s->n, bs), bs, grouping_smem(bs, kBandKeys), s->stream>>>(

@@ -1,9 +1,40 @@
 // Per-point arithmetic of the step shared by the neighbour passes
-// (fl_kernels.cu, fl_cells.cu): one pair's force term and the advance of
-// one point, each in the reference kernels' own operation order. Included
+// (fl_kernels.cu, fl_cells.cu): packed FP32 helpers, one pair's force term
+// and the advance of one point, each in the reference kernels' own
+// operation order. Included
 // inside each file's anonymous namespace; both files are compiled without
 // FMA contraction, so every expression rounds as written.
 #pragma once
+
+// ---- packed f32x2 arithmetic (round-to-nearest per element) ---------------
+// Each packed operation rounds exactly like its scalar form, but ptxas
+// contracts a packed add of two packed products into a packed fused
+// multiply-add (measured on GB300, explicit .rn and --fmad=false
+// notwithstanding): no add2 here may take two mul2 results.
+__device__ __forceinline__ uint64_t pk2(float a, float b) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void up2(uint64_t v, float &a, float &b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+    uint64_t r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
+    uint64_t r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+    uint64_t r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
 
 struct ForcePoint {
     float4 p, vi;

@@ -351,16 +351,16 @@ static int run_reverse(fl_system *s, fl_tape *t) {
             FL_CUDA_TRY(cudaMemcpyAsync(s->time_dev + s->time_slot, t->time + k, sizeof(float),
                                         cudaMemcpyDeviceToDevice, s->stream));
             uint32_t *own_list = s->hitlist, *own_cnt = s->hitcnt;
-            const int own_passes = s->cell_passes;
-            if (t->keep_lists) {   // the step's (per-point) density pass writes its lists into the slot
+            const int own_passes = s->passes;
+            if (t->keep_lists) {   // the step's density pass (one that writes pair lists) fills the slot
                 s->hitlist = t->seg_list + (size_t)(k - t0) * t->list_words;
                 s->hitcnt = t->seg_cnt + (size_t)(k - t0) * t->cap;
-                s->cell_passes = 0;
+                if (s->passes == FL_PASSES_CELL_TASKS) s->passes = FL_PASSES_PER_POINT;
             }
             const int r = fl_step_fused(s);
             s->hitlist = own_list;
             s->hitcnt = own_cnt;
-            s->cell_passes = own_passes;
+            s->passes = own_passes;
             FL_TRY(r);
             FL_TRY(save_force(s, t->force + (size_t)(k - t0) * t->cap));
             if (t->keep_lists && s->n)

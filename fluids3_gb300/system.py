@@ -68,6 +68,9 @@ def _ptr(a: np.ndarray | None):
     return a.ctypes.data_as(C.c_void_p)
 
 
+# fl_set_neighbour_passes modes, by value (FL_PASSES_*)
+PASSES = ("points", "cells", "pairs")
+
 class FluidSystem:
     """One SPH system on the current CUDA device.
 
@@ -394,14 +397,16 @@ class FluidSystem:
         call("fl_set_launch_shapes", self._h, shapes)
 
     def SetNeighbourPasses(self, mode: str) -> None:
-        """Neighbour passes of the fused step: "points" (default, the faster
-        step), one thread per point (the reference's loop structure);
-        "cells", one warp per 64 points of a cell walks their shared search
-        block in lockstep. Results are bit-identical."""
-        call("fl_set_neighbour_passes", self._h, {"points": 0, "cells": 1}[mode])
+        """Neighbour passes of the fused step: "points" (default), one thread
+        per point (the reference's loop structure); "cells", one warp per 64
+        points of a cell walks their shared search block in lockstep;
+        "pairs", the per-point passes with a density walk shared by two
+        points of a cell that visit the same candidates (every density pass
+        of the system). Results are bit-identical."""
+        call("fl_set_neighbour_passes", self._h, PASSES.index(mode))
 
     def NeighbourPasses(self) -> str:
-        return ("points", "cells")[call("fl_neighbour_passes", self._h)]
+        return PASSES[call("fl_neighbour_passes", self._h)]
 
     # -- timing ---------------------------------------------------------------
     def SetTiming(self, enable: bool) -> None:

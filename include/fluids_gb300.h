@@ -343,10 +343,16 @@ int fl_set_launch_shapes(fl_system *s, const int *shapes);
  * masks; the force pass walks the block again and evaluates the hits
  * pair-parallel. Used where the pruned search applies (gridSrch 2 in every
  * scene) and no tape is recording; the phase entry points and recording
- * tapes always use the per-point passes. No counterpart in the reference
- * (which has only the per-point walk). */
-#define FL_PASSES_PER_POINT  0
-#define FL_PASSES_CELL_TASKS 1
+ * tapes always use the per-point passes. FL_PASSES_POINT_PAIRS: the
+ * per-point passes, except that where the pruned search applies one thread
+ * walks the search block once for two points of a cell with the same
+ * lower-band bits (which visit the same candidates in the same order); this
+ * one holds for every density pass of the system (fused step, phase entry
+ * points, tapes). No counterpart in the reference (which has only the
+ * per-point walk). */
+#define FL_PASSES_PER_POINT   0
+#define FL_PASSES_CELL_TASKS  1
+#define FL_PASSES_POINT_PAIRS 2
 int fl_set_neighbour_passes(fl_system *s, int mode);
 int fl_neighbour_passes(const fl_system *s);
 

@@ -1,16 +1,19 @@
-"""The cell-task neighbour passes (fl_cells.cu) against the per-point passes.
+"""The alternative neighbour passes against the per-point passes.
 
-With FL_PASSES_CELL_TASKS the fused step walks each cell's shared search
-block once per 64 of its points, in lockstep, and evaluates the hits
-pair-parallel; the adjoint's rebuilt steps take their pair lists from the
-cell-task density. Every point's sums keep the reference's terms and order,
-so both give bit-identical states: checked over many steps on the wave
-tank, on crowded cells (tasks of one cell split over many warps, unions of
-thousands of candidates, groups past the pair-parallel cap), on cells of
+With FL_PASSES_CELL_TASKS (fl_cells.cu) the fused step walks each cell's
+shared search block once per 64 of its points, in lockstep, and evaluates
+the hits pair-parallel; the adjoint's rebuilt steps take their pair lists
+from the cell-task density. With FL_PASSES_POINT_PAIRS (fl_pairs.cu) every
+density pass walks the search block once for two points of a cell with the
+same lower-band bits. Every point's sums keep the reference's terms and
+order, so all give bit-identical states: checked over many steps on the
+wave tank, on crowded cells (tasks of one cell split over many warps,
+unions of thousands of candidates, groups past the pair-parallel cap; runs
+of hundreds of equal points split over blocks of 1024 slots), on cells of
 1..64 points (one and two points per lane), on batches, through graph
 replay and fl_run_from_host (whose cell-task force pass writes the new
-positions into the caller's page-locked array), against the oracle step by
-step, and through the adjoint.
+positions into the caller's page-locked array), through the phase entry
+points, against the oracle step by step, and through the adjoint.
 """
 from __future__ import annotations
 
@@ -27,9 +30,12 @@ pytestmark = pytest.mark.gpu
 UNDEF = 0xFFFFFFFF
 
 
-def run_both(params, pos, vel, veval, clr, steps, graph=True):
+ALTS = pytest.mark.parametrize("alt", ["cells", "pairs"])
+
+
+def run_both(params, pos, vel, veval, clr, steps, graph=True, alt="cells"):
     out = {}
-    for mode in ("points", "cells"):
+    for mode in ("points", alt):
         with F.FluidSystem(params, pos.shape[0]) as s:
             s.SetParticles(pos, vel, veval, clr=clr)
             s.SetNeighbourPasses(mode)
@@ -42,7 +48,7 @@ def run_both(params, pos, vel, veval, clr, steps, graph=True):
             s.Sync()
             assert s.IntegrityCheck() == 0
             out[mode] = s.state()
-    return out["points"], out["cells"]
+    return out["points"], out[alt]
 
 
 def assert_states_equal(a, b, what):
@@ -50,23 +56,27 @@ def assert_states_equal(a, b, what):
         assert_bit_equal(b[k], a[k], f"{what}: {k}")
 
 
-def test_cells_equal_points_on_the_wave_tank():
+@ALTS
+def test_alt_equals_points_on_the_wave_tank(alt):
     sc = scenes.wave_tank(n=300_000)
-    a, b = run_both(sc.params, sc.pos, sc.vel, sc.veval, sc.clr, 40)
+    a, b = run_both(sc.params, sc.pos, sc.vel, sc.veval, sc.clr, 40, alt=alt)
     assert_states_equal(a, b, "wave tank, 40 steps")
 
 
+@ALTS
 @pytest.mark.parametrize("graph", [False, True])
-def test_cells_equal_points_on_the_dam_break(graph):
+def test_alt_equals_points_on_the_dam_break(graph, alt):
     sc = scenes.dam_break()
-    a, b = run_both(sc.params, sc.pos, sc.vel, sc.veval, sc.clr, 30, graph=graph)
+    a, b = run_both(sc.params, sc.pos, sc.vel, sc.veval, sc.clr, 30, graph=graph, alt=alt)
     assert_states_equal(a, b, "dam break, 30 steps")
 
 
+@ALTS
 @pytest.mark.parametrize("m", [1, 31, 32, 33, 63, 64, 65, 129, 700, 3000])
-def test_cells_equal_points_with_a_crowded_cell(m):
+def test_alt_equals_points_with_a_crowded_cell(m, alt):
     """m points packed into one cell among a dam break: tasks of 1..64
-    points, a cell split into several tasks, unions of thousands."""
+    points, a cell split into several tasks, unions of thousands; runs of
+    equal points longer than a block."""
     sc = scenes.dam_break(n=6000, seed=31)
     p = sc.params
     rng = np.random.default_rng(100 + m)
@@ -74,17 +84,18 @@ def test_cells_equal_points_with_a_crowded_cell(m):
     pick = rng.choice(pos.shape[0], size=m, replace=False)
     c = np.array([p.gridMin[0] + 7.5 * 5.0, p.gridMin[1] + 5.5 * 5.0, p.gridMin[2] + 6.5 * 5.0], np.float32)
     pos[pick] = c + rng.uniform(-2.4, 2.4, size=(m, 3)).astype(np.float32)
-    a, b = run_both(p, pos, sc.vel, sc.veval, sc.clr, 4)
+    a, b = run_both(p, pos, sc.vel, sc.veval, sc.clr, 4, alt=alt)
     assert_states_equal(a, b, f"crowded cell of {m}")
 
 
-def test_cells_match_the_oracle_step_by_step():
+@ALTS
+def test_alt_matches_the_oracle_step_by_step(alt):
     sc = scenes.dam_break(n=20_000, seed=4)
     p = sc.params
     with F.FluidSystem(p, sc.n) as s:
         s.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
         assert s.NeighbourPasses() == "points"   # the default
-        s.SetNeighbourPasses("cells")
+        s.SetNeighbourPasses(alt)
         s.RunSteps(40)
         s.Sync()
         for _ in range(3):
@@ -98,25 +109,27 @@ def test_cells_match_the_oracle_step_by_step():
                 assert_bit_equal(st[k], getattr(ref, k), k)
 
 
-def test_cells_equal_points_on_a_batch():
+@ALTS
+def test_alt_equals_points_on_a_batch(alt):
     scs = scenes.batch_scenes(nscenes=12, seed=23, nmin=500, nmax=20000)
     cat = scenes.concat(scs)
     out = {}
-    for mode in ("points", "cells"):
+    for mode in ("points", alt):
         with F.FluidSystem.batch([sc.params for sc in scs], [sc.n for sc in scs]) as b:
             b.SetParticles(cat["pos"], cat["vel"], cat["veval"], clr=cat["clr"])
             b.SetNeighbourPasses(mode)
             b.RunSteps(25)
             b.Sync()
             out[mode] = b.state()
-    assert_states_equal(out["points"], out["cells"], "batch of 12, 25 steps")
+    assert_states_equal(out["points"], out[alt], "batch of 12, 25 steps")
 
 
-def test_cells_with_escaped_points_and_nan():
+@ALTS
+def test_alt_with_escaped_points_and_nan(alt):
     sc = scenes.dam_break(n=3000, seed=12)
     pos = sc.pos.copy()
     pos[:4] = [(-500.0, 1.0, 1.0), (1.0, -300.0, 1.0), (np.nan, 0.0, 0.0), (1e30, 1e30, 1e30)]
-    a, b = run_both(sc.params, pos, sc.vel, sc.veval, sc.clr, 3)
+    a, b = run_both(sc.params, pos, sc.vel, sc.veval, sc.clr, 3, alt=alt)
     assert_states_equal(a, b, "escapes")
     assert (b["gcell"] == UNDEF).sum() >= 4
 
@@ -159,15 +172,16 @@ def test_run_from_host_with_cells_writes_positions_back():
             a.free()
 
 
+@ALTS
 @pytest.mark.parametrize("every", [1, 3])
-def test_adjoint_identical_with_either_passes(every):
-    """The adjoint's rebuilt steps take their pair lists from the cell-task
-    density and its segment replays run the cell-task step: gradients must
-    equal those of the per-point pass bit for bit."""
+def test_adjoint_identical_with_any_passes(every, alt):
+    """The adjoint's rebuilt steps take their pair lists from the selected
+    density pass and its segment replays run the selected step: gradients
+    must equal those of the per-point pass bit for bit."""
     sc = scenes.dam_break(n=6000, seed=41)
     w = np.random.default_rng(42).standard_normal((3, sc.n, 3)).astype(np.float32)
     got = {}
-    for mode in ("points", "cells"):
+    for mode in ("points", alt):
         with F.FluidSystem(sc.params, sc.n) as s:
             s.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
             s.SetNeighbourPasses(mode)
@@ -177,5 +191,33 @@ def test_adjoint_identical_with_either_passes(every):
                 s.Run()
             got[mode] = s.Backward(*w)
     for k, name in enumerate(("pos", "vel", "veval")):
-        assert_bit_equal(got["cells"][k], got["points"][k], f"every={every}: dL/d{name}")
-    assert np.array_equal(got["cells"][3], got["points"][3])
+        assert_bit_equal(got[alt][k], got["points"][k], f"every={every}: dL/d{name}")
+    assert np.array_equal(got[alt][3], got["points"][3])
+
+
+@pytest.mark.parametrize("n", [1, 2, 1023, 1024, 1025, 5000])
+def test_pairs_through_the_phase_entry_points(n):
+    """The reference's phase sequence (insert, prefix sum, counting sort,
+    ComputePressure, ComputeForce, Advance) with the paired density: the
+    same densities, pair lists and forces as the per-point pass, at sizes
+    around the pass's 1024-slot blocks."""
+    sc = scenes.dam_break(n=max(n, 2), seed=7)
+    pos, vel, veval, clr = sc.pos[:n], sc.vel[:n], sc.veval[:n], sc.clr[:n]
+    if n == 2:   # two points of one cell with the same band bits: one item
+        pos = np.array([[0.0, 0.0, 0.0]], np.float32) + sc.pos[:1]
+        pos = np.concatenate([pos, pos + np.float32(0.01)])
+    out = {}
+    for mode in ("points", "pairs"):
+        with F.FluidSystem(sc.params, n) as s:
+            s.SetParticles(pos, vel, veval, clr=clr)
+            s.SetNeighbourPasses(mode)
+            for _ in range(3):
+                s.InsertParticlesCUDA()
+                s.PrefixSumCellsCUDA(1)
+                s.CountingSortFullCUDA()
+                s.ComputePressureCUDA()
+                s.ComputeForceCUDA()
+                s.AdvanceCUDA(s.time, sc.params.dt, sc.params.sim_scale)
+            s.Sync()
+            out[mode] = s.state()
+    assert_states_equal(out["points"], out["pairs"], f"phase sequence, n={n}")

@@ -709,11 +709,11 @@ def test_run_from_host_equals_set_particles_then_run(case):
             p.free()
 
 
-@pytest.mark.parametrize("passes", ["points", "cells"])
+@pytest.mark.parametrize("passes", ["points", "cells", "pairs"])
 def test_run_from_host_reads_back_in_slot_ranges(passes):
     """Above 2^21 points the force pass of fl_run_from_host runs in slot
     ranges whose positions go back while the next range computes (after
-    either density pass): the positions read back and the state still equal
+    any density pass): the positions read back and the state still equal
     SetParticles + Run + GetBuffer."""
     sc = scenes.wave_tank(n=2_200_000)
     n = sc.n
