@@ -465,15 +465,10 @@ struct CrowdList {
 // block a point visits (all threads of the block call it, with
 // grouping_smem(blockDim, kBandKeys) bytes of dynamic shared memory).
 template <bool PRUNE>
-__global__ void __launch_bounds__(kThreads)
-k_adj_revwalk(const __grid_constant__ DevParams P0, const SceneTab T, int n, const float4 *__restrict__ pos,
-              const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ off,
-              const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
-              uint32_t *__restrict__ revlist, uint32_t *__restrict__ revcnt) {
-    extern __shared__ uint32_t s_dyn[];
-    const int s = PRUNE ? band_grouped_slot(n, pos, gcell, 0, s_dyn) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    if (s >= n) return;
-    const DevParams &P = scene_params(P0, T, s);
+__device__ __forceinline__ void rev_walk_point(const DevParams &P, int s, const float4 *__restrict__ pos,
+                                               const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ off,
+                                               const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
+                                               uint32_t *__restrict__ revlist, uint32_t *__restrict__ revcnt) {
     const uint32_t gc = gcell[s];
     uint32_t nrev = 0;
     if (gc != kUndef) {
@@ -503,6 +498,134 @@ k_adj_revwalk(const __grid_constant__ DevParams P0, const SceneTab T, int n, con
         }
     }
     revcnt[s] = nrev;
+}
+
+template <bool PRUNE>
+__global__ void __launch_bounds__(kThreads)
+k_adj_revwalk(const __grid_constant__ DevParams P0, const SceneTab T, int n, const float4 *__restrict__ pos,
+              const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ off,
+              const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
+              uint32_t *__restrict__ revlist, uint32_t *__restrict__ revcnt) {
+    extern __shared__ uint32_t s_dyn[];
+    const int s = PRUNE ? band_grouped_slot(n, pos, gcell, 0, s_dyn) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (s >= n) return;
+    rev_walk_point<PRUNE>(scene_params(P0, T, s), s, pos, gcell, off, cnt, upbits, revlist, revcnt);
+}
+
+// The walk for the points k_adj_revsort listed (reverse lists too long to
+// sort in registers), a grid-stride loop over the listed count.
+template <bool PRUNE>
+__global__ void __launch_bounds__(kThreads)
+k_adj_revwalk_listed(const __grid_constant__ DevParams P0, const SceneTab T, const float4 *__restrict__ pos,
+                     const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ off,
+                     const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
+                     const uint32_t *__restrict__ listed, const uint32_t *__restrict__ listed_count,
+                     uint32_t *__restrict__ revlist, uint32_t *__restrict__ revcnt) {
+    const uint32_t m = *listed_count;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+        const int s = (int)listed[k];
+        rev_walk_point<PRUNE>(scene_params(P0, T, s), s, pos, gcell, off, cnt, upbits, revlist, revcnt);
+    }
+}
+
+// The same reverse lists by transposing the density pass's pair lists
+// (one thread per owner q; the walk above is kept for comparison): every
+// pair (q, s) of q's list with s outside q's cell is a reverse pair of s
+// outside its own cell, and the pair lists hold exactly the pairs that pass
+// (the test is symmetric). Each is appended to s's list at a position taken
+// from s's count by an atomic; k_adj_revsort then puts every list in
+// ascending slot order, the walk's order (the reverse block's cells in
+// ascending index, each in ascending slot), so consumers see the same
+// lists. An owner whose own list overflowed walks its search block again.
+// revcnt must be zero before the launch.
+template <bool PRUNE>
+__global__ void __launch_bounds__(kThreads)
+k_adj_revscatter(const __grid_constant__ DevParams P0, const SceneTab T, int n, const float4 *__restrict__ pos,
+                 const uint32_t *__restrict__ gcell, const uint32_t *__restrict__ off,
+                 const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ upbits,
+                 const uint32_t *__restrict__ hitlist, const uint32_t *__restrict__ hitcnt,
+                 uint32_t *__restrict__ revlist, uint32_t *__restrict__ revcnt) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const uint32_t gq = gcell[q];
+    if (gq == kUndef) return;
+    const DevParams &P = scene_params(P0, T, q);
+    const uint32_t hcap = (uint32_t)P.hcap;
+    auto push = [&](uint32_t s) {
+        if (gcell[s] == gq) return;   // in q's cell: a pair of s's own cell
+        const uint32_t at = atomicAdd(&revcnt[s], 1u);
+        if (at < hcap) revlist[list_at(P, (int)s, at)] = (uint32_t)q;
+    };
+    const uint32_t nh = hitcnt[q];
+    if (nh <= hcap) {
+        for (uint32_t t = 0; t < nh; t++) push(hitlist[list_at(P, q, t)]);
+        return;
+    }
+    const float4 p = pos[q];
+    const int base = (int)gq - P.nadj;
+    for (int c = 0; c < P.gridAdjCnt; c++) {
+        CandIter it;
+        cand_begin<PRUNE>(it, P, c, base + P.adj[c], __float_as_uint(p.w), true, off, cnt, upbits);
+        uint32_t j;
+        while (cand_next<PRUNE>(it, P, upbits, j)) {
+            const float4 o = pos[j];
+            const float dsq = dsq_rn(p.x - o.x, p.y - o.y, p.z - o.z);
+            if (dsq < P.rd2 && dsq > 0.0f) push(j);
+        }
+    }
+}
+
+// Ascending order for each reverse list of k_adj_revscatter: up to 32
+// entries by a bitonic network in registers (a warp runs the network its
+// longest list needs); a longer list is listed for k_adj_revwalk_listed,
+// which writes it again by walking; a count above hcap becomes hcap + 1,
+// the walk's overflow mark.
+template <int N>
+__device__ __forceinline__ void sort_row(uint32_t *row, uint32_t c) {   // entry t at row[32 t]
+    uint32_t r[N];
+#pragma unroll
+    for (int t = 0; t < N; t++) r[t] = ((uint32_t)t < c) ? row[32 * t] : 0xffffffffu;
+#pragma unroll
+    for (int k = 2; k <= N; k <<= 1)
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1)
+#pragma unroll
+            for (int i = 0; i < N; i++) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const uint32_t lo = min(r[i], r[l]), hi = max(r[i], r[l]);
+                    const bool up = (i & k) == 0;
+                    r[i] = up ? lo : hi;
+                    r[l] = up ? hi : lo;
+                }
+            }
+#pragma unroll
+    for (int t = 0; t < N; t++)
+        if ((uint32_t)t < c) row[32 * t] = r[t];
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_adj_revsort(int n, int hcap_in, uint32_t *__restrict__ revlist, uint32_t *__restrict__ revcnt,
+              uint32_t *__restrict__ listed, uint32_t *__restrict__ listed_count) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (blockIdx.x * blockDim.x + (threadIdx.x & ~31u) >= (unsigned)n) return;   // whole warp past n
+    const uint32_t hcap = (uint32_t)hcap_in;
+    uint32_t c = (s < n) ? revcnt[s] : 0u;
+    if (c > hcap) {
+        revcnt[s] = hcap + 1;
+        c = 0;
+    } else if (c > 32) {
+        listed[atomicAdd(listed_count, 1u)] = (uint32_t)s;
+        c = 0;
+    }
+    if (c < 2) c = 0;
+    // one network per warp, the size its longest list needs
+    const uint32_t most = __reduce_max_sync(0xffffffffu, c);
+    if (most == 0) return;
+    uint32_t *row = revlist + ((size_t)(s >> 5) * hcap) * 32u + (uint32_t)(s & 31);
+    if (most <= 8) sort_row<8>(row, c);
+    else if (most <= 16) sort_row<16>(row, c);
+    else sort_row<32>(row, c);
 }
 
 // Reverse of computeForce for point s (all 32 lanes of a warp call it):
@@ -931,28 +1054,62 @@ __device__ __forceinline__ float abs_max4(float4 v, float m) {
 
 // Per-scene largest |component| of (dL/dX, dL/dV, dL/dE) as float bits
 // (non-negative floats order like their bit patterns); NaN is kept as the
-// largest value so that no scaling hides it.
-__global__ void __launch_bounds__(kThreads)
+// largest value so that no scaling hides it. A block takes kGmaxPoints
+// consecutive slots; a scene's points are one slot range, so a block whose
+// first and last slots share a scene reduces in shared memory and issues
+// one atomic (one per point on the same address was the kernel's cost),
+// and a block across a scene boundary issues one per warp and scene.
+constexpr int kGmaxThreads = 256;
+constexpr int kGmaxPer = 8;
+constexpr int kGmaxPoints = kGmaxThreads * kGmaxPer;
+
+__device__ __forceinline__ uint32_t gmax_bits(const float4 a, const float4 b, const float4 c) {
+    const float m = abs_max4(c, abs_max4(b, abs_max4(a, 0.0f)));
+    const bool nan = isnan(a.x + a.y + a.z + b.x + b.y + b.z + c.x + c.y + c.z);
+    return nan ? 0x7fffffffu : __float_as_uint(m);
+}
+
+__global__ void __launch_bounds__(kGmaxThreads)
 k_adj_gmax(int n, const uint16_t *__restrict__ point_scene, const float4 *__restrict__ gx,
            const float4 *__restrict__ gv, const float4 *__restrict__ ge, uint32_t *__restrict__ gmax) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = i < n;
-    float m = 0.0f;
-    bool nan = false;
-    uint32_t scene = 0;
-    if (valid) {
-        const float4 a = gx[i], b = gv[i], c = ge[i];
-        m = abs_max4(c, abs_max4(b, abs_max4(a, 0.0f)));
-        nan = isnan(a.x + a.y + a.z + b.x + b.y + b.z + c.x + c.y + c.z);
-        scene = point_scene ? point_scene[i] : 0u;
-    }
-    uint32_t bits = nan ? 0x7fffffffu : __float_as_uint(m);
-    const uint32_t s0 = __shfl_sync(0xffffffffu, scene, 0);
-    if (__all_sync(0xffffffffu, !valid || scene == s0)) {
+    __shared__ uint32_t s_max[kGmaxThreads / 32];
+    const int b0 = blockIdx.x * kGmaxPoints;
+    const int last = min(b0 + kGmaxPoints, n) - 1;
+    const unsigned lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    const uint32_t first_scene = point_scene ? point_scene[b0] : 0u;
+    if (!point_scene || point_scene[last] == first_scene) {
+        uint32_t bits = 0;
+#pragma unroll
+        for (int k = 0; k < kGmaxPer; k++) {
+            const int i = b0 + k * kGmaxThreads + (int)threadIdx.x;
+            if (i < n) bits = max(bits, gmax_bits(gx[i], gv[i], ge[i]));
+        }
         bits = __reduce_max_sync(0xffffffffu, bits);
-        if ((threadIdx.x & 31u) == 0 && bits) atomicMax(&gmax[s0], bits);
-    } else if (valid && bits) {
-        atomicMax(&gmax[scene], bits);
+        if (lane == 0) s_max[w] = bits;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t m = 0;
+#pragma unroll
+            for (int k = 0; k < kGmaxThreads / 32; k++) m = max(m, s_max[k]);
+            if (m) atomicMax(&gmax[first_scene], m);
+        }
+        return;
+    }
+    for (int k = 0; k < kGmaxPer; k++) {   // across a scene boundary
+        const int i = b0 + k * kGmaxThreads + (int)threadIdx.x;
+        const bool valid = i < n;
+        uint32_t bits = 0, scene = 0;
+        if (valid) {
+            bits = gmax_bits(gx[i], gv[i], ge[i]);
+            scene = point_scene[i];
+        }
+        const uint32_t s0 = __shfl_sync(0xffffffffu, scene, 0);
+        if (__all_sync(0xffffffffu, !valid || scene == s0)) {
+            bits = __reduce_max_sync(0xffffffffu, bits);
+            if (lane == 0 && bits) atomicMax(&gmax[s0], bits);
+        } else if (valid && bits) {
+            atomicMax(&gmax[scene], bits);
+        }
     }
 }
 
@@ -1056,16 +1213,37 @@ static int crowd_grid(const fl_system *s) { return 4 * s->num_sms; }
 
 int fl_launch_adj_force(fl_system *s, const float2 *rr, const float4 *fb, float4 *xa, const float4 *ea, float *rb,
                         float4 *pc, float4 *e_out, uint32_t *revlist, uint32_t *revcnt, uint32_t *crowd,
-                        uint32_t *crowd_count) {
+                        uint32_t *crowd_count, uint32_t *revlong, uint32_t *revlong_count) {
     if (s->n == 0) return FL_OK;
     if (s->max_points > (int)kSlotMask)
         return fl_fail(FL_ERR_CAPACITY, "adjoint: %d points (at most %u)", s->max_points, kSlotMask);
     const bool pr = adj_prune(s);
-    auto walk = pr ? k_adj_revwalk<true> : k_adj_revwalk<false>;
-    walk<<<blocks_for(s->n, kThreads), kThreads, grouping_smem(kThreads, kBandKeys), s->stream>>>(
-        s->D, fl_scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt,
-        s->upbits, revlist, revcnt);
-    FL_LAUNCH_CHECK("adj_revwalk");
+    // the transposition saves work but adds three launches: it pays on
+    // large systems, where the reverse step is bound by throughput
+    const bool walk = s->adj_revmode == FL_REVERSE_WALK ||
+                      (s->adj_revmode == FL_REVERSE_AUTO && s->n < FL_REVERSE_TRANSPOSE_MIN);
+    if (walk) {
+        auto walk = pr ? k_adj_revwalk<true> : k_adj_revwalk<false>;
+        walk<<<blocks_for(s->n, kThreads), kThreads, grouping_smem(kThreads, kBandKeys), s->stream>>>(
+            s->D, fl_scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt,
+            s->upbits, revlist, revcnt);
+        FL_LAUNCH_CHECK("adj_revwalk");
+    } else {
+        FL_CUDA_TRY(cudaMemsetAsync(revcnt, 0, 4 * (size_t)s->n, s->stream));
+        auto scatter = pr ? k_adj_revscatter<true> : k_adj_revscatter<false>;
+        scatter<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(
+            s->D, fl_scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt,
+            s->upbits, s->hitlist, s->hitcnt, revlist, revcnt);
+        FL_LAUNCH_CHECK("adj_revscatter");
+        k_adj_revsort<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(s->n, s->D.hcap, revlist, revcnt,
+                                                                              revlong, revlong_count);
+        FL_LAUNCH_CHECK("adj_revsort");
+        auto listed = pr ? k_adj_revwalk_listed<true> : k_adj_revwalk_listed<false>;
+        listed<<<crowd_grid(s), kThreads, 0, s->stream>>>(
+            s->D, fl_scene_tab(s), s->f[F_POS].cur<float4>(), s->f[F_GCELL].cur<uint32_t>(), s->off, s->cnt,
+            s->upbits, revlong, revlong_count, revlist, revcnt);
+        FL_LAUNCH_CHECK("adj_revwalk_listed");
+    }
     auto kern = pr ? k_adj_force<true> : k_adj_force<false>;
     kern<<<blocks_for(s->n, kAdjThreads), kAdjThreads, 0, s->stream>>>(
         s->D, fl_scene_tab(s), s->n, s->f[F_POS].cur<float4>(), s->f[F_VEVAL].cur<float4>(),
@@ -1124,7 +1302,7 @@ int fl_launch_adj_apply_exponent(fl_system *s, float4 *gx, float4 *gv, float4 *g
 int fl_launch_adj_rescale(fl_system *s, float4 *gx, float4 *gv, float4 *ge, uint32_t *gmax, int *gexp) {
     if (s->n == 0) return FL_OK;
     const uint16_t *ps = s->batched ? s->point_scene : nullptr;
-    k_adj_gmax<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(s->n, ps, gx, gv, ge, gmax);
+    k_adj_gmax<<<blocks_for(s->n, kGmaxPoints), kGmaxThreads, 0, s->stream>>>(s->n, ps, gx, gv, ge, gmax);
     FL_LAUNCH_CHECK("adj_gmax");
     k_adj_rescale<<<blocks_for(s->n, kThreads), kThreads, 0, s->stream>>>(s->n, ps, gx, gv, ge, gmax);
     FL_LAUNCH_CHECK("adj_rescale");

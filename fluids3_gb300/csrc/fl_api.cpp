@@ -1269,6 +1269,15 @@ extern "C" int fl_set_neighbour_passes(fl_system *s, int mode) {
     return FL_OK;
 }
 
+extern "C" int fl_set_reverse_lists(fl_system *s, int mode) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_set_reverse_lists: null system");
+    if (mode != FL_REVERSE_AUTO && mode != FL_REVERSE_WALK && mode != FL_REVERSE_TRANSPOSE)
+        return fl_fail(FL_ERR_ARG, "fl_set_reverse_lists: mode %d is none of %d, %d, %d", mode, FL_REVERSE_AUTO,
+                       FL_REVERSE_WALK, FL_REVERSE_TRANSPOSE);
+    s->adj_revmode = mode;
+    return FL_OK;
+}
+
 extern "C" int fl_neighbour_passes(const fl_system *s) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_neighbour_passes: null system");
     return s->passes;

@@ -134,6 +134,7 @@ struct fl_system {
     size_t task_cap;
     uint32_t *task_counters;
     int passes;            // FL_PASSES_*: the neighbour passes of the fused step
+    int adj_revmode;       // FL_REVERSE_*: how the adjoint finds its reverse pair lists
     int cells_grid[2];     // blocks of the cell-task density and force passes (all resident)
 
     uint32_t *hitlist;     // ceil(N/32) * hcap * 32 entries
@@ -235,10 +236,12 @@ int fl_launch_adj_advance(fl_system *s, const float *time_ptr, const float4 *for
                           const float4 *vo_b, const float4 *eo_b, float4 *xa, float4 *ea, float4 *fb, float4 *v_out,
                           float2 *rr);
 // crowd / crowd_count: the list of points whose pair lists overflowed
-// (capacity n; the count starts at zero)
+// (capacity n; the count starts at zero); revlong / revlong_count: the
+// points whose transposed reverse lists are walked again (capacity n; the
+// count starts at zero)
 int fl_launch_adj_force(fl_system *s, const float2 *rr, const float4 *fb, float4 *xa, const float4 *ea, float *rb,
                         float4 *pc, float4 *e_out, uint32_t *revlist, uint32_t *revcnt, uint32_t *crowd,
-                        uint32_t *crowd_count);
+                        uint32_t *crowd_count, uint32_t *revlong, uint32_t *revlong_count);
 int fl_launch_adj_density(fl_system *s, const uint32_t *revlist, const uint32_t *revcnt, const float *rb,
                           const float4 *xa, float4 *x_out, uint32_t *crowd, uint32_t *crowd_count);
 int fl_param_chunks(int max_scene_points);

@@ -39,8 +39,9 @@ struct fl_tape {
     float4 *xa, *ea, *fb, *pc;
     float *rb;
     float2 *rr;                   // per slot: density and its reciprocal
-    uint32_t *revlist, *revcnt;   // reverse pairs found by the reverse walk, for both pair adjoints
+    uint32_t *revlist, *revcnt;   // reverse pairs (transposed pair lists), for both pair adjoints
     uint32_t *crowd, *crowd_count; // points whose pair lists overflowed (count cleared per reverse step)
+    uint32_t *revlong;             // points whose reverse lists are walked (count: crowd_count[1])
     int nchunks;
     double *partial, *acc;  // per-scene parameter gradients (visc, rest density, IntStiff)
     uint32_t *gmax;         // per scene: largest cotangent component of the last reverse step (float bits)
@@ -67,7 +68,7 @@ static void tape_release(fl_tape *t) {
     }
     cudaFree(t->xa); cudaFree(t->ea); cudaFree(t->fb); cudaFree(t->pc); cudaFree(t->rb);
     cudaFree(t->revlist); cudaFree(t->revcnt); cudaFree(t->rr);
-    cudaFree(t->crowd); cudaFree(t->crowd_count);
+    cudaFree(t->crowd); cudaFree(t->crowd_count); cudaFree(t->revlong);
     cudaFree(t->partial); cudaFree(t->acc); cudaFree(t->sbase); cudaFree(t->sn);
     cudaFree(t->gmax); cudaFree(t->gexp);
     for (int k = 0; k < F_COUNT; k++) cudaFree(t->save[k]);
@@ -169,6 +170,7 @@ extern "C" int fl_tape_begin_ex(fl_system *s, int max_steps, int every, int flag
         if ((r = fl_dalloc((void **)&t->rb, 4 * cap)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&t->revcnt, 4 * cap)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&t->crowd, 4 * cap)) != FL_OK) break;
+        if ((r = fl_dalloc((void **)&t->revlong, 4 * cap)) != FL_OK) break;
         if ((r = fl_dalloc((void **)&t->crowd_count, 256)) != FL_OK) break;
         if (cudaMemsetAsync(t->crowd_count, 0, 256, s->stream) != cudaSuccess) {
             r = fl_fail(FL_ERR_CUDA, "tape: memset failed");
@@ -313,11 +315,11 @@ static int backward_step(fl_system *s, fl_tape *t, const float4 *state, const fl
     }
     const int c = t->gcur, x = c ^ 1;
     const int r = [&]() {
-        FL_CUDA_TRY(cudaMemsetAsync(t->crowd_count, 0, sizeof(uint32_t), s->stream));
+        FL_CUDA_TRY(cudaMemsetAsync(t->crowd_count, 0, 2 * sizeof(uint32_t), s->stream));
         FL_TRY(fl_launch_adj_advance(s, t->time + k, force, t->g[c][0], t->g[c][1], t->g[c][2], t->xa, t->ea,
                                      t->fb, t->g[x][1], t->rr));
         FL_TRY(fl_launch_adj_force(s, t->rr, t->fb, t->xa, t->ea, t->rb, t->pc, t->g[x][2], t->revlist,
-                                   t->revcnt, t->crowd, t->crowd_count));
+                                   t->revcnt, t->crowd, t->crowd_count, t->revlong, t->crowd_count + 1));
         FL_TRY(fl_launch_adj_density(s, t->revlist, t->revcnt, t->rb, t->xa, t->g[x][0], t->crowd,
                                      t->crowd_count));
         FL_TRY(fl_launch_param_reduce(s, t->pc, t->sbase, t->sn, t->nchunks, t->partial, t->gexp, t->acc));

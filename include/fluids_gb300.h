@@ -479,6 +479,19 @@ int fl_test_scan_timeout(fl_system *s, int spin_limit);
 int fl_test_scan_noalloc_timeout(const uint32_t *d_counts, uint32_t *d_offsets, int n, uint32_t *d_status,
                                  int spin_limit, void *stream);
 
+/* How fl_backward finds each point's reverse pairs (no counterpart in the
+ * reference): FL_REVERSE_WALK walks the point's reverse block (one launch);
+ * FL_REVERSE_TRANSPOSE transposes the density pass's pair lists (atomics,
+ * then a per-list sort: less work, more launches); FL_REVERSE_AUTO (the
+ * default) transposes from FL_REVERSE_TRANSPOSE_MIN points (all scenes of
+ * a batch together) and walks below. All give the same lists, so the same
+ * gradients bit for bit. */
+#define FL_REVERSE_AUTO      0
+#define FL_REVERSE_WALK      1
+#define FL_REVERSE_TRANSPOSE 2
+#define FL_REVERSE_TRANSPOSE_MIN (1 << 20)
+int fl_set_reverse_lists(fl_system *s, int mode);
+
 /* The CUDA stream (cudaStream_t) the system issues its work on. */
 void *fl_stream(fl_system *s);
 

@@ -317,3 +317,70 @@ def test_long_rollout_gradient_stays_finite_and_matches_fp64():
     for k in range(3):
         assert abs(gp[0, k] - want[3][k]) <= 1e-3 * abs(want[3][k]), ("param", k, gp[0, k], want[3][k])
     print(f"\n300-step gradient: exponent {int(ex[0])}, relative errors {errs}")
+
+
+def _reverse_lists_both_ways(make, w, every=2):
+    """Gradients with the reverse lists transposed from the pair lists and
+    walked (fl_set_reverse_lists), from the same recording."""
+    out = []
+    for mode in (2, 1):   # FL_REVERSE_TRANSPOSE, FL_REVERSE_WALK
+        with make() as s:
+            s.RunSteps(5)
+            _lib.check("fl_set_reverse_lists", _lib.lib().fl_set_reverse_lists(s.handle, mode))
+            s.TapeBegin(4, every)
+            s.RunSteps(4)
+            out.append(s.Backward(*w))
+    return out
+
+
+@pytest.mark.parametrize("case", ["wave", "crowd", "keep_lists", "srch3", "batch"])
+def test_reverse_lists_transposed_equal_walked(case):
+    """The reverse pair lists are the density pass's pair lists transposed
+    and sorted into ascending slot order; the walk of each point's reverse
+    block finds the same lists, so every gradient is bit-identical: on the
+    wave tank, with a crowd whose lists overflow (owners walk their blocks
+    again, reverse counts clamp to the overflow mark), with kept lists, with
+    a wider (unpruned) search block, and in a batch."""
+    rng = np.random.default_rng(61)
+    if case == "batch":
+        scs = scenes.batch_scenes(nscenes=3, nmin=1500, nmax=4000, seed=62)
+        c = scs[1].pos[scs[1].n // 2].copy()
+        scs[1].pos[:400] = c + rng.uniform(-0.5, 0.5, (400, 3)).astype(np.float32)
+        cat = scenes.concat(scs)
+
+        def make():
+            b = F.FluidSystem.batch([sc.params for sc in scs], [sc.n for sc in scs])
+            b.SetParticles(cat["pos"], cat["vel"], cat["veval"], clr=cat["clr"])
+            return b
+        n = cat["pos"].shape[0]
+    else:
+        sc = scenes.wave_tank(n=8000) if case != "srch3" else scenes.dam_break(n=3000)
+        p = sc.params
+        if case == "srch3":
+            p = scenes.make_params((-30.0, 0.0, -30.0), (30.0, 60.0, 30.0), grid_density=2.0)
+            assert p.gridSrch == 3
+        pos = sc.pos.copy()
+        if case == "crowd":
+            pos[:1500] = pos[2000] + rng.uniform(-0.6, 0.6, (1500, 3)).astype(np.float32)
+
+        def make():
+            s = F.FluidSystem(p, sc.n)
+            s.SetParticles(pos, sc.vel, sc.veval, clr=sc.clr)
+            return s
+        n = sc.n
+    w = rng.standard_normal((3, n, 3)).astype(np.float32)
+    if case == "keep_lists":
+        out = []
+        for mode in (2, 1):   # FL_REVERSE_TRANSPOSE, FL_REVERSE_WALK
+            with make() as s:
+                s.RunSteps(5)
+                _lib.check("fl_set_reverse_lists", _lib.lib().fl_set_reverse_lists(s.handle, mode))
+                s.TapeBegin(4, 2, True)
+                s.RunSteps(4)
+                out.append(s.Backward(*w))
+    else:
+        out = _reverse_lists_both_ways(make, w)
+    for j in range(3):
+        assert np.isfinite(out[0][j]).all()
+        assert_bit_equal(out[0][j], out[1][j], f"{case}: state gradient {j}")
+    assert np.array_equal(out[0][3], out[1][3]), f"{case}: parameter gradients"
