@@ -102,6 +102,9 @@ def parse():
     ap.add_argument("--profile", action="store_true",
                     help="profiling run for ncu: the wave tank of --n points, --warmup eager steps, then "
                          "--steps eager steps (one launch per kernel per step), no timing, no JSON line")
+    ap.add_argument("--profile-tape", type=int, default=0,
+                    help="with --profile: then record this many steps on a tape (checkpoints every "
+                         "--adjoint-every) and run one reverse pass")
     ap.add_argument("--passes", choices=["cells", "points", "pairs"], default="points",
                     help="neighbour passes of the fused step (bit-identical results)")
     ap.add_argument("--fit-iters", type=int, default=40,
@@ -919,8 +922,18 @@ def profile_run(args):
         for _ in range(args.warmup + args.steps):
             s.Run()
         s.Sync()
-        print(f"profile run: {scene.n:,} points, {args.warmup} + {args.steps} eager steps ({args.passes} passes), "
-              f"device status {s.DeviceStatus()}", flush=True)
+        tape = ""
+        if args.profile_tape > 0:   # then one reverse pass over a recorded rollout
+            T = args.profile_tape
+            every = max(1, min(args.adjoint_every, T))
+            s.TapeBegin(T, every)
+            s.RunSteps(T)
+            w = np.random.default_rng(1).standard_normal((scene.n, 3)).astype(np.float32)
+            s.Backward(w)
+            s.Sync()
+            tape = f", then a {T}-step tape (checkpoints every {every}) and one fl_backward"
+        print(f"profile run: {scene.n:,} points, {args.warmup} + {args.steps} eager steps ({args.passes} passes)"
+              f"{tape}, device status {s.DeviceStatus()}", flush=True)
 
 
 def main():

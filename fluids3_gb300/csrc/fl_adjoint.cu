@@ -538,6 +538,8 @@ k_adj_revwalk_listed(const __grid_constant__ DevParams P0, const SceneTab T, con
 // ascending index, each in ascending slot), so consumers see the same
 // lists. An owner whose own list overflowed walks its search block again.
 // revcnt must be zero before the launch.
+constexpr uint32_t kScatterBatch = 4;
+
 template <bool PRUNE>
 __global__ void __launch_bounds__(kThreads)
 k_adj_revscatter(const __grid_constant__ DevParams P0, const SceneTab T, int n, const float4 *__restrict__ pos,
@@ -558,7 +560,23 @@ k_adj_revscatter(const __grid_constant__ DevParams P0, const SceneTab T, int n, 
     };
     const uint32_t nh = hitcnt[q];
     if (nh <= hcap) {
-        for (uint32_t t = 0; t < nh; t++) push(hitlist[list_at(P, q, t)]);
+        // four entries per round: their list words, cells and count atomics
+        // are each requested before the first is waited for
+        for (uint32_t t = 0; t < nh; t += kScatterBatch) {
+            uint32_t sj[kScatterBatch], at[kScatterBatch];
+#pragma unroll
+            for (uint32_t k = 0; k < kScatterBatch; k++)
+                sj[k] = (t + k < nh) ? hitlist[list_at(P, q, t + k)] : kUndef;
+#pragma unroll
+            for (uint32_t k = 0; k < kScatterBatch; k++)
+                at[k] = (sj[k] != kUndef && gcell[sj[k]] != gq) ? 0u : hcap;
+#pragma unroll
+            for (uint32_t k = 0; k < kScatterBatch; k++)
+                if (at[k] == 0u) at[k] = atomicAdd(&revcnt[sj[k]], 1u);
+#pragma unroll
+            for (uint32_t k = 0; k < kScatterBatch; k++)
+                if (at[k] < hcap) revlist[list_at(P, (int)sj[k], at[k])] = (uint32_t)q;
+        }
         return;
     }
     const float4 p = pos[q];
