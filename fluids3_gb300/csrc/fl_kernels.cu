@@ -596,13 +596,19 @@ __device__ __forceinline__ float3 force_of(const DevParams &P, int i, bool activ
         const uint32_t nh = active ? hitcnt[i] : 0u;
         const bool over = nh > (uint32_t)P.hcap;
         if (!__any_sync(0xffffffffu, over)) {
-            // Four pairs in flight: their list entries and records are all
-            // requested before the first of them is evaluated, so the drain
-            // (bound by these dependent loads, not by arithmetic) waits one
-            // round trip per four pairs; each point still adds its pairs in
-            // list order.
+            // Four pairs in flight: their records are all requested before
+            // the first of them is evaluated, and the next four list entries
+            // while they are, so the drain (bound by these dependent loads,
+            // not by arithmetic) waits one round trip per four pairs. Each
+            // point still adds its pairs in list order; a lane past its
+            // list's end adds +0.0, which leaves a force sum's bits unchanged
+            // (a sum that starts at +0.0 never becomes -0.0), so the adds
+            // need no branch.
             const uint32_t most = __reduce_max_sync(0xffffffffu, nh);
             uint32_t t = 0;
+            uint32_t jn[kPairsInFlight];
+#pragma unroll
+            for (uint32_t k = 0; k < kPairsInFlight; k++) jn[k] = (k < nh) ? hitlist[list_at(P, i, k)] : 0u;
             for (; t + kPairsInFlight <= most; t += kPairsInFlight) {
                 float4 q[kPairsInFlight], v[kPairsInFlight];
 #pragma unroll
@@ -610,14 +616,23 @@ __device__ __forceinline__ float3 force_of(const DevParams &P, int i, bool activ
                     q[k] = make_float4(0.f, 0.f, 0.f, 1.f);
                     v[k] = q[k];
                     if (t + k < nh) {
-                        const uint32_t j = hitlist[list_at(P, i, t + k)];
-                        q[k] = pairdata[2 * (size_t)j];
-                        v[k] = pairdata[2 * (size_t)j + 1];
+                        q[k] = pairdata[2 * (size_t)jn[k]];
+                        v[k] = pairdata[2 * (size_t)jn[k] + 1];
                     }
                 }
 #pragma unroll
-                for (uint32_t k = 0; k < kPairsInFlight; k++)
-                    if (t + k < nh) add_pair_terms(P, fp, q[k], v[k], q[k].w);
+                for (uint32_t k = 0; k < kPairsInFlight; k++) {
+                    const uint32_t tn = t + kPairsInFlight + k;
+                    jn[k] = (tn < nh) ? hitlist[list_at(P, i, tn)] : 0u;
+                }
+#pragma unroll
+                for (uint32_t k = 0; k < kPairsInFlight; k++) {
+                    const float3 tk = pair_term(P, fp.p, fp.pi, fp.vi, fp.di, q[k], v[k], q[k].w);
+                    const bool ok = t + k < nh;
+                    fp.f.x += ok ? tk.x : 0.0f;
+                    fp.f.y += ok ? tk.y : 0.0f;
+                    fp.f.z += ok ? tk.z : 0.0f;
+                }
             }
             for (; t < most; t++)
                 if (t < nh) add_pair_force_rec(P, fp, hitlist[list_at(P, i, t)], pairdata);
