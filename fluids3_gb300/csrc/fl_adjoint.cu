@@ -787,8 +787,18 @@ k_adj_density(const __grid_constant__ DevParams P0, const SceneTab T, int n,
         if (j >= c_lo && j < c_hi) rev(j);
     };
     const uint32_t nh = hitcnt[s];
+    // the lists are read four entries per round, all requested before the
+    // first is used (the pairs still add in list order)
     if (nh <= (uint32_t)P.hcap) {
-        for (uint32_t t = 0; t < nh; t++) both(hitlist[list_at(P, s, t)]);
+        uint32_t t = 0;
+        for (; t + 4 <= nh; t += 4) {
+            uint32_t j[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) j[k] = hitlist[list_at(P, s, t + k)];
+#pragma unroll
+            for (int k = 0; k < 4; k++) both(j[k]);
+        }
+        for (; t < nh; t++) both(hitlist[list_at(P, s, t)]);
     } else if (walk_overflow) {
         const int base = (int)gc - P.nadj;
         for (int c = 0; c < P.gridAdjCnt; c++) {
@@ -805,7 +815,15 @@ k_adj_density(const __grid_constant__ DevParams P0, const SceneTab T, int n,
     // reverse pairs in the other cells: the force adjoint's list, or a walk
     const uint32_t nr = revcnt[s];
     if (nr <= (uint32_t)P.hcap) {
-        for (uint32_t t = 0; t < nr; t++) rev(revlist[list_at(P, s, t)]);
+        uint32_t t = 0;
+        for (; t + 4 <= nr; t += 4) {
+            uint32_t o[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) o[k] = revlist[list_at(P, s, t + k)];
+#pragma unroll
+            for (int k = 0; k < 4; k++) rev(o[k]);
+        }
+        for (; t < nr; t++) rev(revlist[list_at(P, s, t)]);
     } else if (walk_overflow) {
         const uint32_t *lobits = upbits + 3 * (size_t)P.upwords;
         RevIter it;

@@ -171,8 +171,6 @@ static void free_all(fl_system *s) {
         if (s->ev[k]) cudaEventDestroy(s->ev[k]);
     if (s->ev_early) cudaEventDestroy(s->ev_early);
     if (s->ev_late) cudaEventDestroy(s->ev_late);
-    for (int k = 0; k < 4; k++)
-        if (s->ev_chunk[k]) cudaEventDestroy(s->ev_chunk[k]);
     if (s->side) cudaStreamDestroy(s->side);
     if (s->stream) cudaStreamDestroy(s->stream);
 }
@@ -972,27 +970,10 @@ static int run_step_late(fl_system *s, const float *vel3, const float *veval3, c
         // the force pass also writes the new positions into the caller's
         // page-locked array as it goes (no separate readback)
         FL_TRY(fl_launch_force_cells(s, s->P.dt, pos_out ? (float *)mapped_device_ptr(pos_out) : nullptr));
-    } else if (!pos_out) {
-        FL_TRY(fl_launch_force_advance(s, s->P.dt));
     } else {
-        // the force pass in up to four slot ranges of whole blocks; as each
-        // ends, the side stream packs its new positions and a copy engine
-        // takes them to pos_out while the next range computes
-        const int bs = fl_force_block(s);
-        const int nblk = (s->n + bs - 1) / bs;
-        const int chunks = std::max(1, std::min(4, s->n / (1 << 20)));
-        const float4 *pnew = s->f[F_POS].nxt<float4>();
-        float *stage = (float *)s->stage;
-        for (int c = 0; c < chunks; c++) {
-            const int b = (int)((long long)nblk * c / chunks) * bs;
-            const int e = (c + 1 == chunks) ? s->n : (int)((long long)nblk * (c + 1) / chunks) * bs;
-            FL_TRY(fl_launch_force_advance(s, s->P.dt, b, e));
-            FL_CUDA_TRY(cudaEventRecord(s->ev_chunk[c], s->stream));
-            FL_CUDA_TRY(cudaStreamWaitEvent(s->side, s->ev_chunk[c], 0));
-            FL_TRY(fl_launch_pack3(s, pnew + b, stage + 3 * (size_t)b, e - b, s->side));
-            FL_CUDA_TRY(cudaMemcpyAsync(pos_out + 3 * (size_t)b, stage + 3 * (size_t)b, 12 * (size_t)(e - b),
-                                        cudaMemcpyDeviceToHost, s->side));
-        }
+        // the force pass writes the new positions into the caller's
+        // page-locked array as it goes (no separate readback)
+        FL_TRY(fl_launch_force_advance(s, s->P.dt, 0, -1, pos_out ? (float *)mapped_device_ptr(pos_out) : nullptr));
     }
     flip(s, F_POS); flip(s, F_VEVAL);
     s->codes_valid = 0;
@@ -1002,17 +983,9 @@ static int run_step_late(fl_system *s, const float *vel3, const float *veval3, c
 }
 
 static int ensure_side(fl_system *s) {
-    if (!s->side) {
-        // the highest priority, so the readback's pack kernels take SMs as the
-        // running force blocks retire instead of queueing behind the next range
-        int least = 0, greatest = 0;
-        FL_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-        FL_CUDA_TRY(cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, greatest));
-    }
+    if (!s->side) FL_CUDA_TRY(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));   // the input copies
     if (!s->ev_early) FL_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_early, cudaEventDisableTiming));
     if (!s->ev_late) FL_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_late, cudaEventDisableTiming));
-    for (int k = 0; k < 4; k++)
-        if (!s->ev_chunk[k]) FL_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_chunk[k], cudaEventDisableTiming));
     return FL_OK;
 }
 
@@ -1021,7 +994,8 @@ static int ensure_side(fl_system *s) {
 // in page-locked memory, the positions are read over the host link first;
 // velocities, evaluated velocities and colours, first needed by the force
 // pass, follow on a copy engine (side stream) while insert, sort and density
-// run, and k_gather_late puts them in sorted order. Results equal
+// run, and k_gather_late puts them in sorted order; the force pass writes
+// the new positions into pos_out itself as it computes them. Results equal
 // fl_set_particles followed by fl_run, bit for bit; other host memory, a
 // batched system, a recording tape or phase timing take that path.
 extern "C" int fl_run_from_host(fl_system *s, int n, const float *pos, const float *vel, const float *veval,
@@ -1067,7 +1041,7 @@ extern "C" int fl_run_from_host(fl_system *s, int n, const float *pos, const flo
     FL_TRY(begin_run(s));
     const int r = run_step_late(s, stage_vel, stage_vev, stage_clr, pos_out);
     // the host arrays are the caller's again once the step (and the
-    // readback on the side stream) is done
+    // input copies on the side stream) are done
     cudaError_t e = cudaStreamSynchronize(s->stream);
     const cudaError_t e2 = cudaStreamSynchronize(s->side);
     if (e == cudaSuccess) e = e2;

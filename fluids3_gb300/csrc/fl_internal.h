@@ -185,7 +185,6 @@ struct fl_system {
     // (created on first use)
     cudaStream_t side;
     cudaEvent_t ev_early, ev_late;
-    cudaEvent_t ev_chunk[4];   // force-pass chunks whose positions go back while the next computes
 
     // per-phase event timing (PERF_PUSH/PERF_POP of Run, cpp:507-515)
     int timing;
@@ -280,7 +279,7 @@ int fl_launch_density(fl_system *s);
 int fl_launch_force(fl_system *s);
 // slots [begin, end) (end < 0: n); both whole blocks of fl_force_block(s)
 // threads, except end == n
-int fl_launch_force_advance(fl_system *s, float dt, int begin = 0, int end = -1);
+int fl_launch_force_advance(fl_system *s, float dt, int begin = 0, int end = -1, float *host_pos = nullptr);
 int fl_force_block(const fl_system *s);
 int fl_launch_advance(fl_system *s, float time, float dt, float ss);
 int fl_launch_pack3(fl_system *s, const float4 *src, float *dst, int n, cudaStream_t stream = nullptr);

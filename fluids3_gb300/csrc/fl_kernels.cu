@@ -736,7 +736,10 @@ k_force_advance(const __grid_constant__ DevParams P0, const SceneTab T, int n, f
                 const uint32_t *__restrict__ hitlist, const uint32_t *__restrict__ hitcnt,
                 const float4 *__restrict__ pairdata, float4 *__restrict__ vel, float4 *__restrict__ force,
                 float4 *__restrict__ pos_out, float4 *__restrict__ veval_out,
-                uint32_t *__restrict__ err, int base) {
+                uint32_t *__restrict__ err, int base, float *__restrict__ host_pos) {
+    // host_pos (fl_run_from_host): the new positions also go straight into
+    // the caller's page-locked float3 array, in slot order, while the pass
+    // runs (each warp's 384 contiguous bytes over the host link)
     const int i = base + blockIdx.x * blockDim.x + threadIdx.x;   // base: a whole number of blocks
     const float time = time_dev[slot];
     if (i == 0) time_dev[slot ^ 1] = time + dt;
@@ -751,6 +754,11 @@ k_force_advance(const __grid_constant__ DevParams P0, const SceneTab T, int n, f
         pos_out[i] = make_float4(-1000.f, -1000.f, -1000.f, 0.f);
         vel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         veval_out[i] = veval_in[i];
+        if (host_pos) {
+            host_pos[3 * (size_t)i] = -1000.f;
+            host_pos[3 * (size_t)i + 1] = -1000.f;
+            host_pos[3 * (size_t)i + 2] = -1000.f;
+        }
         return;
     }
     force[i] = f4(f);
@@ -760,6 +768,11 @@ k_force_advance(const __grid_constant__ DevParams P0, const SceneTab T, int n, f
     pos_out[i] = f4(po);
     vel[i] = f4(vo);
     veval_out[i] = f4(eo);
+    if (host_pos) {
+        host_pos[3 * (size_t)i] = po.x;
+        host_pos[3 * (size_t)i + 1] = po.y;
+        host_pos[3 * (size_t)i + 2] = po.z;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1096,7 +1109,7 @@ int fl_launch_force(fl_system *s) {
 
 int fl_force_block(const fl_system *s) { return s->blk_force ? s->blk_force : kForceThreads; }
 
-int fl_launch_force_advance(fl_system *s, float dt, int begin, int end) {
+int fl_launch_force_advance(fl_system *s, float dt, int begin, int end, float *host_pos) {
     const bool pr = use_prune(s);
     auto kern = s->lists_valid
                     ? (s->batched ? force_advance_kernel<true, true>(pr) : force_advance_kernel<true, false>(pr))
@@ -1111,7 +1124,7 @@ int fl_launch_force_advance(fl_system *s, float dt, int begin, int end) {
         s->f[F_VEVAL].cur<float4>(), s->f[F_PRESS].cur<float>(), s->f[F_GCELL].cur<uint32_t>(), s->off,
         s->cnt, s->upbits, s->hitlist, s->hitcnt, s->pairdata,
         s->f[F_VEL].cur<float4>(), s->f[F_FORCE].cur<float4>(),
-        s->f[F_POS].nxt<float4>(), s->f[F_VEVAL].nxt<float4>(), s->dev_err, begin);
+        s->f[F_POS].nxt<float4>(), s->f[F_VEVAL].nxt<float4>(), s->dev_err, begin, host_pos);
     FL_LAUNCH_CHECK("force_advance");
     return FL_OK;
 }

@@ -208,8 +208,8 @@ int fl_add_particles(fl_system *s, int k, const float *pos, const float *vel, co
  * bit for bit. With every given array in page-locked memory (fl_host_alloc)
  * on a single-scene system, the positions are read over the host link
  * first, velocities, evaluated velocities and colours follow on a copy
- * engine while the insert, sort and density kernels run, and the new
- * positions go back in slot ranges while the force pass computes the next. */
+ * engine while the insert, sort and density kernels run, and the force
+ * pass writes the new positions into pos_out as it computes them. */
 int fl_run_from_host(fl_system *s, int n, const float *pos, const float *vel, const float *veval,
                      const uint32_t *clr, float *pos_out);
 

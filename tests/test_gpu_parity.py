@@ -710,11 +710,11 @@ def test_run_from_host_equals_set_particles_then_run(case):
 
 
 @pytest.mark.parametrize("passes", ["points", "cells", "pairs"])
-def test_run_from_host_reads_back_in_slot_ranges(passes):
-    """Above 2^21 points the force pass of fl_run_from_host runs in slot
-    ranges whose positions go back while the next range computes (after
-    any density pass): the positions read back and the state still equal
-    SetParticles + Run + GetBuffer."""
+def test_run_from_host_writes_positions_back_at_2m(passes):
+    """At 2.2M points fl_run_from_host's force pass writes the new
+    positions into the caller's page-locked array as it computes them
+    (after any density pass): the positions read back and the state still
+    equal SetParticles + Run + GetBuffer."""
     sc = scenes.wave_tank(n=2_200_000)
     n = sc.n
     pins = {k: F.PinnedArray((n, 3), np.float32) for k in ("pos", "vel", "veval", "out")}
