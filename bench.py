@@ -93,9 +93,8 @@ def parse():
                     help="skip timing the reference's own GPU kernels on the same workload")
     ap.add_argument("--batch-scenes", type=int, default=256,
                     help="scenes in the batched-vs-one-at-a-time comparison (0 skips it)")
-    ap.add_argument("--batch-passes", choices=["cells", "points", "pairs"], default="cells",
-                    help="neighbour passes of both arms of the batched comparison (default: the cell tasks, "
-                         "faster than the per-point passes once this batch's scenes clump)")
+    ap.add_argument("--batch-passes", choices=["cells", "points", "pairs", "auto"], default="auto",
+                    help="neighbour passes of both arms of the batched comparison")
     ap.add_argument("--batch-steps", type=int, default=500,
                     help="continuous steps of the batched comparison")
     ap.add_argument("--adjoint-steps", type=int, default=200,
@@ -108,7 +107,7 @@ def parse():
     ap.add_argument("--profile-tape", type=int, default=0,
                     help="with --profile: then record this many steps on a tape (checkpoints every "
                          "--adjoint-every) and run one reverse pass")
-    ap.add_argument("--passes", choices=["cells", "points", "pairs"], default="points",
+    ap.add_argument("--passes", choices=["cells", "points", "pairs", "auto"], default="auto",
                     help="neighbour passes of the fused step (bit-identical results)")
     ap.add_argument("--fit-iters", type=int, default=40,
                     help="iterations of the 64-scene batched parameter fit (0 skips it)")

@@ -133,6 +133,7 @@ static int alloc_grid(fl_system *s) {
     s->cnt = (uint32_t *)blk;
     s->scan_ticket = (uint32_t *)((char *)blk + s->grid_pad * sizeof(uint32_t));
     s->task_counters = s->scan_ticket + 1;   // same 256-byte slot as the ticket
+    s->crowd_dev = s->scan_ticket + 4;       // cleared with it every step
     s->scan_status = (uint64_t *)((char *)s->scan_ticket + 256);
     s->off = (uint32_t *)off;
     s->scan_epoch = 1;
@@ -142,6 +143,9 @@ static int alloc_grid(fl_system *s) {
     return FL_OK;
 }
 
+static int ensure_side(fl_system *s);
+static int reset_auto(fl_system *s);
+
 static void destroy_graph(fl_system *s) {
     if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
     s->graph_exec = nullptr;
@@ -150,6 +154,7 @@ static void destroy_graph(fl_system *s) {
 
 static void free_all(fl_system *s) {
     destroy_graph(s);
+    if (s->crowd_host) cudaFreeHost(s->crowd_host);
     fl_tape_free(s);
     for (int k = 0; k < F_COUNT; k++)
         for (int c = 0; c < 2; c++) cudaFree(s->f[k].p[c]);
@@ -171,6 +176,9 @@ static void free_all(fl_system *s) {
         if (s->ev[k]) cudaEventDestroy(s->ev[k]);
     if (s->ev_early) cudaEventDestroy(s->ev_early);
     if (s->ev_late) cudaEventDestroy(s->ev_late);
+    if (s->ev_crowd) cudaEventDestroy(s->ev_crowd);
+    if (s->ev_crowd_done) cudaEventDestroy(s->ev_crowd_done);
+    cudaFree(s->crowd_epoch);
     if (s->side) cudaStreamDestroy(s->side);
     if (s->stream) cudaStreamDestroy(s->stream);
 }
@@ -188,7 +196,7 @@ extern "C" int fl_create(const fl_params *p, int max_points, fl_system **out) {
     FL_TRY(check_derived(p));
     fl_system *s = (fl_system *)calloc(1, sizeof(fl_system));
     if (!s) return fl_fail(FL_ERR_NOMEM, "fl_create: host allocation failed");
-    s->passes = FL_PASSES_PER_POINT;   // the faster step (fl_set_neighbour_passes)
+    s->passes = FL_PASSES_AUTO;   // per-point passes, cell tasks once cells crowd (fl_set_neighbour_passes)
     int r = FL_OK;
     do {
         if (cudaGetDevice(&s->device) != cudaSuccess) {
@@ -199,6 +207,18 @@ extern "C" int fl_create(const fl_params *p, int max_points, fl_system **out) {
             r = fl_fail(FL_ERR_CUDA, "fl_create: cudaStreamCreate failed");
             break;
         }
+        if (cudaHostAlloc((void **)&s->crowd_host, 64, cudaHostAllocDefault) != cudaSuccess) {
+            s->crowd_host = nullptr;
+            r = fl_fail(FL_ERR_NOMEM, "fl_create: page-locked allocation failed");
+            break;
+        }
+        s->crowd_host[0] = s->crowd_host[1] = 0;
+        if ((r = fl_dalloc((void **)&s->crowd_epoch, 256)) != FL_OK) break;
+        if (cudaMemset(s->crowd_epoch, 0, 256) != cudaSuccess) {
+            r = fl_fail(FL_ERR_CUDA, "fl_create: memset failed");
+            break;
+        }
+        if ((r = ensure_side(s)) != FL_OK) break;
         s->P = *p;
         fl_make_dev_params(*p, &s->D);
         s->max_points = max_points;
@@ -570,6 +590,7 @@ extern "C" int fl_set_particles(fl_system *s, int n, const float *pos, const flo
         return fl_fail(FL_ERR_ARG, "fl_set_particles: a batched system takes all %d points (scenes concatenated)",
                        s->max_points);
     destroy_graph(s);
+    FL_TRY(reset_auto(s));
     s->n = n;
     if (n > 0) {
         // one staging slice per float3 field, then unpack to float4 on device
@@ -854,8 +875,60 @@ static int record(fl_system *s, TimingState *t, int k) {
 // The cell-task passes (fl_cells.cu) need the pruned search (gridSrch 2 in
 // every scene) with band codes from this step's sort. A recording tape keeps
 // the per-point passes (its hooks keep each step's pair lists).
+static bool cells_selected(const fl_system *s) {
+    return s->passes == FL_PASSES_CELL_TASKS || (s->passes == FL_PASSES_AUTO && s->auto_cells);
+}
+
 static bool use_cell_passes(const fl_system *s, bool taped) {
-    return s->passes == FL_PASSES_CELL_TASKS && s->D.prune && s->codes_valid && !taped && s->n > 0;
+    return cells_selected(s) && s->D.prune && s->codes_valid && !taped && s->n > 0;
+}
+
+// FL_PASSES_AUTO: measured on GB300 (4M-point wave tank, 10-step runs as it
+// clumps), the cell tasks overtake the per-point passes once the largest
+// cell holds about 450-490 points (15% more time per step at 396, 4% less
+// at 489, 15-25% less from 581 to 13,144). Every step's sort records the
+// largest in-range cell above 128 points and sends it to page-locked host
+// memory; the next call reads whatever copy has arrived (a step or two
+// old, no wait) and switches with hysteresis. The passes give identical
+// results, so when the switch happens changes no result.
+constexpr uint32_t kAutoCellsOn = 512, kAutoCellsOff = 384;
+
+static void update_auto(fl_system *s) {
+    if (s->passes != FL_PASSES_AUTO || !s->crowd_host) return;
+    volatile const uint32_t *h = s->crowd_host;
+    if (h[1] != s->auto_epoch) return;   // no count of the current state has arrived yet
+    const uint32_t big = h[0];
+    if (!s->auto_cells && big >= kAutoCellsOn) s->auto_cells = 1;
+    else if (s->auto_cells && big < kAutoCellsOff) s->auto_cells = 0;
+}
+
+// The state was replaced (particles set, checkpoint restored): back to the
+// per-point passes until a count of the new state arrives (the counts
+// carry the state's epoch, so an older count in flight is ignored).
+static int reset_auto(fl_system *s) {
+    s->auto_cells = 0;
+    s->auto_epoch++;
+    return fl_launch_set_word(s, s->crowd_epoch, s->auto_epoch);
+}
+
+// After the sort: the count and the epoch go to the host on the side stream,
+// off the step's critical path; join_crowd makes the step's end wait for
+// them (the next step's memset clears the count).
+static int send_crowd(fl_system *s) {
+    if (s->passes != FL_PASSES_AUTO || !s->crowd_host) return FL_OK;
+    FL_CUDA_TRY(cudaEventRecord(s->ev_crowd, s->stream));
+    FL_CUDA_TRY(cudaStreamWaitEvent(s->side, s->ev_crowd, 0));
+    FL_CUDA_TRY(cudaMemcpyAsync(s->crowd_host, s->crowd_dev, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->side));
+    FL_CUDA_TRY(cudaMemcpyAsync(s->crowd_host + 1, s->crowd_epoch, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                s->side));
+    FL_CUDA_TRY(cudaEventRecord(s->ev_crowd_done, s->side));
+    return FL_OK;
+}
+
+static int join_crowd(fl_system *s) {
+    if (s->passes != FL_PASSES_AUTO || !s->crowd_host) return FL_OK;
+    FL_CUDA_TRY(cudaStreamWaitEvent(s->stream, s->ev_crowd_done, 0));
+    return FL_OK;
 }
 
 static int run_step(fl_system *s, TimingState *t) {
@@ -873,6 +946,7 @@ static int run_step(fl_system *s, TimingState *t) {
     FL_TRY(fl_launch_scatter_index(s));
     FL_TRY(record(s, t, 3));
     FL_TRY(fl_launch_sort_cells(s, 1));
+    FL_TRY(send_crowd(s));
     flip(s, F_POS); flip(s, F_VEL); flip(s, F_VEVAL); flip(s, F_CLR); flip(s, F_GCELL); flip(s, F_GNDX);
     const bool cells = use_cell_passes(s, taped);
     if (cells) FL_TRY(fl_launch_make_tasks(s));
@@ -880,6 +954,7 @@ static int run_step(fl_system *s, TimingState *t) {
     FL_TRY(cells ? fl_launch_density_cells(s) : fl_launch_density(s));
     FL_TRY(record(s, t, 5));
     FL_TRY(cells ? fl_launch_force_cells(s, s->P.dt, nullptr) : fl_launch_force_advance(s, s->P.dt));
+    FL_TRY(join_crowd(s));
     flip(s, F_POS); flip(s, F_VEVAL);
     s->codes_valid = 0;
     s->lists_valid = 0;
@@ -939,6 +1014,7 @@ static int begin_run(fl_system *s) {
 
 extern "C" int fl_run(fl_system *s) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_run: null system");
+    update_auto(s);
     FL_TRY(begin_run(s));
     FL_TRY(run_step(s, active_timing(s)));
     if (s->time_host_valid) s->time += s->P.dt;   // AdvanceTime (cpp:529), same float add
@@ -960,6 +1036,7 @@ static int run_step_late(fl_system *s, const float *vel3, const float *veval3, c
     FL_TRY(fl_launch_scan(s, s->gcells, 0));
     FL_TRY(fl_launch_scatter_index(s));
     FL_TRY(fl_launch_sort_cells(s, 1, true));
+    FL_TRY(send_crowd(s));
     flip(s, F_POS); flip(s, F_VEL); flip(s, F_VEVAL); flip(s, F_CLR); flip(s, F_GCELL); flip(s, F_GNDX);
     const bool cells = use_cell_passes(s, false);
     if (cells) FL_TRY(fl_launch_make_tasks(s));
@@ -975,6 +1052,7 @@ static int run_step_late(fl_system *s, const float *vel3, const float *veval3, c
         // page-locked array as it goes (no separate readback)
         FL_TRY(fl_launch_force_advance(s, s->P.dt, 0, -1, pos_out ? (float *)mapped_device_ptr(pos_out) : nullptr));
     }
+    FL_TRY(join_crowd(s));
     flip(s, F_POS); flip(s, F_VEVAL);
     s->codes_valid = 0;
     s->lists_valid = 0;
@@ -986,6 +1064,8 @@ static int ensure_side(fl_system *s) {
     if (!s->side) FL_CUDA_TRY(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));   // the input copies
     if (!s->ev_early) FL_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_early, cudaEventDisableTiming));
     if (!s->ev_late) FL_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_late, cudaEventDisableTiming));
+    if (!s->ev_crowd) FL_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_crowd, cudaEventDisableTiming));
+    if (!s->ev_crowd_done) FL_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_crowd_done, cudaEventDisableTiming));
     return FL_OK;
 }
 
@@ -1016,6 +1096,7 @@ extern "C" int fl_run_from_host(fl_system *s, int n, const float *pos, const flo
         return FL_OK;
     }
     destroy_graph(s);
+    update_auto(s);
     FL_TRY(ensure_side(s));
     const size_t n3 = 12 * (size_t)n;
     FL_TRY(fl_ensure_stage(s, 2 * n3 + 4 * (size_t)n));
@@ -1077,6 +1158,7 @@ static int capture_pair(fl_system *s) {
         return fl_fail(FL_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
     }
     s->graph_steps = 2;
+    s->graph_cells = (int)cells_selected(s);
     for (int k = 0; k < F_COUNT; k++) s->graph_live[k] = live[k];
     return FL_OK;
 }
@@ -1088,9 +1170,10 @@ extern "C" int fl_run_steps(fl_system *s, int nsteps) {
         for (int k = 0; k < nsteps; k++) FL_TRY(fl_run(s));
         return FL_OK;
     }
+    update_auto(s);
     const int pairs = nsteps / 2;
     if (pairs > 0) {
-        bool match = s->graph_exec != nullptr;
+        bool match = s->graph_exec != nullptr && s->graph_cells == (int)cells_selected(s);
         for (int k = 0; k < F_COUNT && match; k++) match = s->graph_live[k] == s->f[k].live;
         if (!match) FL_TRY(capture_pair(s));
         FL_TRY(begin_run(s));
@@ -1149,6 +1232,7 @@ extern "C" int fl_checkpoint_restore(fl_system *s, int slot) {
 
 static int restore_slot(fl_system *s, int slot) {
     s->n = s->ckpt_n[slot];
+    FL_TRY(reset_auto(s));
     for (int k = 0; k < F_COUNT; k++)
         if (s->n > 0)
             FL_CUDA_TRY(cudaMemcpyAsync(s->f[k].cur<void>(), s->ckpt[slot][k], s->f[k].esz * (size_t)s->n,
@@ -1234,11 +1318,13 @@ extern "C" int fl_set_launch_shapes(fl_system *s, const int *shapes) {
 
 extern "C" int fl_set_neighbour_passes(fl_system *s, int mode) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_set_neighbour_passes: null system");
-    if (mode != FL_PASSES_PER_POINT && mode != FL_PASSES_CELL_TASKS && mode != FL_PASSES_POINT_PAIRS)
-        return fl_fail(FL_ERR_ARG, "fl_set_neighbour_passes: mode %d is none of %d, %d, %d", mode,
-                       FL_PASSES_PER_POINT, FL_PASSES_CELL_TASKS, FL_PASSES_POINT_PAIRS);
+    if (mode != FL_PASSES_PER_POINT && mode != FL_PASSES_CELL_TASKS && mode != FL_PASSES_POINT_PAIRS &&
+        mode != FL_PASSES_AUTO)
+        return fl_fail(FL_ERR_ARG, "fl_set_neighbour_passes: mode %d is none of %d, %d, %d, %d", mode,
+                       FL_PASSES_PER_POINT, FL_PASSES_CELL_TASKS, FL_PASSES_POINT_PAIRS, FL_PASSES_AUTO);
     FL_CUDA_TRY(cudaStreamSynchronize(s->stream));
     s->passes = mode;
+    s->auto_cells = 0;
     destroy_graph(s);   // the captured step holds the other passes
     return FL_OK;
 }
@@ -1255,6 +1341,13 @@ extern "C" int fl_set_reverse_lists(fl_system *s, int mode) {
 extern "C" int fl_neighbour_passes(const fl_system *s) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_neighbour_passes: null system");
     return s->passes;
+}
+
+extern "C" int fl_neighbour_passes_in_use(fl_system *s) {
+    if (!s) return fl_fail(FL_ERR_ARG, "fl_neighbour_passes_in_use: null system");
+    if (s->passes != FL_PASSES_AUTO) return s->passes;
+    update_auto(s);   // the latest count that has reached the host
+    return s->auto_cells ? FL_PASSES_CELL_TASKS : FL_PASSES_PER_POINT;
 }
 
 extern "C" int fl_launch_shapes(fl_system *s, int *shapes) {

@@ -134,6 +134,12 @@ struct fl_system {
     size_t task_cap;
     uint32_t *task_counters;
     int passes;            // FL_PASSES_*: the neighbour passes of the fused step
+    int auto_cells;        // FL_PASSES_AUTO: the cell tasks are in use (hysteresis state)
+    int graph_cells;       // the captured step pair runs the cell tasks
+    uint32_t *crowd_dev;   // largest in-range cell above 128 points, this step (0: none)
+    uint32_t *crowd_epoch; // device: the state's epoch (bumped when the state is replaced)
+    uint32_t *crowd_host;  // page-locked [count, epoch], sent after each step's sort
+    uint32_t auto_epoch;   // host: the current state's epoch
     int adj_revmode;       // FL_REVERSE_*: how the adjoint finds its reverse pair lists
     int cells_grid[2];     // blocks of the cell-task density and force passes (all resident)
 
@@ -184,7 +190,7 @@ struct fl_system {
     // colours in while the step's first kernels run, and its two events
     // (created on first use)
     cudaStream_t side;
-    cudaEvent_t ev_early, ev_late;
+    cudaEvent_t ev_early, ev_late, ev_crowd, ev_crowd_done;
 
     // per-phase event timing (PERF_PUSH/PERF_POP of Run, cpp:507-515)
     int timing;
@@ -284,6 +290,7 @@ int fl_force_block(const fl_system *s);
 int fl_launch_advance(fl_system *s, float time, float dt, float ss);
 int fl_launch_pack3(fl_system *s, const float4 *src, float *dst, int n, cudaStream_t stream = nullptr);
 int fl_launch_set_time(fl_system *s, int slot, float value);
+int fl_launch_set_word(fl_system *s, uint32_t *word, uint32_t value);
 int fl_launch_unpack3(fl_system *s, const float *src, float4 *dst, int n);
 // up to 4 float3 -> float4 fields in one pass (src[k] may be host-mapped)
 int fl_launch_unpack3_set(fl_system *s, int count, const float *const *src, float4 *const *dst, int n);

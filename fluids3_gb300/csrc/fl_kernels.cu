@@ -122,7 +122,18 @@ struct SortArgs {
     uint32_t *big_cells, *big_count;   // cell entries above 128 points, for k_sort_big
     uint32_t big_cap;
     int gcells;                        // internal cell entries (all scenes, bins included)
+    uint32_t *crowd_max;               // largest in-range cell above 128 points (atomic max)
+    const DevParams *scenes;           // batched: the scene table (bins at cell_base + ncells)
+    const uint16_t *cell_scene;
+    int ncells0;                       // single scene: its bin's entry
 };
+
+// Whether cell entry c is a scene's out-of-range bin.
+__device__ __forceinline__ bool is_bin(const SortArgs &a, int c) {
+    if (!a.scenes) return c == a.ncells0;
+    const DevParams &P = a.scenes[a.cell_scene[c]];
+    return c - P.cell_base == P.ncells;
+}
 
 template <int MODE, int K>
 __device__ __forceinline__ void sort_segment(const SortArgs &a, uint32_t o, uint32_t m) {
@@ -209,6 +220,7 @@ k_sort_cells(const __grid_constant__ SortArgs a) {
         } else if (lane == 0) {
             const uint32_t slot = atomicAdd(a.big_count, 1u);
             if (slot < a.big_cap) a.big_cells[slot] = (uint32_t)(c0 + k);
+            if (!is_bin(a, c0 + k)) atomicMax(a.crowd_max, lm);
         }
     }
 }
@@ -777,6 +789,7 @@ k_force_advance(const __grid_constant__ DevParams P0, const SceneTab T, int n, f
 
 // ---------------------------------------------------------------------------
 __global__ void k_set_time(float *time_dev, float value) { *time_dev = value; }
+__global__ void k_set_word(uint32_t *word, uint32_t value) { *word = value; }
 
 __global__ void k_pack3(int n, const float4 *__restrict__ src, float *__restrict__ dst) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -979,6 +992,10 @@ int fl_launch_sort_cells(fl_system *s, int mode, bool late) {
     a.big_cells = s->big_cells; a.big_count = s->big_count;
     a.big_cap = (uint32_t)fl_big_cells_cap(s->max_points);
     a.gcells = s->gcells;
+    a.crowd_max = s->crowd_dev;
+    a.scenes = s->batched ? s->d_scenes : nullptr;
+    a.cell_scene = s->cell_scene;
+    a.ncells0 = s->ncells;
     if (mode == 0) a.gndx_pre = s->f[F_GNDX].cur<uint32_t>();
     const int bs = s->blk_sort ? s->blk_sort : kThreads;
     const int cells = s->sort_cells ? s->sort_cells : kSortCells;
@@ -1142,6 +1159,12 @@ int fl_launch_advance(fl_system *s, float time, float dt, float ss) {
 int fl_launch_set_time(fl_system *s, int slot, float value) {
     k_set_time<<<1, 1, 0, s->stream>>>(s->time_dev + slot, value);
     FL_LAUNCH_CHECK("set_time");
+    return FL_OK;
+}
+
+int fl_launch_set_word(fl_system *s, uint32_t *word, uint32_t value) {
+    k_set_word<<<1, 1, 0, s->stream>>>(word, value);
+    FL_LAUNCH_CHECK("set_word");
     return FL_OK;
 }
 

@@ -357,7 +357,7 @@ static int run_reverse(fl_system *s, fl_tape *t) {
             if (t->keep_lists) {   // the step's density pass (one that writes pair lists) fills the slot
                 s->hitlist = t->seg_list + (size_t)(k - t0) * t->list_words;
                 s->hitcnt = t->seg_cnt + (size_t)(k - t0) * t->cap;
-                if (s->passes == FL_PASSES_CELL_TASKS) s->passes = FL_PASSES_PER_POINT;
+                if (s->passes == FL_PASSES_CELL_TASKS || s->passes == FL_PASSES_AUTO) s->passes = FL_PASSES_PER_POINT;
             }
             const int r = fl_step_fused(s);
             s->hitlist = own_list;

@@ -69,7 +69,7 @@ def _ptr(a: np.ndarray | None):
 
 
 # fl_set_neighbour_passes modes, by value (FL_PASSES_*)
-PASSES = ("points", "cells", "pairs")
+PASSES = ("points", "cells", "pairs", "auto")
 
 class FluidSystem:
     """One SPH system on the current CUDA device.
@@ -397,16 +397,22 @@ class FluidSystem:
         call("fl_set_launch_shapes", self._h, shapes)
 
     def SetNeighbourPasses(self, mode: str) -> None:
-        """Neighbour passes of the fused step: "points" (default), one thread
-        per point (the reference's loop structure); "cells", one warp per 64
-        points of a cell walks their shared search block in lockstep;
-        "pairs", the per-point passes with a density walk shared by two
-        points of a cell that visit the same candidates (every density pass
-        of the system). Results are bit-identical."""
+        """Neighbour passes of the fused step: "points", one thread per point
+        (the reference's loop structure); "cells", one warp per 64 points of
+        a cell walks their shared search block in lockstep; "pairs", the
+        per-point passes with a density walk shared by two points of a cell
+        that visit the same candidates (every density pass of the system);
+        "auto" (default), "points" until the largest cell reaches 512
+        points, "cells" from then until it falls below 384. Results are
+        bit-identical."""
         call("fl_set_neighbour_passes", self._h, PASSES.index(mode))
 
     def NeighbourPasses(self) -> str:
         return PASSES[call("fl_neighbour_passes", self._h)]
+
+    def NeighbourPassesInUse(self) -> str:
+        """The passes the next fused step takes ("auto" resolved)."""
+        return PASSES[call("fl_neighbour_passes_in_use", self._h)]
 
     # -- timing ---------------------------------------------------------------
     def SetTiming(self, enable: bool) -> None:

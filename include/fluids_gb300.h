@@ -334,8 +334,8 @@ int fl_launch_shapes(fl_system *s, int *shapes);
 int fl_set_launch_shapes(fl_system *s, const int *shapes);
 
 /* Which neighbour passes the fused step (fl_run, fl_run_steps,
- * fl_run_from_host) uses; both give bit-identical densities, forces and
- * states. FL_PASSES_PER_POINT (the default, the faster step): one thread
+ * fl_run_from_host) uses; all give bit-identical densities, forces and
+ * states. FL_PASSES_PER_POINT (the faster step while cells are small): one thread
  * per point walks its own search block (fluids4.0/fluid_kernels.cu:112-149
  * as written) and records its pair list, which the force pass drains.
  * FL_PASSES_CELL_TASKS: one warp per 64 points of a cell walks their shared
@@ -348,13 +348,22 @@ int fl_set_launch_shapes(fl_system *s, const int *shapes);
  * walks the search block once for two points of a cell with the same
  * lower-band bits (which visit the same candidates in the same order); this
  * one holds for every density pass of the system (fused step, phase entry
- * points, tapes). No counterpart in the reference (which has only the
- * per-point walk). */
+ * points, tapes). FL_PASSES_AUTO (the default): the per-point passes until
+ * the largest in-range cell reaches 512 points, the cell tasks from then
+ * until it falls below 384 (each step's sort records the largest cell; a
+ * fused-step call acts on the last value that has reached the host, a
+ * step or two old). No counterpart in the reference (which has only the
+ * per-point walk). fl_neighbour_passes returns the mode set;
+ * fl_neighbour_passes_in_use the passes the next fused step takes
+ * (FL_PASSES_AUTO resolved with the latest count on the host: after
+ * fl_sync, the last step's). */
 #define FL_PASSES_PER_POINT   0
 #define FL_PASSES_CELL_TASKS  1
 #define FL_PASSES_POINT_PAIRS 2
+#define FL_PASSES_AUTO        3
 int fl_set_neighbour_passes(fl_system *s, int mode);
 int fl_neighbour_passes(const fl_system *s);
+int fl_neighbour_passes_in_use(fl_system *s);
 
 /* Wait for the system stream; returns FL_ERR_DEVICE if a kernel raised the
  * device error word since the last fl_sync (bits in *dev_flags if non-NULL). */

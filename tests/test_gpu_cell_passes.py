@@ -5,8 +5,9 @@ shared search block once per 64 of its points, in lockstep, and evaluates
 the hits pair-parallel; the adjoint's rebuilt steps take their pair lists
 from the cell-task density. With FL_PASSES_POINT_PAIRS (fl_pairs.cu) every
 density pass walks the search block once for two points of a cell with the
-same lower-band bits. Every point's sums keep the reference's terms and
-order, so all give bit-identical states: checked over many steps on the
+same lower-band bits. FL_PASSES_AUTO switches between the per-point and
+cell-task passes by the largest cell. Every point's sums keep the
+reference's terms and order, so all give bit-identical states: checked over many steps on the
 wave tank, on crowded cells (tasks of one cell split over many warps,
 unions of thousands of candidates, groups past the pair-parallel cap; runs
 of hundreds of equal points split over blocks of 1024 slots), on cells of
@@ -30,7 +31,7 @@ pytestmark = pytest.mark.gpu
 UNDEF = 0xFFFFFFFF
 
 
-ALTS = pytest.mark.parametrize("alt", ["cells", "pairs"])
+ALTS = pytest.mark.parametrize("alt", ["cells", "pairs", "auto"])
 
 
 def run_both(params, pos, vel, veval, clr, steps, graph=True, alt="cells"):
@@ -94,7 +95,7 @@ def test_alt_matches_the_oracle_step_by_step(alt):
     p = sc.params
     with F.FluidSystem(p, sc.n) as s:
         s.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
-        assert s.NeighbourPasses() == "points"   # the default
+        assert s.NeighbourPasses() == "auto"   # the default
         s.SetNeighbourPasses(alt)
         s.RunSteps(40)
         s.Sync()
@@ -221,3 +222,48 @@ def test_pairs_through_the_phase_entry_points(n):
             s.Sync()
             out[mode] = s.state()
     assert_states_equal(out["points"], out["pairs"], f"phase sequence, n={n}")
+
+
+def test_auto_switches_to_cell_tasks_when_a_cell_crowds_and_back():
+    """FL_PASSES_AUTO: the per-point passes while every cell is small, the
+    cell tasks once the largest in-range cell passes 512 points (acting on
+    the count a step or two late), the per-point passes again below 384;
+    points out of range (the bin) do not count. The states equal the
+    per-point passes' at every stage."""
+    sc = scenes.dam_break(n=8000, seed=71)
+    p = sc.params
+    rng = np.random.default_rng(72)
+    crowded = sc.pos.copy()
+    c = np.array([p.gridMin[0] + 7.5 * 5.0, p.gridMin[1] + 5.5 * 5.0, p.gridMin[2] + 6.5 * 5.0], np.float32)
+    crowded[:1500] = c + rng.uniform(-2.4, 2.4, size=(1500, 3)).astype(np.float32)
+    escaped = sc.pos.copy()
+    escaped[:2000] = (-500.0, 1.0, 1.0)
+    for name, pos, want in (("small cells", sc.pos, "points"), ("escaped", escaped, "points"),
+                            ("crowded", crowded, "cells")):
+        out = {}
+        for mode in ("points", "auto"):
+            with F.FluidSystem(p, sc.n) as s:
+                s.SetParticles(pos, sc.vel, sc.veval, clr=sc.clr)
+                s.SetNeighbourPasses(mode)
+                s.RunSteps(3)
+                s.Sync()
+                for _ in range(2):   # the recorded count reaches the host
+                    s.Run()
+                s.Sync()
+                if mode == "auto":
+                    assert s.NeighbourPassesInUse() == want, name
+                s.RunSteps(6)   # graph replays in the selected passes
+                s.Sync()
+                out[mode] = s.state()
+        assert_states_equal(out["points"], out["auto"], name)
+    # back to the per-point passes once the crowd is gone
+    with F.FluidSystem(p, sc.n) as s:
+        s.SetParticles(crowded, sc.vel, sc.veval, clr=sc.clr)
+        s.RunSteps(3)
+        s.Run(); s.Run(); s.Sync()
+        assert s.NeighbourPassesInUse() == "cells"
+        s.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
+        for _ in range(4):
+            s.Run()
+        s.Sync()
+        assert s.NeighbourPassesInUse() == "points"
