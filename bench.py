@@ -85,7 +85,8 @@ def parse():
     ap.add_argument("--segment", type=int, default=50,
                     help="timed steps run as rollouts of at most this many steps from the warm state")
     ap.add_argument("--long-steps", type=int, default=300,
-                    help="also time this many continuous steps from the warm state, per 100-step run")
+                    help="also time this many continuous steps from the warm state, per --long-chunk-step run")
+    ap.add_argument("--long-chunk", type=int, default=100, help="steps per timed run of --long-steps")
     ap.add_argument("--e2e-steps", type=int, default=None, help="steps in the e2e region (default: min(K, 20))")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -770,7 +771,7 @@ def our_arm(args, rank, world, local_rank):
     long_run = None
     if args.long_steps > 0:
         s.RestoreCheckpoint(0)
-        long_run = continuous_profile(s, args.long_steps)
+        long_run = continuous_profile(s, args.long_steps, args.long_chunk)
 
     # -- per-kernel times: the same K steps again from the saved state, eager,
     #    each launch bracketed by CUDA events

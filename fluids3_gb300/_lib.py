@@ -65,6 +65,7 @@ SIGNATURES = [
     ("fl_test_scan_noalloc_timeout", C.c_int, [vp, vp, C.c_int, vp, C.c_int, vp]),
     ("fl_set_reverse_lists", C.c_int, [vp, C.c_int]),
     ("fl_neighbour_passes_in_use", C.c_int, [vp]),
+    ("fl_passes_steps", C.c_int, [vp, C.POINTER(C.c_int64)]),
     ("fl_batch_get_params", C.c_int, [vp, C.c_int, C.POINTER(FlParams)]),
     ("fl_batch_set_params", C.c_int, [vp, C.c_int, C.POINTER(FlParams)]),
     ("fl_add_particles", C.c_int, [vp, C.c_int, vp, vp, vp, vp]),

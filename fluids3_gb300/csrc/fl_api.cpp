@@ -178,6 +178,8 @@ static void free_all(fl_system *s) {
     if (s->ev_late) cudaEventDestroy(s->ev_late);
     if (s->ev_crowd) cudaEventDestroy(s->ev_crowd);
     if (s->ev_crowd_done) cudaEventDestroy(s->ev_crowd_done);
+    for (int k = 0; k < 2; k++)
+        if (s->ev_auto[k]) cudaEventDestroy(s->ev_auto[k]);
     cudaFree(s->crowd_epoch);
     if (s->side) cudaStreamDestroy(s->side);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -949,6 +951,7 @@ static int run_step(fl_system *s, TimingState *t) {
     FL_TRY(send_crowd(s));
     flip(s, F_POS); flip(s, F_VEL); flip(s, F_VEVAL); flip(s, F_CLR); flip(s, F_GCELL); flip(s, F_GNDX);
     const bool cells = use_cell_passes(s, taped);
+    if (!s->capturing) s->passes_steps[cells ? 1 : 0]++;
     if (cells) FL_TRY(fl_launch_make_tasks(s));
     FL_TRY(record(s, t, 4));
     FL_TRY(cells ? fl_launch_density_cells(s) : fl_launch_density(s));
@@ -1066,6 +1069,8 @@ static int ensure_side(fl_system *s) {
     if (!s->ev_late) FL_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_late, cudaEventDisableTiming));
     if (!s->ev_crowd) FL_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_crowd, cudaEventDisableTiming));
     if (!s->ev_crowd_done) FL_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_crowd_done, cudaEventDisableTiming));
+    for (int k = 0; k < 2; k++)
+        if (!s->ev_auto[k]) FL_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_auto[k], cudaEventDisableTiming));
     return FL_OK;
 }
 
@@ -1144,8 +1149,10 @@ static int capture_pair(fl_system *s) {
     const int slot = s->time_slot;
     cudaGraph_t g = nullptr;
     FL_CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    s->capturing = 1;
     int r = run_step(s, nullptr);
     if (r == FL_OK) r = run_step(s, nullptr);
+    s->capturing = 0;
     cudaError_t e = cudaStreamEndCapture(s->stream, &g);
     for (int k = 0; k < F_COUNT; k++) s->f[k].live = live[k];
     s->time_slot = slot;
@@ -1163,6 +1170,13 @@ static int capture_pair(fl_system *s) {
     return FL_OK;
 }
 
+static int run_steps_graph(fl_system *s, int nsteps);
+
+// With FL_PASSES_AUTO a long call runs in chunks of kAutoChunk steps, each
+// chunk's passes chosen from the counts of the chunk two before it (waited
+// for, so one chunk stays queued and the GPU never idles).
+constexpr int kAutoChunk = 32;
+
 extern "C" int fl_run_steps(fl_system *s, int nsteps) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_run_steps: null system");
     if (nsteps < 0) return fl_fail(FL_ERR_ARG, "fl_run_steps: nsteps < 0");
@@ -1170,6 +1184,19 @@ extern "C" int fl_run_steps(fl_system *s, int nsteps) {
         for (int k = 0; k < nsteps; k++) FL_TRY(fl_run(s));
         return FL_OK;
     }
+    if (s->passes != FL_PASSES_AUTO || nsteps <= kAutoChunk) return run_steps_graph(s, nsteps);
+    int left = nsteps;
+    for (int k = 0; left > 0; k++) {
+        const int c = left < kAutoChunk ? left : kAutoChunk;
+        if (k >= 2) FL_CUDA_TRY(cudaEventSynchronize(s->ev_auto[k & 1]));
+        FL_TRY(run_steps_graph(s, c));
+        FL_CUDA_TRY(cudaEventRecord(s->ev_auto[k & 1], s->stream));
+        left -= c;
+    }
+    return FL_OK;
+}
+
+static int run_steps_graph(fl_system *s, int nsteps) {
     update_auto(s);
     const int pairs = nsteps / 2;
     if (pairs > 0) {
@@ -1178,6 +1205,7 @@ extern "C" int fl_run_steps(fl_system *s, int nsteps) {
         if (!match) FL_TRY(capture_pair(s));
         FL_TRY(begin_run(s));
         for (int p = 0; p < pairs; p++) FL_CUDA_TRY(cudaGraphLaunch(s->graph_exec, s->stream));
+        s->passes_steps[s->graph_cells ? 1 : 0] += 2 * (int64_t)pairs;
         s->time_host_valid = 0;   // the device slot now holds the time
         s->have_insert = 0;
         s->have_offsets = 1;
@@ -1341,6 +1369,13 @@ extern "C" int fl_set_reverse_lists(fl_system *s, int mode) {
 extern "C" int fl_neighbour_passes(const fl_system *s) {
     if (!s) return fl_fail(FL_ERR_ARG, "fl_neighbour_passes: null system");
     return s->passes;
+}
+
+extern "C" int fl_passes_steps(const fl_system *s, int64_t *counts) {
+    if (!s || !counts) return fl_fail(FL_ERR_ARG, "fl_passes_steps: null argument");
+    counts[0] = s->passes_steps[0];
+    counts[1] = s->passes_steps[1];
+    return FL_OK;
 }
 
 extern "C" int fl_neighbour_passes_in_use(fl_system *s) {

@@ -136,6 +136,8 @@ struct fl_system {
     int passes;            // FL_PASSES_*: the neighbour passes of the fused step
     int auto_cells;        // FL_PASSES_AUTO: the cell tasks are in use (hysteresis state)
     int graph_cells;       // the captured step pair runs the cell tasks
+    int capturing;         // run_step is being captured into the step-pair graph
+    int64_t passes_steps[2]; // fused steps issued with the per-point passes / the cell tasks
     uint32_t *crowd_dev;   // largest in-range cell above 128 points, this step (0: none)
     uint32_t *crowd_epoch; // device: the state's epoch (bumped when the state is replaced)
     uint32_t *crowd_host;  // page-locked [count, epoch], sent after each step's sort
@@ -190,7 +192,7 @@ struct fl_system {
     // colours in while the step's first kernels run, and its two events
     // (created on first use)
     cudaStream_t side;
-    cudaEvent_t ev_early, ev_late, ev_crowd, ev_crowd_done;
+    cudaEvent_t ev_early, ev_late, ev_crowd, ev_crowd_done, ev_auto[2];
 
     // per-phase event timing (PERF_PUSH/PERF_POP of Run, cpp:507-515)
     int timing;

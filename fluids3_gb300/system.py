@@ -414,6 +414,13 @@ class FluidSystem:
         """The passes the next fused step takes ("auto" resolved)."""
         return PASSES[call("fl_neighbour_passes_in_use", self._h)]
 
+    def PassesSteps(self) -> tuple:
+        """Fused steps issued so far with the per-point passes and with the
+        cell tasks."""
+        c = (C.c_int64 * 2)()
+        call("fl_passes_steps", self._h, c)
+        return int(c[0]), int(c[1])
+
     # -- timing ---------------------------------------------------------------
     def SetTiming(self, enable: bool) -> None:
         call("fl_set_timing", self._h, 1 if enable else 0)

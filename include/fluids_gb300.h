@@ -364,6 +364,9 @@ int fl_set_launch_shapes(fl_system *s, const int *shapes);
 int fl_set_neighbour_passes(fl_system *s, int mode);
 int fl_neighbour_passes(const fl_system *s);
 int fl_neighbour_passes_in_use(fl_system *s);
+/* Fused steps issued since creation with the per-point passes (counts[0])
+ * and with the cell tasks (counts[1]) -- what FL_PASSES_AUTO chose. */
+int fl_passes_steps(const fl_system *s, int64_t *counts);
 
 /* Wait for the system stream; returns FL_ERR_DEVICE if a kernel raised the
  * device error word since the last fl_sync (bits in *dev_flags if non-NULL). */

@@ -267,3 +267,31 @@ def test_auto_switches_to_cell_tasks_when_a_cell_crowds_and_back():
             s.Run()
         s.Sync()
         assert s.NeighbourPassesInUse() == "points"
+
+
+def test_auto_switches_within_one_long_call():
+    """One RunSteps call of 100 steps with FL_PASSES_AUTO runs in chunks of
+    32 steps, each chunk's passes chosen from the counts of the chunk two
+    before it: a crowd that forms switches the call to the cell tasks
+    midway, with the per-point passes' states."""
+    sc = scenes.dam_break(n=8000, seed=73)
+    p = sc.params
+    rng = np.random.default_rng(74)
+    pos = sc.pos.copy()
+    c = np.array([p.gridMin[0] + 7.5 * 5.0, p.gridMin[1] + 5.5 * 5.0, p.gridMin[2] + 6.5 * 5.0], np.float32)
+    pos[:3000] = c + rng.uniform(-2.4, 2.4, size=(3000, 3)).astype(np.float32)
+    out = {}
+    for mode in ("points", "auto"):
+        with F.FluidSystem(p, sc.n) as s:
+            s.SetParticles(pos, sc.vel, sc.veval, clr=sc.clr)
+            s.SetNeighbourPasses(mode)
+            before = s.PassesSteps()
+            s.RunSteps(100)
+            s.Sync()
+            points_steps, cell_steps = (a - b for a, b in zip(s.PassesSteps(), before))
+            assert points_steps + cell_steps == 100
+            if mode == "auto":   # the call began with the per-point passes and switched
+                assert points_steps >= 32 and cell_steps >= 32, (points_steps, cell_steps)
+            assert s.IntegrityCheck() == 0
+            out[mode] = s.state()
+    assert_states_equal(out["points"], out["auto"], "100 steps in one call")
