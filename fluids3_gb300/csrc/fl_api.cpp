@@ -951,6 +951,7 @@ static int run_step(fl_system *s, TimingState *t) {
     FL_TRY(send_crowd(s));
     flip(s, F_POS); flip(s, F_VEL); flip(s, F_VEVAL); flip(s, F_CLR); flip(s, F_GCELL); flip(s, F_GNDX);
     const bool cells = use_cell_passes(s, taped);
+    s->last_step_cells = cells;
     if (!s->capturing) s->passes_steps[cells ? 1 : 0]++;
     if (cells) FL_TRY(fl_launch_make_tasks(s));
     FL_TRY(record(s, t, 4));
@@ -1042,6 +1043,8 @@ static int run_step_late(fl_system *s, const float *vel3, const float *veval3, c
     FL_TRY(send_crowd(s));
     flip(s, F_POS); flip(s, F_VEL); flip(s, F_VEVAL); flip(s, F_CLR); flip(s, F_GCELL); flip(s, F_GNDX);
     const bool cells = use_cell_passes(s, false);
+    s->last_step_cells = cells;
+    s->passes_steps[cells ? 1 : 0]++;
     if (cells) FL_TRY(fl_launch_make_tasks(s));
     FL_TRY(cells ? fl_launch_density_cells(s) : fl_launch_density(s));
     FL_CUDA_TRY(cudaStreamWaitEvent(s->stream, s->ev_late, 0));
@@ -1166,6 +1169,7 @@ static int capture_pair(fl_system *s) {
     }
     s->graph_steps = 2;
     s->graph_cells = (int)cells_selected(s);
+    s->graph_ran_cells = s->last_step_cells;
     for (int k = 0; k < F_COUNT; k++) s->graph_live[k] = live[k];
     return FL_OK;
 }
@@ -1205,7 +1209,7 @@ static int run_steps_graph(fl_system *s, int nsteps) {
         if (!match) FL_TRY(capture_pair(s));
         FL_TRY(begin_run(s));
         for (int p = 0; p < pairs; p++) FL_CUDA_TRY(cudaGraphLaunch(s->graph_exec, s->stream));
-        s->passes_steps[s->graph_cells ? 1 : 0] += 2 * (int64_t)pairs;
+        s->passes_steps[s->graph_ran_cells ? 1 : 0] += 2 * (int64_t)pairs;
         s->time_host_valid = 0;   // the device slot now holds the time
         s->have_insert = 0;
         s->have_offsets = 1;

@@ -137,6 +137,8 @@ struct fl_system {
     int auto_cells;        // FL_PASSES_AUTO: the cell tasks are in use (hysteresis state)
     int graph_cells;       // the captured step pair runs the cell tasks
     int capturing;         // run_step is being captured into the step-pair graph
+    int last_step_cells;   // the last issued (or captured) step took the cell tasks
+    int graph_ran_cells;   // the captured step pair takes the cell tasks
     int64_t passes_steps[2]; // fused steps issued with the per-point passes / the cell tasks
     uint32_t *crowd_dev;   // largest in-range cell above 128 points, this step (0: none)
     uint32_t *crowd_epoch; // device: the state's epoch (bumped when the state is replaced)

@@ -295,3 +295,23 @@ def test_auto_switches_within_one_long_call():
             assert s.IntegrityCheck() == 0
             out[mode] = s.state()
     assert_states_equal(out["points"], out["auto"], "100 steps in one call")
+
+
+def test_passes_and_reverse_list_modes_reject_unknown_values():
+    sc = scenes.dam_break(n=500)
+    lib = F.lib()
+    with F.FluidSystem(sc.params, sc.n) as s:
+        for bad in (-1, 4, 99):
+            assert lib.fl_set_neighbour_passes(s.handle, bad) == -1          # FL_ERR_ARG
+            assert lib.fl_set_reverse_lists(s.handle, bad if bad != 4 else 3) == -1
+        assert s.NeighbourPasses() == "auto"
+        assert s.PassesSteps() == (0, 0)
+        s.SetParticles(sc.pos, sc.vel, sc.veval, clr=sc.clr)
+        s.RunSteps(3)
+        s.Sync()
+        assert s.PassesSteps() == (3, 0)
+        s.SetNeighbourPasses("cells")
+        s.RunSteps(2)
+        s.Sync()
+        assert s.PassesSteps() == (3, 2)
+        assert s.NeighbourPassesInUse() == "cells"
