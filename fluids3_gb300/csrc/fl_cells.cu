@@ -1,6 +1,6 @@
-// Cell-task neighbour passes of the fused step (FL_PASSES_CELL_TASKS;
-// gridSrch 2, band codes set), and the cell-task density of the adjoint's
-// rebuilt steps.
+// Cell-task neighbour passes of the fused step (FL_PASSES_CELL_TASKS, and
+// FL_PASSES_AUTO once a cell crowds; gridSrch 2, band codes set), and the
+// cell-task density of the adjoint's rebuilt steps.
 //
 // computePressure and computeForce (fluids4.0/fluid_kernels.cu:112-149,
 // 180-217) walk, for every point, the 2x2x2 search block c-1..c of its cell
