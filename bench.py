@@ -5,7 +5,9 @@ Workload (N=1): the 4,000,000-point wave tank -- a jittered lattice filling
 the low-x 40% of a ~330-unit box, dam-break parameters (h = 0.01 m, cell 2h,
 gridSrch 2), X- wall forcing at frequency 0.2 and amplitude 0.3. One step
 is one full Run: insert, scan, index scatter, canonical cell sort (and the
-crowded-cell sort), gather, density, force + advance (eight kernels).
+crowded-cell sort), gather, density, force + advance (eight kernels; the
+neighbour passes per --passes, by default switching from the per-point to
+the cell-task passes once a cell crowds past 512 points).
 
   value   device-timed throughput, state resident in HBM, graph replay of
           exactly K steps between CUDA events on the system stream, run as
@@ -19,8 +21,8 @@ crowded-cell sort), gather, density, force + advance (eight kernels).
   e2e     the same metric through the public C ABI with host buffers: per
           step one fl_run_from_host call -- the step's inputs uploaded from
           pinned host memory (all but the positions on a copy engine during
-          the step's first kernels), the step, and the new positions read
-          back into pinned host memory (in slot ranges during the force pass)
+          the step's first kernels), the step, and the new positions written
+          into pinned host memory by the force pass itself
   roofline  the dominant kernel's algorithmic bytes per launch / its mean
           launch time (per-phase CUDA events over a second K-step region)
   cpu_baseline  the reference's CPU path (the reference kernels built for the
@@ -29,6 +31,8 @@ crowded-cell sort), gather, density, force + advance (eight kernels).
           sm_103a with its build's flags, driven as its Run drives them) on
           the same workload, state and segment protocol as value
 
+  long_continuous  --long-steps continuous steps from the warm state, timed
+          per --long-chunk-step run, with the largest cell after each
   batched  256 scenes stepped as one batched system vs one at a time
   adjoint  adjoint/forward time per step: the differentiated 65,536-point
           rollout (checkpointed and every-step tapes, their device memory)
