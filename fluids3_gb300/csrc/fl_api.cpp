@@ -886,9 +886,11 @@ static bool use_cell_passes(const fl_system *s, bool taped) {
 }
 
 // FL_PASSES_AUTO: measured on GB300 (4M-point wave tank, 10-step runs as it
-// clumps), the cell tasks overtake the per-point passes once the largest
-// cell holds about 450-490 points (15% more time per step at 396, 4% less
-// at 489, 15-25% less from 581 to 13,144). Every step's sort records the
+// clumps, the largest cell read after each run), the cell tasks take 1.19x
+// the per-point step time by a largest cell of 489, 1.04x at 581, 0.91x at
+// 691 and 0.75-0.86x from 789 to 14,935 points (1.69x at the start, 61).
+// The cells grow during a run, so the switch sits a little below where the
+// run-end figures cross. Every step's sort records the
 // largest in-range cell above 128 points and sends it to page-locked host
 // memory; the next call reads whatever copy has arrived (a step or two
 // old, no wait) and switches with hysteresis. The passes give identical
