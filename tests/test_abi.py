@@ -180,3 +180,27 @@ def test_reference_arm_loads_no_product_library():
     line = json.loads([l for l in out.stdout.splitlines() if l.startswith("{")][-1])
     assert line["impl"] == "reference" and line["value"] > 0
     assert "PRODUCT_NOT_LOADED" in out.stdout
+
+
+def header_defines(prefix: str) -> dict[str, int]:
+    out = {}
+    for h in HEADERS:
+        for m in re.finditer(rf"^#define\s+({prefix}[A-Z_0-9]*)\s+\(?(\d+)", h.read_text(), re.M):
+            out[m.group(1)] = int(m.group(2))
+    return out
+
+
+def test_python_mode_names_follow_the_header_values():
+    """SetNeighbourPasses / NeighbourPasses index system.PASSES by the
+    FL_PASSES_* values: the names must sit at those values."""
+    from fluids3_gb300 import system
+    passes = header_defines("FL_PASSES_")
+    assert passes == {"FL_PASSES_PER_POINT": 0, "FL_PASSES_CELL_TASKS": 1, "FL_PASSES_POINT_PAIRS": 2,
+                      "FL_PASSES_AUTO": 3}
+    names = {"FL_PASSES_PER_POINT": "points", "FL_PASSES_CELL_TASKS": "cells",
+             "FL_PASSES_POINT_PAIRS": "pairs", "FL_PASSES_AUTO": "auto"}
+    for define, value in passes.items():
+        assert system.PASSES[value] == names[define]
+    reverse = header_defines("FL_REVERSE_")
+    assert reverse["FL_REVERSE_AUTO"] == 0 and reverse["FL_REVERSE_WALK"] == 1
+    assert reverse["FL_REVERSE_TRANSPOSE"] == 2
